@@ -1,0 +1,65 @@
+# Test infrastructure: builds the UNMODIFIED reference (spaceauk/AMR2D_MHD)
+# from its sources where they lie, plus oracle/ref_hook.cpp, into oracle/_ref/.
+# Nothing is copied: the only generated source is defs.hpp with `maxlevs`
+# replaced (it is a compile-time constant in the reference, defs.hpp:28), and
+# `-I-` makes the compiler pick that header instead of the one beside the
+# sources (likewise `nghosts`, defs.hpp:27, which WENO5 needs at 4).  main.cpp is compiled with two renames (see ref_hook.cpp).
+#
+#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=shipped   # makefile:9-13 flags
+#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=nofma     # same + -ffp-contract=off
+#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=omp       # same as shipped + USE_OMP
+#
+# The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>/main.x; run it in a directory
+# holding input.txt with stdin "2\n0\n" (main.cpp:188,388).
+
+REF     ?= /root/reference
+MAXLEVS ?= 5
+NGHOSTS ?= 2
+FLAVOR  ?= shipped
+HERE    := $(dir $(lastword $(MAKEFILE_LIST)))
+OUT     := $(HERE)_ref/L$(MAXLEVS)_G$(NGHOSTS)_$(FLAVOR)
+
+CXX     ?= g++
+# makefile:9-13 of the reference
+CFLAGS  := -O3 -std=c++17 -march=native -funroll-loops -g -DDOUBLE_PREC -w
+LFLAGS  :=
+ifeq ($(FLAVOR),nofma)
+CFLAGS  += -ffp-contract=off
+endif
+ifeq ($(FLAVOR),omp)
+CFLAGS  += -fopenmp -DOPENMP
+LFLAGS  += -fopenmp
+endif
+
+# every reference translation unit except savedata.cpp (text output, replaced
+# by the hook's no-op) and main.cpp (built with renames below)
+SRCS := meshblock IC2Dtype MUSCL2D slopelimiter celledges riemannS \
+        WENO2D_primvar parameters diffusivity timeIntegral basegrid \
+        locate_bounds boundary extboundary markref criteria critneighup \
+        critneighdown refine coarsen updatelpup updatelpdown admesh misc \
+        CT2D refineBi_CT coarsenBi_CT boundaryfc boundaryec
+OBJS := $(addprefix $(OUT)/,$(addsuffix .o,$(SRCS))) $(OUT)/main.o $(OUT)/ref_hook.o
+INC  := -I- -I$(OUT) -I$(REF)
+
+all: $(OUT)/main.x
+
+$(OUT)/defs.hpp: $(REF)/defs.hpp
+	@mkdir -p $(OUT)
+	sed -e 's/^const int maxlevs=5;/const int maxlevs=$(MAXLEVS);/' \
+	    -e 's/^const int nghosts=2; /const int nghosts=$(NGHOSTS); /' $< > $@
+	@grep -q 'const int maxlevs=$(MAXLEVS);' $@ || (echo "maxlevs patch failed" && rm -f $@ && false)
+	@grep -q 'const int nghosts=$(NGHOSTS); ' $@ || (echo "nghosts patch failed" && rm -f $@ && false)
+
+$(OUT)/%.o: $(REF)/%.cpp $(OUT)/defs.hpp
+	$(CXX) -c $(CFLAGS) $(INC) $< -o $@
+
+$(OUT)/main.o: $(REF)/main.cpp $(OUT)/defs.hpp
+	$(CXX) -c $(CFLAGS) $(INC) -Dadmesh=amr_ref_admesh_hook -Dsave4py=amr_ref_save4py $< -o $@
+
+$(OUT)/ref_hook.o: $(HERE)ref_hook.cpp $(OUT)/defs.hpp
+	$(CXX) -c $(CFLAGS) $(INC) $< -o $@
+
+$(OUT)/main.x: $(OBJS)
+	$(CXX) $(LFLAGS) $(OBJS) -o $@
+
+.PHONY: all
