@@ -1,0 +1,229 @@
+"""amr2d_mhd_gb300 — GB300 (sm_103a) per-block finite-volume update of a 2-D
+block-structured AMR ideal-MHD solver, drop-in for the hot path of
+spaceauk/AMR2D_MHD.
+
+The compute path is the CUDA library libamr2d_mhd.so (C ABI in
+include/amr2d_mhd.h); this module is a thin ctypes mirror of it.  There is no
+CPU fallback: if the library is missing or no GPU is present the calls fail
+with AmrError.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["AmrError", "Config", "Simulation", "load", "FIELDS", "STATUS"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIELDS = dict(U=0, Us=1, Bi=2, Bis=3, ff=4, gg=5, EMF=6, W=7)
+STATUS = {0: "AMR_OK", -1: "AMR_E_CONFIG", -2: "AMR_E_CUDA", -3: "AMR_E_OOM", -4: "AMR_E_MAXBLOCKS",
+          -5: "AMR_E_PRESSURE", -6: "AMR_E_NAN", -7: "AMR_E_DT", -8: "AMR_E_HLLC", -9: "AMR_E_STATE",
+          -10: "AMR_E_TIMEOUT", -11: "AMR_E_UNSUPPORTED", -12: "AMR_E_ARG"}
+
+# every entry point declared in include/amr2d_mhd.h
+EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_abi_version", "amr_status_string",
+           "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
+           "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
+           "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
+           "amr_upload"]
+
+
+class AmrError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__("%s (%d): %s" % (STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+                ("nvar", ctypes.c_int32), ("lenx", ctypes.c_double), ("leny", ctypes.c_double),
+                ("cfl", ctypes.c_double), ("ic", ctypes.c_char * 16), ("limiter", ctypes.c_char * 16),
+                ("flux", ctypes.c_char * 16), ("maxlevs", ctypes.c_int32), ("nghosts", ctypes.c_int32),
+                ("nroots_x", ctypes.c_int32), ("nroots_y", ctypes.c_int32), ("periodic", ctypes.c_int32),
+                ("geometry", ctypes.c_int32), ("gamma", ctypes.c_double), ("t_end", ctypes.c_double),
+                ("ic_param", ctypes.c_double * 24), ("precision", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 7)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_double), ("dt", ctypes.c_double), ("dt_next", ctypes.c_double),
+                ("t_end", ctypes.c_double), ("gamma", ctypes.c_double), ("steps", ctypes.c_int64),
+                ("last_active", ctypes.c_int32), ("n_leaves", ctypes.c_int32), ("nb_leafs", ctypes.c_int32),
+                ("done", ctypes.c_int32), ("n_instances", ctypes.c_int32), ("nx_tot", ctypes.c_int32),
+                ("ny_tot", ctypes.c_int32), ("cell_updates", ctypes.c_int64)]
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libamr2d_mhd.so (building it when the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise ImportError("libamr2d_mhd.so is not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    vp, i32, i64, dp = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p
+    sig = {
+        "amr_config_default": (None, [ctypes.POINTER(Config)]),
+        "amr_config_from_input": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Config)]),
+        "amr_abi_version": (ctypes.c_int, []),
+        "amr_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+        "amr_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(vp)]),
+        "amr_create_batch": (ctypes.c_int, [ctypes.POINTER(Config), i32, ctypes.POINTER(vp)]),
+        "amr_destroy": (ctypes.c_int, [vp]),
+        "amr_set_stream": (ctypes.c_int, [vp, vp]),
+        "amr_last_error": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t]),
+        "amr_init": (ctypes.c_int, [vp]),
+        "amr_step": (ctypes.c_int, [vp]),
+        "amr_run": (ctypes.c_int, [vp, i64]),
+        "amr_get_info": (ctypes.c_int, [vp, i32, ctypes.POINTER(Info)]),
+        "amr_locate_bounds": (ctypes.c_int, [vp]),
+        "amr_boundary": (ctypes.c_int, [vp, i32]),
+        "amr_muscl2d_rk": (ctypes.c_int, [vp, i32]),
+        "amr_ct2d": (ctypes.c_int, [vp, i32]),
+        "amr_cfl_dt": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+        "amr_admesh": (ctypes.c_int, [vp]),
+        "amr_get_tree": (ctypes.c_int, [vp, i32, dp, dp, dp, i32]),
+        "amr_download": (ctypes.c_int, [vp, i32, i32, dp, i64]),
+        "amr_upload": (ctypes.c_int, [vp, i32, i32, dp, i64]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def make_config(ic="rotor", limiter="MC", flux="RUSA", cfl=0.5, maxlevs=5, nghosts=2, nroots=(2, 2),
+                periodic=False, geometry=0, gamma=0.0, t_end=0.0, ic_param=None, precision="fp64",
+                lenx=1.0, leny=1.0, nx=16, ny=16, input_txt=None) -> Config:
+    """An amr_config; defaults are the reference's input.txt and defs.hpp."""
+    L = load()
+    c = Config()
+    L.amr_config_default(ctypes.byref(c))
+    if input_txt is not None:
+        rc = L.amr_config_from_input(os.fsencode(input_txt), ctypes.byref(c))
+        if rc:
+            raise AmrError(rc, "cannot read %s" % input_txt)
+    else:
+        c.nx, c.ny, c.lenx, c.leny, c.cfl = nx, ny, lenx, leny, cfl
+        c.ic, c.limiter, c.flux = ic.encode(), limiter.encode(), flux.encode()
+    c.maxlevs, c.nghosts = maxlevs, nghosts
+    c.nroots_x, c.nroots_y = nroots
+    c.periodic, c.geometry = int(periodic), int(geometry)
+    c.gamma, c.t_end = gamma, t_end
+    for i, v in enumerate(ic_param or []):
+        c.ic_param[i] = v
+    c.precision = {"fp64": 0, "fp32": 1}[precision]
+    return c
+
+
+class Simulation:
+    """One handle: an AMR problem (or a batch of them) resident on the GPU.
+
+    The methods mirror the reference's seam: init() is basegrid + IC2Dtype +
+    the initial admesh, step() one iteration of main.cpp's time loop, and
+    boundary / MUSCL2D / CT2D / cfl_dt / admesh the individual calls.
+    """
+
+    def __init__(self, configs=None, **kw):
+        L = load()
+        if configs is None:
+            configs = [make_config(**kw)]
+        elif isinstance(configs, Config):
+            configs = [configs]
+        arr = (Config * len(configs))(*configs)
+        h = ctypes.c_void_p()
+        rc = L.amr_create_batch(arr, len(configs), ctypes.byref(h))
+        if rc:
+            raise AmrError(rc, "amr_create failed")
+        self.h = h
+        self.n = len(configs)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().amr_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _ck(self, rc):
+        if rc:
+            buf = ctypes.create_string_buffer(512)
+            load().amr_last_error(self.h, buf, 512)
+            raise AmrError(rc, buf.value.decode(errors="replace"))
+
+    def init(self):
+        self._ck(load().amr_init(self.h))
+        return self
+
+    def step(self):
+        self._ck(load().amr_step(self.h))
+
+    def run(self, max_steps=-1):
+        self._ck(load().amr_run(self.h, max_steps))
+
+    def info(self, instance=0):
+        inf = Info()
+        self._ck(load().amr_get_info(self.h, instance, ctypes.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in Info._fields_}
+
+    # reference-function entry points
+    def locate_bounds(self):
+        self._ck(load().amr_locate_bounds(self.h))
+
+    def boundary(self, field):
+        self._ck(load().amr_boundary(self.h, FIELDS[field]))
+
+    def MUSCL2D(self, step):
+        self._ck(load().amr_muscl2d_rk(self.h, step))
+
+    def CT2D(self, step):
+        self._ck(load().amr_ct2d(self.h, step))
+
+    def cfl_dt(self):
+        v = ctypes.c_double()
+        self._ck(load().amr_cfl_dt(self.h, ctypes.byref(v)))
+        return v.value
+
+    def admesh(self):
+        self._ck(load().amr_admesh(self.h))
+
+    # state exchange
+    def tree(self, instance=0):
+        na = self.info(instance)["last_active"]
+        lp = np.zeros((na, 8), np.int32)
+        ic = np.zeros((na, 2), np.int32)
+        lf = np.zeros(na, np.uint8)
+        self._ck(load().amr_get_tree(self.h, instance, lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, na))
+        return lp, ic, lf.astype(bool)
+
+    def download(self, field, instance=0):
+        inf = self.info(instance)
+        nv = {"Bi": 2, "Bis": 2, "EMF": 1}.get(field, 8)
+        n = inf["nx_tot"]
+        a = np.empty((inf["last_active"], nv, n, n), np.float64)
+        self._ck(load().amr_download(self.h, instance, FIELDS[field], a.ctypes.data, a.size))
+        return a
+
+    def upload(self, field, arr, instance=0):
+        a = np.ascontiguousarray(arr, np.float64)
+        self._ck(load().amr_upload(self.h, instance, FIELDS[field], a.ctypes.data, a.size))
+
+    def state(self, instance=0):
+        """Dict in the form the oracle's state() returns."""
+        inf = self.info(instance)
+        lp, ic, lf = self.tree(instance)
+        return dict(t=inf["t"], dt=inf["dt"], step=inf["steps"], lastActive=inf["last_active"],
+                    nbleafs=inf["nb_leafs"], lp=lp, icoord=ic, leafs=lf, U=self.download("U", instance),
+                    Bi=self.download("Bi", instance))

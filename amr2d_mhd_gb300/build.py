@@ -1,0 +1,81 @@
+"""Build of the sm_103a library libamr2d_mhd.so (in-tree, amr2d_mhd_gb300/_build/).
+
+Every translation unit compiles in parallel with nvcc for sm_103a only.  The
+FP64 kernels (stage_f64_*.cu, aux.cu) are compiled with -fmad=false and the
+host code with -ffp-contract=off: that path reproduces the reference's
+floating-point operations one by one, so nothing may be fused.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libamr2d_mhd.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found: the CUDA extension cannot be built")
+
+
+def sources():
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def _flags(src: str):
+    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I" + CSRC]
+    if src.endswith(".cpp"):
+        return ["-x", "cu"] + ARCH + common
+    fmad = ["-fmad=false"] if (src.startswith("stage_f64") or src == "aux.cu") else []
+    return ARCH + common + fmad
+
+
+def _stamp() -> float:
+    t = 0.0
+    for f in os.listdir(CSRC):
+        t = max(t, os.path.getmtime(os.path.join(CSRC, f)))
+    t = max(t, os.path.getmtime(os.path.join(HERE, "..", "include", "amr2d_mhd.h")))
+    return max(t, os.path.getmtime(__file__))
+
+
+def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _stamp():
+        return LIB
+    nvcc = _nvcc()
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sources()
+
+    def compile_one(src):
+        obj = os.path.join(BUILD, src + ".o")
+        cmd = [nvcc, "-c", os.path.join(CSRC, src), "-o", obj] + _flags(src)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed on %s:\n%s%s" % (src, r.stdout, r.stderr))
+        if verbose and (r.stdout or r.stderr):
+            sys.stderr.write(r.stdout + r.stderr)
+        return obj
+
+    n = jobs or min(len(srcs), max(2, os.cpu_count() or 2))
+    with cf.ThreadPoolExecutor(n) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

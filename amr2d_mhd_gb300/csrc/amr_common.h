@@ -1,0 +1,80 @@
+// Shared definitions of the host engine and the sm_103a kernels.
+#pragma once
+
+#include <stdint.h>
+
+namespace amr {
+
+constexpr int NI = 16;     // interior cells per block edge (input.txt "16 16 8")
+constexpr int NVAR = 8;    // rho, rho u, rho v, rho w, E, Bx, By, Bz (meshblock.cpp:19-21)
+constexpr double EPS = 1.0E-15;  // defs.hpp:16 (DOUBLE_PREC)
+
+// limiter ids (slopelimiter.cpp:8-48) and reconstruction families (MUSCL2D.cpp:24-34)
+enum Limiter { LIM_1ST = 0, LIM_NOSL, LIM_MINMOD, LIM_VANLEER, LIM_SUPERBEE, LIM_MC, LIM_KOREN,
+               LIM_CADA3RD, LIM_WENO3, LIM_WENO5 };
+enum Recon { REC_MUSCL = 0, REC_WENO3 = 1, REC_WENO5 = 2 };
+// Riemann solvers (riemannS.cpp:30-44)
+enum Flux { FLX_RUSA = 0, FLX_HLLE, FLX_HLLC, FLX_HLLD, FLX_ROE };
+
+// device error word: first failure wins (code, block, i, j)
+enum DevErr { DERR_NONE = 0, DERR_PRESSURE = 1, DERR_NAN = 2, DERR_HLLC = 3, DERR_REFINE_NAN = 4 };
+struct DevError {
+  int code;
+  int blk;
+  int i, j;
+  double value;
+};
+
+// One leaf block to process: its physical slot and the instance it belongs to.
+struct LeafTask {
+  int slot;
+  int inst;
+  double dx, dy;
+};
+
+// Per-instance scalars read by the kernels (kept in device memory so that a
+// captured CUDA graph sees the values of the current step).
+struct InstParams {
+  double gamma;
+  double dt;      // dom.dt of the current step
+  int limiter;
+  int pad;
+};
+
+// One gather of a compiled ghost fill (see ghost_compile.cpp).
+//   COPY:   dst <- src                      (value before the fill)
+//   SNAP:   dst <- snapshot[src_slot]       (a pre-fill value of a cell that the
+//                                            same fill overwrites; saved first)
+//   AVG4:   dst <- 0.25*(s(i,j)+s(i,j+1)+s(i+1,j)+s(i+1,j+1))     boundary.cpp:48
+//   AVGJ:   dst <- 0.5*(s(i,j)+s(i,j+1))                          boundaryfc.cpp:48, k==0
+//   AVGI:   dst <- 0.5*(s(i,j)+s(i+1,j))                          boundaryfc.cpp:48, k>0
+//   SAVG4 / SAVGJ / SAVGI: the same averages of saved pre-fill values (rows
+//                          src_slot.. of the snapshot buffer, in stencil order)
+enum GhostOpType : uint8_t { GOP_COPY = 0, GOP_SNAP = 1, GOP_AVG4 = 2, GOP_AVGJ = 3, GOP_AVGI = 4,
+                             GOP_SAVG4 = 5, GOP_SAVGJ = 6, GOP_SAVGI = 7 };
+struct GhostOp {
+  int dst_slot;
+  int src_slot;     // for GOP_SNAP: index into the snapshot buffer (times nvar)
+  int16_t dst_pos;  // j * N + i within the block plane
+  int16_t src_pos;
+  uint8_t type;
+  uint8_t k0, k1;   // variables [k0, k1) this gather applies to
+  uint8_t field;    // which field of a merged fill (index into the field table)
+};
+// A pre-fill value that must be saved before a fill runs.
+struct GhostSnap {
+  int slot;
+  int16_t pos;
+  uint8_t k0, k1;
+  uint8_t field;
+  uint8_t pad[3];
+};
+
+// refine (dad -> 4 sons) or coarsen (4 sons -> dad) in physical slots
+struct TreeOp {
+  int dad;
+  int son[4];
+  int inst;
+};
+
+}  // namespace amr

@@ -1,0 +1,133 @@
+// Launchers of the ghost-fill, CT, dt / criterion and refine / coarsen
+// kernels, and the stage dispatcher.  Compiled without FMA contraction: the
+// FP64 instantiations reproduce the reference's arithmetic.
+#include "aux_kernels.cuh"
+#include "launch.hpp"
+
+namespace amr {
+
+bool method_supported(const Method &m) {
+  if (m.flux < FLX_RUSA || m.flux > FLX_HLLD) return false;
+  if (m.ng == 2) return m.recon == REC_MUSCL || m.recon == REC_WENO3;
+  if (m.ng == 4) return m.recon == REC_MUSCL || m.recon == REC_WENO3 || m.recon == REC_WENO5;
+  return false;
+}
+
+cudaError_t launch_stage(const Method &m, const StageArgs &a, int n, cudaStream_t s) {
+  if (!method_supported(m)) return cudaErrorInvalidValue;
+  if (!m.f32) {
+    switch (m.flux) {
+      case FLX_RUSA: return launch_stage_f64_rusa(m, a, n, s);
+      case FLX_HLLE: return launch_stage_f64_hlle(m, a, n, s);
+      case FLX_HLLC: return launch_stage_f64_hllc(m, a, n, s);
+      default: return launch_stage_f64_hlld(m, a, n, s);
+    }
+  }
+  switch (m.flux) {
+    case FLX_RUSA: return launch_stage_f32_rusa(m, a, n, s);
+    case FLX_HLLE: return launch_stage_f32_hlle(m, a, n, s);
+    case FLX_HLLC: return launch_stage_f32_hllc(m, a, n, s);
+    default: return launch_stage_f32_hlld(m, a, n, s);
+  }
+}
+
+cudaError_t launch_ghost(int ng, const GhostLaunch &g, int nsnaps, int nops, cudaStream_t s) {
+  constexpr int B = 256;
+  if (nsnaps > 0) {
+    if (ng == 2) k_ghost_snap<Geo<2>::N><<<(nsnaps + B - 1) / B, B, 0, s>>>(g);
+    else k_ghost_snap<Geo<4>::N><<<(nsnaps + B - 1) / B, B, 0, s>>>(g);
+  }
+  if (nops > 0) {
+    if (ng == 2) k_ghost_apply<Geo<2>::N><<<(nops + B - 1) / B, B, 0, s>>>(g);
+    else k_ghost_apply<Geo<4>::N><<<(nops + B - 1) / B, B, 0, s>>>(g);
+  }
+  return cudaGetLastError();
+}
+
+#define AMR_DISPATCH_NG_S(m, KERNEL, grid, block, smem, s, args)                 \
+  do {                                                                            \
+    if ((m).ng == 2 && !(m).f32) KERNEL<2, double><<<grid, block, smem, s>>>(args); \
+    else if ((m).ng == 2) KERNEL<2, float><<<grid, block, smem, s>>>(args);       \
+    else if (!(m).f32) KERNEL<4, double><<<grid, block, smem, s>>>(args);         \
+    else KERNEL<4, float><<<grid, block, smem, s>>>(args);                        \
+  } while (0)
+
+cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  AMR_DISPATCH_NG_S(m, k_ct_emf, n, 128, 0, s, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (m.ng == 2) k_ct_face<2><<<n, 128, 0, s>>>(a);
+  else k_ct_face<4><<<n, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  AMR_DISPATCH_NG_S(m, k_ct_cell, n, 128, 0, s, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dt_crit(const Method &m, const DtArgs &a, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  AMR_DISPATCH_NG_S(m, k_dt_crit, n, 256, 0, s, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  AMR_DISPATCH_NG_S(m, k_refine, n, 256, 0, s, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coarsen(const Method &m, const TreeOpArgs &a, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  AMR_DISPATCH_NG_S(m, k_coarsen, n, 256, 0, s, a);
+  return cudaGetLastError();
+}
+
+// Copy whole blocks between the slot pool and a dense float64 staging array
+// (block b of the staging array <-> slot slots[b]), converting FP32 fields.
+__global__ void k_gather(const int *slots, int nblk, const void *src, int f32, int per, double *dst) {
+  const size_t total = static_cast<size_t>(nblk) * per;
+  for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t b = e / per, r = e % per;
+    const size_t s = static_cast<size_t>(slots[b]) * per + r;
+    dst[e] = f32 ? static_cast<double>(static_cast<const float *>(src)[s]) : static_cast<const double *>(src)[s];
+  }
+}
+
+__global__ void k_scatter(const int *slots, int nblk, void *dst, int f32, int per, const double *src) {
+  const size_t total = static_cast<size_t>(nblk) * per;
+  for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t b = e / per, r = e % per;
+    const size_t d = static_cast<size_t>(slots[b]) * per + r;
+    if (f32) static_cast<float *>(dst)[d] = static_cast<float>(src[e]);
+    else static_cast<double *>(dst)[d] = src[e];
+  }
+}
+
+cudaError_t launch_gather(const int *slots, int nblk, const void *src, int f32, int per, double *dst,
+                          cudaStream_t s) {
+  if (nblk <= 0) return cudaSuccess;
+  const size_t total = static_cast<size_t>(nblk) * per;
+  const int grid = static_cast<int>((total + 255) / 256 < 152 * 16 ? (total + 255) / 256 : 152 * 16);
+  k_gather<<<grid, 256, 0, s>>>(slots, nblk, src, f32, per, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const int *slots, int nblk, void *dst, int f32, int per, const double *src,
+                           cudaStream_t s) {
+  if (nblk <= 0) return cudaSuccess;
+  const size_t total = static_cast<size_t>(nblk) * per;
+  const int grid = static_cast<int>((total + 255) / 256 < 152 * 16 ? (total + 255) / 256 : 152 * 16);
+  k_scatter<<<grid, 256, 0, s>>>(slots, nblk, dst, f32, per, src);
+  return cudaGetLastError();
+}
+
+}  // namespace amr

@@ -1,0 +1,497 @@
+// Ghost-fill gathers, constrained transport, the CFL / refinement reduction
+// and the prolongation / restriction kernels.
+#pragma once
+
+#include "amr_common.h"
+#include "physics.cuh"
+#include "stage.cuh"
+
+namespace amr {
+
+// ------------------------------------------------------------ ghost fills
+// A launch applies up to kMaxSeg (program, field) segments.
+constexpr int kMaxSeg = 3;
+struct GhostSeg {
+  const GhostOp *ops;
+  const GhostSnap *snaps;
+  int nops, nsnaps;
+  int snap_off;       // first snapshot row of this segment
+  void *field;
+  int nv;
+  int f32;            // field stored as float
+};
+struct GhostLaunch {
+  GhostSeg seg[kMaxSeg];
+  int nseg;
+  double *snapbuf;    // [total snaps][8]
+};
+
+template <int N>
+__device__ __forceinline__ double gload(const GhostSeg &s, int slot, int k, int pos) {
+  const size_t idx = (static_cast<size_t>(slot) * s.nv + k) * (N * N) + pos;
+  return s.f32 ? static_cast<double>(static_cast<const float *>(s.field)[idx])
+               : static_cast<const double *>(s.field)[idx];
+}
+
+// save the pre-fill values the same fill overwrites
+template <int N>
+__global__ void k_ghost_snap(GhostLaunch g) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int q = 0; q < g.nseg; q++) {
+    const GhostSeg &s = g.seg[q];
+    if (t < s.nsnaps) {
+      const GhostSnap sn = s.snaps[t];
+      for (int k = sn.k0; k < sn.k1; k++)
+        g.snapbuf[static_cast<size_t>(s.snap_off + t) * 8 + k] = gload<N>(s, sn.slot, k, sn.pos);
+      return;
+    }
+    t -= s.nsnaps;
+  }
+}
+
+// boundary.cpp / boundaryfc.cpp / boundaryec.cpp as compiled gathers
+template <int N, typename F>
+__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, const double *snapbuf) {
+  constexpr int NN = N * N;
+  F *fld = static_cast<F *>(s.field);
+  const F *src = fld + static_cast<size_t>(op.src_slot) * s.nv * NN + op.src_pos;
+  F *dst = fld + static_cast<size_t>(op.dst_slot) * s.nv * NN + op.dst_pos;
+  for (int k = op.k0; k < op.k1; k++) {
+    F v;
+    switch (op.type) {
+      case GOP_COPY: v = src[k * NN]; break;
+      case GOP_SNAP: v = static_cast<F>(snapbuf[static_cast<size_t>(s.snap_off + op.src_slot) * 8 + k]); break;
+      case GOP_AVG4: {  // sum_irjr order: (i,j) (i,j+1) (i+1,j) (i+1,j+1)
+        F a = F(0.);
+        a += src[k * NN];
+        a += src[k * NN + N];
+        a += src[k * NN + 1];
+        a += src[k * NN + 1 + N];
+        v = F(0.25) * a;
+      } break;
+      case GOP_AVGJ: { F a = F(0.); a += src[k * NN]; a += src[k * NN + N]; v = F(0.5) * a; } break;
+      case GOP_AVGI: { F a = F(0.); a += src[k * NN]; a += src[k * NN + 1]; v = F(0.5) * a; } break;
+      default: {  // SAVG4 / SAVGJ / SAVGI
+        const double *sv = snapbuf + static_cast<size_t>(s.snap_off + op.src_slot) * 8 + k;
+        const int nc = op.type == GOP_SAVG4 ? 4 : 2;
+        F a = F(0.);
+        for (int q = 0; q < nc; q++) a += static_cast<F>(sv[q * 8]);
+        v = (op.type == GOP_SAVG4 ? F(0.25) : F(0.5)) * a;
+      } break;
+    }
+    dst[k * NN] = v;
+  }
+}
+
+template <int N>
+__global__ void k_ghost_apply(GhostLaunch g) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int q = 0; q < g.nseg; q++) {
+    const GhostSeg &s = g.seg[q];
+    if (t < s.nops) {
+      const GhostOp op = s.ops[t];
+      if (s.f32) ghost_apply_one<N, float>(s, op, g.snapbuf);
+      else ghost_apply_one<N, double>(s, op, g.snapbuf);
+      return;
+    }
+    t -= s.nops;
+  }
+}
+
+// ------------------------------------------------------------- CT2D.cpp
+struct CtArgs {
+  const LeafTask *tasks;
+  const InstParams *inst;
+  const void *ff, *gg;    // fluxes (storage type S)
+  double *EMF;
+  const double *Bsrc;     // CT2D's Bi argument
+  double *Bnew;           // CT2D's Binew argument
+  void *q;                // cell state corrected by the face average
+  int step;
+};
+
+// CT2D.cpp:16-26 corner EMF for i, j in [1, N)
+template <int NG, typename S>
+__global__ void k_ct_emf(CtArgs a) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  const LeafTask t = a.tasks[blockIdx.x];
+  const S *ff = static_cast<const S *>(a.ff) + static_cast<size_t>(t.slot) * 8 * NN;
+  const S *gg = static_cast<const S *>(a.gg) + static_cast<size_t>(t.slot) * 8 * NN;
+  double *E = a.EMF + static_cast<size_t>(t.slot) * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    if (i < 1 || j < 1) continue;
+    const double g5a = gg[5 * NN + j * N + i - 1], g5b = gg[5 * NN + c];
+    const double f6a = ff[6 * NN + (j - 1) * N + i], f6b = ff[6 * NN + c];
+    E[c] = 0.25 * ((g5a + g5b) - (f6a + f6b));
+  }
+}
+
+// CT2D.cpp:78-92 face update with the RK2 combine
+template <int NG>
+__global__ void k_ct_face(CtArgs a) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  const LeafTask t = a.tasks[blockIdx.x];
+  const double dt = a.inst[t.inst].dt;
+  const double *E = a.EMF + static_cast<size_t>(t.slot) * NN;
+  const double *B0 = a.Bsrc + static_cast<size_t>(t.slot) * 2 * NN;
+  double *B1 = a.Bnew + static_cast<size_t>(t.slot) * 2 * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    const int ip = i < N - 1 ? i + 1 : i, jp = j < N - 1 ? j + 1 : j;
+    double res = (1. / t.dy) * (E[jp * N + i] - E[c]);
+    if (a.step == 1) B1[c] = B0[c] - dt * res;
+    else B1[c] = 0.5 * (B0[c] + B1[c] - dt * res);
+    res = -(1. / t.dx) * (E[j * N + ip] - E[c]);
+    if (a.step == 1) B1[NN + c] = B0[NN + c] - dt * res;
+    else B1[NN + c] = 0.5 * (B0[NN + c] + B1[NN + c] - dt * res);
+  }
+}
+
+// CT2D.cpp:95-123 cell B := face average, with the energy correction, on
+// every cell of the block (ghosts included)
+template <int NG, typename S>
+__global__ void k_ct_cell(CtArgs a) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  const LeafTask t = a.tasks[blockIdx.x];
+  const double *B = a.Bnew + static_cast<size_t>(t.slot) * 2 * NN;
+  S *q = static_cast<S *>(a.q) + static_cast<size_t>(t.slot) * 8 * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    const int ip = i < N - 1 ? i + 1 : i, ii = ip - 1;
+    const int jp = j < N - 1 ? j + 1 : j, jj = jp - 1;
+    const double bx = 0.5 * (B[j * N + ip] + B[j * N + ii]);
+    const double by = 0.5 * (B[NN + jp * N + i] + B[NN + jj * N + i]);
+    const double q5 = q[5 * NN + c], q6 = q[6 * NN + c];
+    q[4 * NN + c] = static_cast<S>(static_cast<double>(q[4 * NN + c]) +
+                                   0.5 * ((bx * bx + by * by) - (q5 * q5 + q6 * q6)));
+    q[5 * NN + c] = static_cast<S>(bx);
+    q[6 * NN + c] = static_cast<S>(by);
+  }
+}
+
+// --------------------------------------------- dt (main.cpp:322-343) and
+// refinement criterion (criteria.cpp:6-44) of every leaf, one CTA per leaf.
+// Computed in FP64 for both storage types.
+struct DtArgs {
+  const LeafTask *tasks;
+  const InstParams *inst;
+  const void *U;
+  double *lambda;   // per task: min(dx,dy) / max(lambda1, lambda2)
+  double *grad;     // per task: max relative jump
+  DevError *err;
+  int want_grad;
+};
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = v < u ? u : v;
+  }
+  return v;
+}
+
+template <int NG, typename S>
+__global__ void __launch_bounds__(256) k_dt_crit(DtArgs a) {
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN;
+  __shared__ double sW[5][NN];   // rho, u, p, Bx, By (the criterion's variables + u)
+  __shared__ double red[2][8];
+  const LeafTask t = a.tasks[blockIdx.x];
+  const double g = a.inst[t.inst].gamma;
+  const S *U = static_cast<const S *>(a.U) + static_cast<size_t>(t.slot) * 8 * NN;
+  double l1 = 0., l2 = 0.;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    double u[8], w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = static_cast<double>(U[k * NN + c]);
+    cons2prim_cell<double>(u, w, g);
+    sW[0][c] = w[0]; sW[1][c] = w[1]; sW[2][c] = w[4]; sW[3][c] = w[5]; sW[4][c] = w[6];
+    const int i = c % N, j = c / N;
+    if (w[4] <= 0 && i > G::LO && i < G::HI + 1 && j > G::LO && j < G::HI + 1)
+      dev_fail(a.err, DERR_PRESSURE, t.slot, i, j, w[4]);
+    if (i >= NG && i <= G::HI && j >= NG && j <= G::HI) {
+      // note lambda1 takes |rho| (W[..][0], main.cpp:335), lambda2 |u| (:337)
+      l1 = smax(l1, fabs(w[0]) + fast_speed<double>(w, g, 5));
+      l2 = smax(l2, fabs(w[1]) + fast_speed<double>(w, g, 6));
+    }
+  }
+  __syncthreads();
+  double gr = 0.;
+  if (a.want_grad) {
+    for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+      const int i = c % N, j = c / N;
+      if (i < NG || i > G::HI || j < NG || j > G::HI) continue;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int v = q == 0 ? 2 : (q == 1 ? 0 : q + 1);   // p, rho, Bx, By
+        const double c0 = sW[v][c];
+        const double dm = mmax(EPS, fabs(c0));
+        double d1 = fabs(sW[v][c + 1] - c0);
+        double d2 = mmax(d1, fabs(sW[v][c - 1] - c0));
+        d1 = mmax(d2, fabs(sW[v][c + N] - c0));
+        d2 = mmax(d1, fabs(sW[v][c - N] - c0));
+        gr = mmax(gr, d2 / dm);
+      }
+    }
+  }
+  double m = smax(l1, l2);
+  m = warp_max(m);
+  gr = warp_max(gr);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { red[0][wid] = m; red[1][wid] = gr; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = red[0][0], gg = red[1][0];
+    for (int q = 1; q < static_cast<int>(blockDim.x >> 5); q++) {
+      mm = mm < red[0][q] ? red[0][q] : mm;
+      gg = gg < red[1][q] ? red[1][q] : gg;
+    }
+    a.lambda[blockIdx.x] = smin(t.dx, t.dy) / mm;
+    a.grad[blockIdx.x] = gg;
+  }
+}
+
+// -------------------------------------------- refine.cpp / refineBi_CT.cpp
+struct TreeOpArgs {
+  const TreeOp *ops;
+  const InstParams *inst;
+  void *U;
+  double *Bi;
+  DevError *err;
+};
+
+// refine.cpp:17-85 (minmod, the slope multiplies the forward difference) and
+// U2W("refine") on the sons; one CTA per refined block
+template <int NG, typename S>
+__global__ void k_refine(TreeOpArgs a) {
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN, n2 = (N - 1) / 2;
+  using T = S;
+  const TreeOp op = a.ops[blockIdx.x];
+  const S *D = static_cast<const S *>(a.U) + static_cast<size_t>(op.dad) * 8 * NN;
+  const T E = eps_of<T>();
+  // refine.cpp:45-59 for the 4 sons, each (son, cell) with its 8 variables
+  for (int e = threadIdx.x; e < 4 * NN; e += blockDim.x) {
+    const int sq = e / NN, c = e % NN;
+    const int i = c % N, j = c / N;
+    const int sx = (i + NG) % 2, sy = (j + NG) % 2;
+    const int ii = (sq & 1) ? (i - NG + 2) / 2 + n2 : (i + NG) / 2;
+    const int jj = (sq & 2) ? (j - NG + 2) / 2 + n2 : (j + NG) / 2;
+    S *Sn = static_cast<S *>(a.U) + static_cast<size_t>(op.son[sq]) * 8 * NN;
+    T u[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const S *q = D + k * NN;
+      const T q0 = q[jj * N + ii];
+      T res = q0, r, phi;
+      r = (q0 - q[jj * N + ii - 1]) / (q[jj * N + ii + 1] - q0 + E);
+      phi = T(0.25) * slope_limiter<T>(LIM_MINMOD, r, T(0)) * (q[jj * N + ii + 1] - q0);
+      res = sx == 0 ? res - phi : res + phi;
+      r = (q0 - q[(jj - 1) * N + ii]) / (q[(jj + 1) * N + ii] - q0 + E);
+      phi = T(0.25) * slope_limiter<T>(LIM_MINMOD, r, T(0)) * (q[(jj + 1) * N + ii] - q0);
+      res = sy == 0 ? res - phi : res + phi;
+      u[k] = res;
+      Sn[k * NN + c] = res;
+    }
+    // U2W("refine") pressure trap (refine.cpp:70-82)
+    T w[8];
+    cons2prim_cell<S>(u, w, a.inst[op.inst].gamma);
+    if (w[4] <= T(0) && i > G::LO && i < G::HI + 1 && j > G::LO && j < G::HI + 1)
+      dev_fail(a.err, DERR_PRESSURE, op.son[sq], i, j, static_cast<double>(w[4]));
+  }
+  // refineBi_CT.cpp:4-74
+  const double *Bd = a.Bi + static_cast<size_t>(op.dad) * 2 * NN;
+  for (int e = threadIdx.x; e < 4 * NN * 2; e += blockDim.x) {
+    const int k = e / (4 * NN), rem = e % (4 * NN);
+    const int sq = rem / NN, c = rem % NN;
+    const int i0 = c % N, j0 = c / N;
+    const int sx = (i0 + NG) % 2, sy = (j0 + NG) % 2;
+    const int i = (sq & 1) ? (i0 - NG + 2) / 2 + n2 : (i0 + NG) / 2;
+    const int j = (sq & 2) ? (j0 - NG + 2) / 2 + n2 : (j0 + NG) / 2;
+    const double *bx = Bd, *by = Bd + NN;
+    auto X = [&](int di, int dj) { return bx[(j + dj) * N + i + di]; };
+    auto Y = [&](int di, int dj) { return by[(j + dj) * N + i + di]; };
+    const double Bx_jm = X(0, -1), Bx = X(0, 0), Bx_jp = X(0, 1);
+    const double Bx_ip = X(1, 0), Bx_ipjm = X(1, -1), Bx_ipjp = X(1, 1);
+    const double By_im = Y(-1, 0), By = Y(0, 0), By_ip = Y(1, 0);
+    const double By_imjp = Y(-1, 1), By_jp = Y(0, 1), By_ipjp = Y(1, 1);
+    double r;
+    r = (Bx - Bx_jm) / (Bx_jp - Bx + EPS);
+    const double DyBxm = slope_limiter<double>(LIM_MINMOD, r, 0) * (Bx_jp - Bx);
+    r = (Bx_ip - Bx_ipjm) / (Bx_ipjp - Bx_ip + EPS);
+    const double DyBxp = slope_limiter<double>(LIM_MINMOD, r, 0) * (Bx_ipjp - Bx_ip);
+    r = (By - By_im) / (By_ip - By + EPS);
+    const double DxBym = slope_limiter<double>(LIM_MINMOD, r, 0) * (By_ip - By);
+    r = (By_jp - By_imjp) / (By_ipjp - By_jp + EPS);
+    const double DxByp = slope_limiter<double>(LIM_MINMOD, r, 0) * (By_ipjp - By_jp);
+    const double ax = (Bx_ip - Bx);
+    const double by_ = -1. * ax;
+    const double ay = 0.5 * (DyBxp + DyBxm);
+    const double bx_ = 0.5 * (DxByp + DxBym);
+    const double axy = (DyBxp - DyBxm);
+    const double byy = axy / (-2.);
+    const double bxy = (DxByp - DxBym);
+    const double axx = bxy / (-2.);
+    const double a0 = 0.5 * (Bx_ip + Bx) - 0.25 * axx;
+    const double b0 = 0.5 * (By_jp + By) - 0.25 * byy;
+    const double ayy = 0., bxx = 0.;
+    double res;
+    if (k == 0) {
+      const double tx = sx == 0 ? 0 : 0.5, ty = sy == 0 ? -0.25 : 0.25;
+      res = a0 + ax * tx + ay * ty + axx * tx * tx + axy * tx * ty + ayy * ty * ty;
+    } else {
+      const double tx = sx == 0 ? -0.25 : 0.25, ty = sy == 0 ? 0 : 0.5;
+      res = b0 + bx_ * tx + by_ * ty + bxx * tx * tx + bxy * tx * ty + byy * ty * ty;
+    }
+    if (isnan(res)) dev_fail(a.err, DERR_REFINE_NAN, op.son[sq], i0, j0, 0.0);
+    a.Bi[static_cast<size_t>(op.son[sq]) * 2 * NN + k * NN + c] = res;
+  }
+}
+
+// ------------------------------------------- coarsen.cpp / coarsenBi_CT.cpp
+// The reference's nine loop nests run in order (a cell written by two nests
+// keeps the later value); each nest is spread over the CTA.
+template <int NG, typename F, bool FACE>
+__device__ void coarsen_field(F *Q, int nv, const int *son, int dad) {
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN, ng = NG;
+  constexpr int nxmin = NG, nymin = NG, nxminb = NG - 1, nyminb = NG - 1;
+  constexpr int nxmaxb = G::HI + 1, nymaxb = G::HI + 1, nx2 = (N - 1) / 2, ny2 = (N - 1) / 2;
+  const F c = FACE ? F(0.5) : F(0.25);
+  auto SUM = [&](int sb, int k, int i1, int j1) -> F {
+    const F *s = Q + (static_cast<size_t>(sb) * nv + k) * NN;
+    const int i2 = FACE ? (k == 0 ? i1 : i1 + 1) : i1 + 1;
+    const int j2 = FACE ? (k == 0 ? j1 + 1 : j1) : j1 + 1;
+    F v = F(0.);
+    for (int i = i1; i <= i2; i++)
+      for (int j = j1; j <= j2; j++) v += s[j * N + i];
+    return c * v;
+  };
+  auto D = [&](int k, int i, int j) -> F & { return Q[(static_cast<size_t>(dad) * nv + k) * NN + j * N + i]; };
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // the block itself
+  {
+    constexpr int ni = nx2 - nxmin + 1;
+    for (int e = tid; e < ni * ni * nv; e += nt) {
+      const int k = e / (ni * ni), r = e % (ni * ni);
+      const int i = nxmin + r % ni, j = nymin + r / ni;
+      const int i1 = 2 * i - nxmin, j1 = 2 * j - nymin;
+      const int nx2i = nx2 + i - 1 - (ng - 2), ny2j = ny2 + j - 1 - (ng - 2);
+      D(k, i, j) = SUM(son[0], k, i1, j1);
+      D(k, nx2i, j) = SUM(son[1], k, i1, j1);
+      D(k, i, ny2j) = SUM(son[2], k, i1, j1);
+      D(k, nx2i, ny2j) = SUM(son[3], k, i1, j1);
+    }
+  }
+  __syncthreads();
+  constexpr int h = ng / 2;
+  constexpr int nj = ny2 - nymin + 1;
+  // Left corners
+  for (int e = tid; e < nv * h * h; e += nt) {
+    const int k = e / (h * h), i = (e % (h * h)) / h, j = e % h;
+    const int i1 = nxminb - 2 * i - 1;
+    int j1 = nyminb - 2 * j - 1;
+    D(k, nxminb - i, nyminb - j) = SUM(son[0], k, i1, j1);
+    j1 = nymaxb + 2 * j;
+    D(k, nxminb - i, nymaxb + j) = SUM(son[2], k, i1, j1);
+  }
+  __syncthreads();
+  // Left edge
+  for (int e = tid; e < (nxminb + 1) * nj * nv; e += nt) {
+    const int k = e / ((nxminb + 1) * nj), r = e % ((nxminb + 1) * nj);
+    const int i = r / nj, j = nymin + r % nj;
+    const int j1 = 2 * j - nymin, ny2j = j + ny2 - 1 - (ng - 2);
+    int i1 = nxminb - 2 * i - 1;
+    if (i1 < 0) i1 = 0;
+    D(k, nxminb - i, j) = SUM(son[0], k, i1, j1);
+    D(k, nxminb - i, ny2j) = SUM(son[2], k, i1, j1);
+  }
+  __syncthreads();
+  // Right corners
+  for (int e = tid; e < nv * h * h; e += nt) {
+    const int k = e / (h * h), i = (e % (h * h)) / h, j = e % h;
+    const int i1 = nxmaxb + 2 * i;
+    int j1 = nyminb - 2 * j - 1;
+    D(k, nxmaxb + i, nyminb - j) = SUM(son[1], k, i1, j1);
+    j1 = nymaxb + 2 * j;
+    D(k, nxmaxb + i, nymaxb + j) = SUM(son[3], k, i1, j1);
+  }
+  __syncthreads();
+  // Right edge
+  for (int e = tid; e < ng * nj * nv; e += nt) {
+    const int k = e / (ng * nj), r = e % (ng * nj);
+    const int i = r / nj, j = nymin + r % nj;
+    const int j1 = 2 * j - nymin, ny2j = j + ny2 - 1 - (ng - 2);
+    int i1 = nxmaxb + 2 * i;
+    if (i1 + 1 > N - 1) i1 = N - 2;
+    D(k, nxmaxb + i, j) = SUM(son[1], k, i1, j1);
+    D(k, nxmaxb + i, ny2j) = SUM(son[3], k, i1, j1);
+  }
+  __syncthreads();
+  // Bottom corners
+  for (int e = tid; e < nv * h * h; e += nt) {
+    const int k = e / (h * h), j = (e % (h * h)) / h, i = e % h;
+    const int j1 = nyminb - 2 * j - 1;
+    int i1 = nxminb - 2 * i - 1;
+    D(k, nxminb - i, nyminb - j) = SUM(son[0], k, i1, j1);
+    i1 = nxmaxb + 2 * i;
+    D(k, nxmaxb + i, nyminb - j) = SUM(son[1], k, i1, j1);
+  }
+  __syncthreads();
+  // Bottom edge
+  for (int e = tid; e < nj * (nyminb + 1) * nv; e += nt) {
+    const int k = e / (nj * (nyminb + 1)), r = e % (nj * (nyminb + 1));
+    const int i = nxmin + r / (nyminb + 1), j = r % (nyminb + 1);
+    const int i1 = 2 * i - nxmin, nx2i = i + nx2 - 1 - (ng - 2);
+    int j1 = nyminb - 2 * j - 1;
+    if (j1 < 0) j1 = 0;
+    D(k, i, nyminb - j) = SUM(son[0], k, i1, j1);
+    D(k, nx2i, nyminb - j) = SUM(son[1], k, i1, j1);
+  }
+  __syncthreads();
+  // Top corners
+  for (int e = tid; e < nv * h * h; e += nt) {
+    const int k = e / (h * h), j = (e % (h * h)) / h, i = e % h;
+    const int j1 = nymaxb + 2 * j;
+    int i1 = nxminb - 2 * i - 1;
+    D(k, nxminb - i, nymaxb + j) = SUM(son[2], k, i1, j1);
+    i1 = nxmaxb + 2 * i;
+    D(k, nxmaxb + i, nymaxb + j) = SUM(son[3], k, i1, j1);
+  }
+  __syncthreads();
+  // Top edge
+  for (int e = tid; e < nj * ng * nv; e += nt) {
+    const int k = e / (nj * ng), r = e % (nj * ng);
+    const int i = nxmin + r / ng, j = r % ng;
+    const int i1 = 2 * i - nxmin, nx2i = i + nx2 - 1 - (ng - 2);
+    int j1 = nymaxb + 2 * j;
+    if (j1 + 1 > N - 1) j1 = N - 2;
+    D(k, i, nymaxb + j) = SUM(son[2], k, i1, j1);
+    D(k, nx2i, nymaxb + j) = SUM(son[3], k, i1, j1);
+  }
+  __syncthreads();
+}
+
+template <int NG, typename S>
+__global__ void k_coarsen(TreeOpArgs a) {
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN;
+  const TreeOp op = a.ops[blockIdx.x];
+  coarsen_field<NG, S, false>(static_cast<S *>(a.U), 8, op.son, op.dad);
+  // coarsen.cpp:310 U2W("coarsen") pressure trap on the dad
+  const S *D = static_cast<const S *>(a.U) + static_cast<size_t>(op.dad) * 8 * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    S u[8], w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = D[k * NN + c];
+    cons2prim_cell<S>(u, w, a.inst[op.inst].gamma);
+    const int i = c % N, j = c / N;
+    if (w[4] <= S(0) && i > G::LO && i < G::HI + 1 && j > G::LO && j < G::HI + 1)
+      dev_fail(a.err, DERR_PRESSURE, op.dad, i, j, static_cast<double>(w[4]));
+  }
+  coarsen_field<NG, double, true>(a.Bi, 2, op.son, op.dad);
+}
+
+}  // namespace amr

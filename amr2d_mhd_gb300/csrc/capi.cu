@@ -1,0 +1,154 @@
+// extern "C" boundary (include/amr2d_mhd.h).  No C++ exception crosses it.
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <fstream>
+#include <new>
+#include <string>
+
+#include "engine.hpp"
+
+struct amr_handle {
+  amr::Engine engine;
+};
+
+namespace {
+template <typename F>
+int guarded(amr_handle *h, F &&f) {
+  if (!h) return AMR_E_ARG;
+  try {
+    return f(h->engine);
+  } catch (const std::bad_alloc &) {
+    h->engine.last_error = "host out of memory";
+    return AMR_E_OOM;
+  } catch (const std::exception &e) {
+    h->engine.last_error = e.what();
+    return AMR_E_STATE;
+  }
+}
+void copy_name(char *dst, const std::string &s) {
+  std::memset(dst, 0, 16);
+  std::strncpy(dst, s.c_str(), 15);
+}
+}  // namespace
+
+extern "C" {
+
+int amr_abi_version(void) { return AMR_ABI_VERSION; }
+
+const char *amr_status_string(int s) {
+  switch (s) {
+    case AMR_OK: return "ok";
+    case AMR_E_CONFIG: return "invalid configuration";
+    case AMR_E_CUDA: return "CUDA error";
+    case AMR_E_OOM: return "out of memory";
+    case AMR_E_MAXBLOCKS: return "block budget exceeded";
+    case AMR_E_PRESSURE: return "zero or negative pressure";
+    case AMR_E_NAN: return "NaN encountered";
+    case AMR_E_DT: return "invalid dt";
+    case AMR_E_HLLC: return "HLLC wave-speed trap";
+    case AMR_E_STATE: return "call out of order";
+    case AMR_E_TIMEOUT: return "device wait timed out";
+    case AMR_E_UNSUPPORTED: return "unsupported option";
+    case AMR_E_ARG: return "bad argument";
+    default: return "unknown status";
+  }
+}
+
+// defaults = the reference's shipped input.txt and defs.hpp constants
+void amr_config_default(amr_config *c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->struct_size = sizeof(amr_config);
+  c->nx = 16; c->ny = 16; c->nvar = 8;
+  c->lenx = 1.0; c->leny = 1.0;
+  c->cfl = 0.5;
+  copy_name(c->ic, "rotor");
+  copy_name(c->limiter, "MC");
+  copy_name(c->flux, "RUSA");
+  c->maxlevs = 5;
+  c->nghosts = 2;
+  c->nroots_x = 2; c->nroots_y = 2;
+  c->periodic = 0;
+  c->geometry = 0;
+  c->gamma = 0.0;
+  c->t_end = 0.0;
+  c->precision = AMR_FP64;
+}
+
+// main.cpp:156-177
+int amr_config_from_input(const char *path, amr_config *c) {
+  if (!path || !c) return AMR_E_ARG;
+  std::ifstream f(path);
+  if (!f.is_open()) return AMR_E_CONFIG;  // "Unable to open the file..."
+  int nx, ny, nvar;
+  double lx, ly, cfl;
+  std::string ic, lim, flux;
+  if (!(f >> nx >> ny >> nvar >> lx >> ly >> cfl >> ic >> lim >> flux)) return AMR_E_CONFIG;
+  c->nx = nx; c->ny = ny; c->nvar = nvar;
+  c->lenx = lx; c->leny = ly; c->cfl = cfl;
+  if (ic.size() > 15 || lim.size() > 15 || flux.size() > 15) return AMR_E_CONFIG;
+  copy_name(c->ic, ic);
+  copy_name(c->limiter, lim);
+  copy_name(c->flux, flux);
+  return AMR_OK;
+}
+
+int amr_create_batch(const amr_config *cfgs, int32_t n, amr_handle **out) {
+  if (!cfgs || !out || n <= 0) return AMR_E_ARG;
+  *out = nullptr;
+  for (int q = 0; q < n; q++)
+    if (cfgs[q].struct_size != static_cast<int32_t>(sizeof(amr_config))) return AMR_E_CONFIG;
+  amr_handle *h = new (std::nothrow) amr_handle();
+  if (!h) return AMR_E_OOM;
+  int rc = guarded(h, [&](amr::Engine &e) { return e.create(cfgs, n); });
+  if (rc != AMR_OK) {
+    std::fprintf(stderr, "amr_create: %s\n", h->engine.last_error.c_str());
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return AMR_OK;
+}
+
+int amr_create(const amr_config *cfg, amr_handle **out) { return amr_create_batch(cfg, 1, out); }
+
+int amr_destroy(amr_handle *h) {
+  delete h;
+  return AMR_OK;
+}
+
+int amr_set_stream(amr_handle *h, void *s) {
+  return guarded(h, [&](amr::Engine &e) { return e.set_stream(static_cast<cudaStream_t>(s)); });
+}
+
+int amr_last_error(const amr_handle *h, char *buf, size_t len) {
+  if (!h || !buf || len == 0) return AMR_E_ARG;
+  std::strncpy(buf, h->engine.last_error.c_str(), len - 1);
+  buf[len - 1] = 0;
+  return AMR_OK;
+}
+
+int amr_init(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.init(); }); }
+int amr_step(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.step(); }); }
+int amr_run(amr_handle *h, int64_t n) { return guarded(h, [&](amr::Engine &e) { return e.run(n); }); }
+int amr_get_info(amr_handle *h, int32_t q, amr_info *o) {
+  return guarded(h, [&](amr::Engine &e) { return e.info(q, o); });
+}
+int amr_locate_bounds(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.api_locate_bounds(); }); }
+int amr_boundary(amr_handle *h, int32_t f) { return guarded(h, [&](amr::Engine &e) { return e.api_boundary(f); }); }
+int amr_muscl2d_rk(amr_handle *h, int32_t s) { return guarded(h, [&](amr::Engine &e) { return e.api_muscl2d_rk(s); }); }
+int amr_ct2d(amr_handle *h, int32_t s) { return guarded(h, [&](amr::Engine &e) { return e.api_ct2d(s); }); }
+int amr_cfl_dt(amr_handle *h, double *l) { return guarded(h, [&](amr::Engine &e) { return e.api_cfl_dt(l); }); }
+int amr_admesh(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.api_admesh(); }); }
+int amr_get_tree(amr_handle *h, int32_t q, int32_t *lp, int32_t *ic, uint8_t *lf, int32_t cap) {
+  return guarded(h, [&](amr::Engine &e) { return e.get_tree(q, lp, ic, lf, cap); });
+}
+int amr_download(amr_handle *h, int32_t q, int32_t f, double *d, int64_t n) {
+  return guarded(h, [&](amr::Engine &e) { return e.download(q, f, d, n); });
+}
+int amr_upload(amr_handle *h, int32_t q, int32_t f, const double *s, int64_t n) {
+  return guarded(h, [&](amr::Engine &e) { return e.upload(q, f, s, n); });
+}
+
+}  // extern "C"

@@ -1,0 +1,419 @@
+// Engine: device block pool, per-step orchestration and state exchange.
+#include "engine.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <initializer_list>
+#include <string>
+
+#include "aux_kernels.cuh"
+
+namespace amr {
+
+// ------------------------------------------------------------- buffers
+cudaError_t DevBuf::ensure(size_t n) {
+  if (n <= bytes && p) return cudaSuccess;
+  release();
+  size_t want = n < 256 ? 256 : n;
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) { p = nullptr; bytes = 0; return e; }
+  bytes = want;
+  return cudaSuccess;
+}
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+cudaError_t HostBuf::ensure(size_t n) {
+  if (n <= bytes && p) return cudaSuccess;
+  release();
+  size_t want = n < 256 ? 256 : n;
+  cudaError_t e = cudaMallocHost(&p, want);
+  if (e != cudaSuccess) { p = nullptr; bytes = 0; return e; }
+  bytes = want;
+  return cudaSuccess;
+}
+void HostBuf::release() {
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+namespace {
+int lim_from_name(const char *s) {
+  static const char *names[] = {"1st", "noSL", "minmod", "VanLeer", "Superbee", "MC", "Koren", "Cada3rd",
+                                "WENO3", "WENO5"};
+  if (!std::strcmp(s, "WENO2D")) return LIM_NOSL;  // slopelimiter.cpp:10
+  for (int i = 0; i < 10; i++)
+    if (!std::strcmp(s, names[i])) return i;
+  return -1;
+}
+int flux_from_name(const char *s) {
+  static const char *names[] = {"RUSA", "HLLE", "HLLC", "HLLD", "ROE"};
+  for (int i = 0; i < 5; i++)
+    if (!std::strcmp(s, names[i])) return i;
+  return -1;
+}
+int map_dev_error(int code) {
+  switch (code) {
+    case DERR_PRESSURE: return AMR_E_PRESSURE;
+    case DERR_HLLC: return AMR_E_HLLC;
+    default: return AMR_E_NAN;
+  }
+}
+}  // namespace
+
+Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (void *p : {U_, Us_, ff_, gg_}) if (p) cudaFree(p);
+  for (double *p : {Bi_, Bis_, EMF_}) if (p) cudaFree(p);
+  for (DevBuf *b : {&d_tasks_, &d_params_, &d_lambda_, &d_grad_, &d_err_, &d_snap_, &d_treeops_, &d_stage_, &d_slots_})
+    b->release();
+  for (int i = 0; i < 4; i++) { d_ops_[i].release(); d_snaps_[i].release(); }
+  for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_}) b->release();
+  if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+  delete gc_;
+}
+
+int Engine::fail(int code, const std::string &msg) {
+  last_error = msg;
+  if (code != AMR_E_ARG && code != AMR_E_CONFIG && code != AMR_E_STATE && code != AMR_E_UNSUPPORTED)
+    poisoned_ = true;
+  return code;
+}
+
+int Engine::cuda_fail(cudaError_t e, const char *where) {
+  if (e == cudaErrorMemoryAllocation) return fail(AMR_E_OOM, std::string(where) + ": out of device memory");
+  return fail(AMR_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, where)                              \
+  do {                                               \
+    cudaError_t e_ = (expr);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+  } while (0)
+
+// ------------------------------------------------------------- create
+int Engine::create(const amr_config *cfgs, int n) {
+  if (!cfgs || n <= 0) return fail(AMR_E_ARG, "no configuration");
+  const amr_config &c0 = cfgs[0];
+  for (int q = 0; q < n; q++) {
+    const amr_config &c = cfgs[q];
+    if (c.nx != NI || c.ny != NI) return fail(AMR_E_UNSUPPORTED, "blocks of 16 x 16 interior cells only");
+    if (c.nvar != NVAR) return fail(AMR_E_CONFIG, "nvar must be 8 (MHD, meshblock.cpp:10-12)");
+    if (c.nghosts != 2 && c.nghosts != 4) return fail(AMR_E_CONFIG, "nghosts must be 2 or 4");
+    if (c.maxlevs < 1 || c.maxlevs > 12) return fail(AMR_E_CONFIG, "maxlevs out of range");
+    if (c.nroots_x < 1 || c.nroots_y < 1) return fail(AMR_E_CONFIG, "nroots out of range");
+    if (c.periodic && (c.nroots_x < 2 || c.nroots_y < 2))
+      return fail(AMR_E_CONFIG, "a periodic box needs at least 2 x 2 root blocks");
+    const int lim = lim_from_name(c.limiter), fl = flux_from_name(c.flux);
+    if (lim < 0) return fail(AMR_E_CONFIG, std::string("invalid slope limiter '") + c.limiter + "'");
+    if (fl < 0) return fail(AMR_E_CONFIG, std::string("no appropriate Riemann solver '") + c.flux + "'");
+    if (fl == FLX_ROE) return fail(AMR_E_UNSUPPORTED, "ROE not ready with magnetic field (riemannS.cpp:39-40)");
+    if (ic_from_name(c.ic) == IC_INVALID) return fail(AMR_E_CONFIG, std::string("no valid initial condition '") + c.ic + "'");
+    if (lim == LIM_WENO5 && c.nghosts < 4) return fail(AMR_E_CONFIG, "WENO5 needs nghosts = 4");
+    // a batch shares the kernels: same method and block shape
+    auto family = [](int l) { return l == LIM_WENO3 ? 1 : (l == LIM_WENO5 ? 2 : 0); };
+    if (q > 0 && family(lim) != family(lim_from_name(c0.limiter)))
+      return fail(AMR_E_CONFIG, "instances of a batch must share the reconstruction family");
+    if (q > 0 && (fl != flux_from_name(c0.flux) || c.nghosts != c0.nghosts || c.precision != c0.precision))
+      return fail(AMR_E_CONFIG, "instances of a batch must share flux, nghosts and precision");
+  }
+  const int lim0 = lim_from_name(c0.limiter);
+  m_.ng = c0.nghosts;
+  m_.recon = lim0 == LIM_WENO3 ? REC_WENO3 : (lim0 == LIM_WENO5 ? REC_WENO5 : REC_MUSCL);
+  m_.flux = flux_from_name(c0.flux);
+  m_.f32 = c0.precision == AMR_FP32 ? 1 : 0;
+  if (!method_supported(m_)) return fail(AMR_E_UNSUPPORTED, "method not compiled");
+  f32_ = m_.f32 != 0;
+  ng_ = m_.ng;
+  n_ = NI + 2 * ng_;
+  nn_ = n_ * n_;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(AMR_E_CUDA, "no CUDA device");
+  CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+  own_stream_ = true;
+  gc_ = new GhostCompiler(n_, ng_);
+  inst_.reserve(n);
+  for (int q = 0; q < n; q++) {
+    const amr_config &c = cfgs[q];
+    TreeShape s{NI, NI, c.nghosts, c.maxlevs, c.nroots_x, c.nroots_y, c.periodic != 0};
+    inst_.emplace_back(s);
+    Instance &in = inst_.back();
+    in.cfg = c;
+    in.ic = ic_from_name(c.ic);
+    ic_params(in.ic, in.gamma, in.t_end);
+    if (c.gamma > 0) in.gamma = c.gamma;
+    if (c.t_end > 0) in.t_end = c.t_end;
+    in.cfl = c.cfl;
+    in.limiter = lim_from_name(c.limiter);
+    // meshblock.cpp:87-96
+    const int ni = NI;
+    if (c.geometry == 0) {
+      in.dx[0] = c.lenx / (static_cast<double>(c.nroots_x) * (ni - 1));
+      in.dy[0] = c.leny / (static_cast<double>(c.nroots_y) * (ni - 1));
+    } else {
+      in.dx[0] = c.lenx / (static_cast<double>(c.nroots_x) * ni);
+      in.dy[0] = c.leny / (static_cast<double>(c.nroots_y) * ni);
+    }
+    for (int l = 1; l < 16; l++) { in.dx[l] = in.dx[l - 1] / 2.; in.dy[l] = in.dy[l - 1] / 2.; }
+    in.slot.assign(in.tree.maxblocks(), -1);
+  }
+  built_version_.assign(n, ~0ull);
+  CK(d_err_.ensure(sizeof(DevError)), "alloc");
+  CK(cudaMemsetAsync(d_err_.p, 0, sizeof(DevError), stream_), "memset");
+  CK(h_err_.ensure(sizeof(DevError)), "alloc");
+  CK(h_params_.ensure(sizeof(InstParams) * n), "alloc");
+  CK(d_params_.ensure(sizeof(InstParams) * n), "alloc");
+  return AMR_OK;
+}
+
+int Engine::set_stream(cudaStream_t s) {
+  if (stream_) cudaStreamSynchronize(stream_);
+  if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+  own_stream_ = false;
+  stream_ = s;
+  return AMR_OK;
+}
+
+void *Engine::field_ptr(int f) const {
+  switch (f) {
+    case AMR_FIELD_U: return U_;
+    case AMR_FIELD_US: return Us_;
+    case AMR_FIELD_FF: return ff_;
+    case AMR_FIELD_GG: return gg_;
+    case AMR_FIELD_BI: return Bi_;
+    case AMR_FIELD_BIS: return Bis_;
+    case AMR_FIELD_EMF: return EMF_;
+    default: return nullptr;
+  }
+}
+int Engine::field_nv(int f) const {
+  if (f == AMR_FIELD_BI || f == AMR_FIELD_BIS) return 2;
+  if (f == AMR_FIELD_EMF) return 1;
+  return 8;
+}
+bool Engine::field_f32(int f) const {
+  return f32_ && (f == AMR_FIELD_U || f == AMR_FIELD_US || f == AMR_FIELD_FF || f == AMR_FIELD_GG);
+}
+
+// ------------------------------------------------------------- slots
+int Engine::ensure_slots(int needed) {
+  if (needed <= cap_slots_) return AMR_OK;
+  int cap = cap_slots_ ? cap_slots_ : 64;
+  while (cap < needed) cap *= 2;
+  CK(cudaStreamSynchronize(stream_), "sync");
+  const size_t cell = static_cast<size_t>(8) * nn_, face = static_cast<size_t>(2) * nn_, edge = nn_;
+  const size_t se = f32_ ? sizeof(float) : sizeof(double);
+  void **cells[4] = {&U_, &Us_, &ff_, &gg_};
+  for (void **pp : cells) {
+    void *np = nullptr;
+    CK(cudaMalloc(&np, cap * cell * se), "pool alloc");
+    CK(cudaMemsetAsync(np, 0, cap * cell * se, stream_), "pool memset");
+    if (*pp) {
+      CK(cudaMemcpyAsync(np, *pp, cap_slots_ * cell * se, cudaMemcpyDeviceToDevice, stream_), "pool copy");
+      CK(cudaStreamSynchronize(stream_), "sync");
+      cudaFree(*pp);
+    }
+    *pp = np;
+  }
+  double **dbl[3] = {&Bi_, &Bis_, &EMF_};
+  const size_t per[3] = {face, face, edge};
+  for (int q = 0; q < 3; q++) {
+    double *np = nullptr;
+    CK(cudaMalloc(&np, cap * per[q] * sizeof(double)), "pool alloc");
+    CK(cudaMemsetAsync(np, 0, cap * per[q] * sizeof(double), stream_), "pool memset");
+    if (*dbl[q]) {
+      CK(cudaMemcpyAsync(np, *dbl[q], cap_slots_ * per[q] * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
+         "pool copy");
+      CK(cudaStreamSynchronize(stream_), "sync");
+      cudaFree(*dbl[q]);
+    }
+    *dbl[q] = np;
+  }
+  cap_slots_ = cap;
+  return AMR_OK;
+}
+
+int Engine::assign_slots(Instance &in) {
+  for (int b = 0; b < in.tree.lastActive; b++)
+    if (in.slot[b] < 0) in.slot[b] = used_slots_++;
+  return ensure_slots(used_slots_);
+}
+
+// ------------------------------------------------------------- programs
+int Engine::rebuild() {
+  bool need = !programs_valid_ || built_active_ != active_;
+  for (int a : active_)
+    if (built_version_[a] != inst_[a].tree.version) need = true;
+  if (!need) return AMR_OK;
+  tasks_.clear();
+  task_blk_.clear();
+  for (auto &p : prog_) p.clear();
+  std::vector<Bound> bounds;
+  for (int a : active_) {
+    Instance &in = inst_[a];
+    in.task_begin = static_cast<int>(tasks_.size());
+    for (int nb = 0; nb < in.tree.lastActive; nb++) {
+      if (!in.tree.leafs[nb]) continue;
+      const int lev = in.tree.lp[nb][0];
+      tasks_.push_back(LeafTask{in.slot[nb], a, in.dx[lev], in.dy[lev]});
+      task_blk_.push_back(nb);
+    }
+    in.task_end = static_cast<int>(tasks_.size());
+    in.tree.locate_bounds(bounds);
+    try {
+      gc_->compile(in.tree, bounds, FILL_CC, 8, in.slot.data(), 0, prog_[0]);
+      gc_->compile(in.tree, bounds, FILL_FC, 2, in.slot.data(), 0, prog_[1]);
+      gc_->compile(in.tree, bounds, FILL_FC, 8, in.slot.data(), 0, prog_[2]);
+      gc_->compile(in.tree, bounds, FILL_EC, 1, in.slot.data(), 0, prog_[3]);
+    } catch (const std::exception &ex) {
+      return fail(AMR_E_STATE, ex.what());
+    }
+    built_version_[a] = in.tree.version;
+  }
+  built_active_ = active_;
+  const size_t nt = tasks_.size();
+  CK(d_tasks_.ensure(sizeof(LeafTask) * nt), "alloc");
+  CK(cudaMemcpyAsync(d_tasks_.p, tasks_.data(), sizeof(LeafTask) * nt, cudaMemcpyHostToDevice, stream_), "h2d");
+  CK(d_lambda_.ensure(sizeof(double) * nt), "alloc");
+  CK(d_grad_.ensure(sizeof(double) * nt), "alloc");
+  CK(h_lambda_.ensure(sizeof(double) * nt), "alloc");
+  CK(h_grad_.ensure(sizeof(double) * nt), "alloc");
+  size_t nsnap = 0;
+  for (int p = 0; p < 4; p++) {
+    CK(d_ops_[p].ensure(sizeof(GhostOp) * prog_[p].ops.size()), "alloc");
+    CK(d_snaps_[p].ensure(sizeof(GhostSnap) * prog_[p].snaps.size()), "alloc");
+    if (!prog_[p].ops.empty())
+      CK(cudaMemcpyAsync(d_ops_[p].p, prog_[p].ops.data(), sizeof(GhostOp) * prog_[p].ops.size(),
+                         cudaMemcpyHostToDevice, stream_), "h2d");
+    if (!prog_[p].snaps.empty())
+      CK(cudaMemcpyAsync(d_snaps_[p].p, prog_[p].snaps.data(), sizeof(GhostSnap) * prog_[p].snaps.size(),
+                         cudaMemcpyHostToDevice, stream_), "h2d");
+    nsnap += 2 * prog_[p].snaps.size();
+  }
+  CK(d_snap_.ensure(sizeof(double) * 8 * (nsnap + 1)), "alloc");
+  // the host vectors above must outlive the async copies
+  CK(cudaStreamSynchronize(stream_), "sync");
+  programs_valid_ = true;
+  return AMR_OK;
+}
+
+int Engine::upload_params() {
+  InstParams *p = h_params_.as<InstParams>();
+  for (size_t q = 0; q < inst_.size(); q++) {
+    p[q].gamma = inst_[q].gamma;
+    p[q].dt = inst_[q].dt;
+    p[q].limiter = inst_[q].limiter;
+    p[q].pad = 0;
+  }
+  CK(cudaMemcpyAsync(d_params_.p, p, sizeof(InstParams) * inst_.size(), cudaMemcpyHostToDevice, stream_), "h2d");
+  return AMR_OK;
+}
+
+// ------------------------------------------------------------- kernels
+int Engine::fill(std::initializer_list<std::pair<FillKind, int>> what) {
+  GhostLaunch g{};
+  int nsnap = 0, nops = 0, q = 0;
+  for (const auto &w : what) {
+    const int nv = field_nv(w.second);
+    const int p = w.first == FILL_CC ? 0 : (w.first == FILL_EC ? 3 : (nv == 2 ? 1 : 2));
+    GhostSeg &s = g.seg[q++];
+    s.ops = d_ops_[p].as<GhostOp>();
+    s.snaps = d_snaps_[p].as<GhostSnap>();
+    s.nops = static_cast<int>(prog_[p].ops.size());
+    s.nsnaps = static_cast<int>(prog_[p].snaps.size());
+    s.snap_off = nsnap;
+    s.field = field_ptr(w.second);
+    s.nv = nv;
+    s.f32 = field_f32(w.second) ? 1 : 0;
+    nsnap += s.nsnaps;
+    nops += s.nops;
+  }
+  g.nseg = q;
+  g.snapbuf = d_snap_.as<double>();
+  CK(launch_ghost(ng_, g, nsnap, nops, stream_), "ghost fill");
+  return AMR_OK;
+}
+
+int Engine::stage(int step) {
+  StageArgs a{};
+  a.tasks = d_tasks_.as<LeafTask>();
+  a.inst = d_params_.as<InstParams>();
+  a.qin = step == 1 ? U_ : Us_;
+  a.qout = step == 1 ? Us_ : U_;
+  a.B = step == 1 ? Bi_ : Bis_;
+  a.ff = ff_;
+  a.gg = gg_;
+  a.err = d_err_.as<DevError>();
+  a.step = step;
+  CK(launch_stage(m_, a, static_cast<int>(tasks_.size()), stream_), "stage kernel");
+  return AMR_OK;
+}
+
+// CT2D.cpp:11-124: EMF, its ghost fill, the face update, its ghost fill and
+// the cell-centred B / energy correction
+int Engine::ct2d(int step) {
+  CtArgs a{};
+  a.tasks = d_tasks_.as<LeafTask>();
+  a.inst = d_params_.as<InstParams>();
+  a.ff = ff_;
+  a.gg = gg_;
+  a.EMF = EMF_;
+  a.Bsrc = step == 1 ? Bi_ : Bis_;
+  a.Bnew = step == 1 ? Bis_ : Bi_;
+  a.q = step == 1 ? Us_ : U_;
+  a.step = step;
+  const int n = static_cast<int>(tasks_.size());
+  CK(launch_ct_emf(m_, a, n, stream_), "ct emf");
+  if (int rc = fill({{FILL_EC, AMR_FIELD_EMF}})) return rc;
+  CK(launch_ct_face(m_, a, n, stream_), "ct face");
+  if (int rc = fill({{FILL_FC, step == 1 ? AMR_FIELD_BIS : AMR_FIELD_BI}})) return rc;
+  CK(launch_ct_cell(m_, a, n, stream_), "ct cell");
+  return AMR_OK;
+}
+
+int Engine::dt_crit(bool want_grad) {
+  DtArgs a{};
+  a.tasks = d_tasks_.as<LeafTask>();
+  a.inst = d_params_.as<InstParams>();
+  a.U = U_;
+  a.lambda = d_lambda_.as<double>();
+  a.grad = d_grad_.as<double>();
+  a.err = d_err_.as<DevError>();
+  a.want_grad = want_grad ? 1 : 0;
+  CK(launch_dt_crit(m_, a, static_cast<int>(tasks_.size()), stream_), "dt kernel");
+  return AMR_OK;
+}
+
+// main.cpp:242-315: ghost fills, stage 1 with CT, stage 2 with CT
+int Engine::enqueue_stage_sequence() {
+  int rc;
+  if ((rc = fill({{FILL_CC, AMR_FIELD_U}, {FILL_FC, AMR_FIELD_BI}}))) return rc;
+  if ((rc = stage(1))) return rc;
+  if ((rc = fill({{FILL_FC, AMR_FIELD_BI}, {FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}}))) return rc;
+  if ((rc = ct2d(1))) return rc;
+  if ((rc = fill({{FILL_CC, AMR_FIELD_US}}))) return rc;
+  if ((rc = stage(2))) return rc;
+  if ((rc = fill({{FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}}))) return rc;
+  if ((rc = ct2d(2))) return rc;
+  if ((rc = fill({{FILL_CC, AMR_FIELD_U}}))) return rc;
+  return AMR_OK;
+}
+
+int Engine::check_device_error() {
+  CK(cudaMemcpyAsync(h_err_.p, d_err_.p, sizeof(DevError), cudaMemcpyDeviceToHost, stream_), "d2h");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  const DevError &e = *h_err_.as<DevError>();
+  if (e.code != 0) {
+    char msg[256];
+    std::snprintf(msg, sizeof msg, "device check failed (code %d) at slot %d cell (%d,%d) value %g", e.code,
+                  e.blk, e.i, e.j, e.value);
+    return fail(map_dev_error(e.code), msg);
+  }
+  return AMR_OK;
+}
+
+}  // namespace amr

@@ -1,0 +1,127 @@
+// The engine behind the C ABI: a pool of block slots resident on one GPU, the
+// host quadtree of every instance, the compiled ghost fills, and the driver of
+// one time step in the order of main.cpp:241-360.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/amr2d_mhd.h"
+#include "amr_common.h"
+#include "ghost_compile.hpp"
+#include "ic.hpp"
+#include "launch.hpp"
+#include "tree.hpp"
+
+namespace amr {
+
+// growable device buffer (contents are not preserved on growth)
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n);
+  void release();
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+// pinned host buffer
+struct HostBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n);
+  void release();
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct Instance {
+  amr_config cfg{};
+  Tree tree;
+  IcId ic = IC_INVALID;
+  double gamma = 0, t_end = 0, cfl = 0;
+  double t = 0, dt = 0, dtn = 0;
+  int64_t count = 0;
+  int64_t cell_updates = 0;
+  bool done = false;
+  int limiter = 0;
+  std::vector<int> slot;      // block ID -> physical slot, -1 if none yet
+  double dx[16] = {0}, dy[16] = {0};
+  int task_begin = 0, task_end = 0;  // this instance's leaves in the task list
+  explicit Instance(const TreeShape &s) : tree(s) {}
+};
+
+class Engine {
+ public:
+  Engine() = default;
+  ~Engine();
+  int create(const amr_config *cfgs, int n);
+  int init();
+  int step();
+  int run(int64_t max_steps);
+  int info(int inst, amr_info *out);
+  int set_stream(cudaStream_t s);
+  // reference-function entry points (instance 0)
+  int api_locate_bounds();
+  int api_boundary(int field);
+  int api_muscl2d_rk(int step);
+  int api_ct2d(int step);
+  int api_cfl_dt(double *lambda_min);
+  int api_admesh();
+  // host <-> device state
+  int get_tree(int inst, int32_t *lp, int32_t *icoord, uint8_t *leafs, int32_t cap);
+  int download(int inst, int field, double *dst, int64_t count);
+  int upload(int inst, int field, const double *src, int64_t count);
+
+  std::string last_error;
+
+ private:
+  int fail(int code, const std::string &msg);
+  int cuda_fail(cudaError_t e, const char *where);
+  int check_device_error();
+  int ensure_slots(int needed);
+  int assign_slots(Instance &in);
+  int rebuild();               // leaf tasks + ghost programs for the active set
+  int upload_params();
+  int enqueue_stage_sequence();
+  int fill(std::initializer_list<std::pair<FillKind, int>> what);
+  int stage(int step);
+  int ct2d(int step);
+  int dt_crit(bool want_grad);
+  int finish_step();
+  int admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad);
+  int xfer(Instance &in, int field, double *host, bool to_device);
+  void *field_ptr(int field) const;
+  int field_nv(int field) const;
+  bool field_f32(int field) const;
+
+  std::vector<Instance> inst_;
+  Method m_{};
+  int ng_ = 2, n_ = 20, nn_ = 400;
+  bool f32_ = false;
+  cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
+  bool initialised_ = false;
+  bool poisoned_ = false;
+
+  // block pool
+  int cap_slots_ = 0, used_slots_ = 0;
+  void *U_ = nullptr, *Us_ = nullptr, *ff_ = nullptr, *gg_ = nullptr;
+  double *Bi_ = nullptr, *Bis_ = nullptr, *EMF_ = nullptr;
+
+  // active set and compiled programs
+  std::vector<int> active_;        // instances stepping this step
+  std::vector<uint64_t> built_version_;
+  std::vector<int> built_active_;
+  bool programs_valid_ = false;
+  std::vector<LeafTask> tasks_;
+  std::vector<int> task_blk_;      // block ID of each task
+  GhostProgram prog_[4];           // cc8, fc2, fc8, ec1
+  DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_[4], d_snaps_[4];
+  DevBuf d_treeops_, d_stage_, d_slots_;
+  HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_stage_;
+  GhostCompiler *gc_ = nullptr;
+};
+
+}  // namespace amr

@@ -1,0 +1,301 @@
+// Engine: initialisation, the time step, remeshing and the reference-function
+// entry points.
+#include <cmath>
+#include <cstring>
+
+#include "aux_kernels.cuh"
+#include "engine.hpp"
+
+namespace amr {
+
+#define CK(expr, where)                                 \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+  } while (0)
+
+// copy blocks [0, lastActive) of one field between a dense float64 host
+// array [block][var][j][i] and the slot pool
+int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
+  const int nblk = in.tree.lastActive;
+  const int per = field_nv(field) * nn_;
+  const size_t bytes = static_cast<size_t>(nblk) * per * sizeof(double);
+  if (nblk == 0) return AMR_OK;
+  CK(d_slots_.ensure(sizeof(int) * nblk), "alloc");
+  CK(h_stage_.ensure(bytes + sizeof(int) * nblk), "alloc");
+  CK(d_stage_.ensure(bytes), "alloc");
+  int *hs = reinterpret_cast<int *>(h_stage_.as<char>() + bytes);
+  std::memcpy(hs, in.slot.data(), sizeof(int) * nblk);
+  CK(cudaMemcpyAsync(d_slots_.p, hs, sizeof(int) * nblk, cudaMemcpyHostToDevice, stream_), "h2d");
+  void *fp = field_ptr(field);
+  if (to_device) {
+    std::memcpy(h_stage_.p, host, bytes);
+    CK(cudaMemcpyAsync(d_stage_.p, h_stage_.p, bytes, cudaMemcpyHostToDevice, stream_), "h2d");
+    CK(launch_scatter(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
+       "scatter");
+    CK(cudaStreamSynchronize(stream_), "sync");
+  } else {
+    CK(launch_gather(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
+       "gather");
+    CK(cudaMemcpyAsync(h_stage_.p, d_stage_.p, bytes, cudaMemcpyDeviceToHost, stream_), "d2h");
+    CK(cudaStreamSynchronize(stream_), "sync");
+    std::memcpy(host, h_stage_.p, bytes);
+  }
+  return AMR_OK;
+}
+
+// admesh.cpp:17-102 for the instances in `which`; the criterion comes from the
+// device reduction of the last dt_crit (or, at initialisation, from the IC's
+// primitive state on the host)
+int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad) {
+  std::vector<TreeOp> ref, crs;
+  for (int q : which) {
+    Instance &in = inst_[q];
+    if (in.cfg.maxlevs <= 1) continue;
+    std::vector<double> grad(in.tree.lastActive, 0.0);
+    if (host_grad) {
+      grad = (*host_grad)[q];
+    } else {
+      const double *hg = h_grad_.as<double>();
+      for (int t = in.task_begin; t < in.task_end; t++) grad[task_blk_[t]] = hg[t];
+    }
+    AdmeshPlan plan;
+    std::string err;
+    if (!in.tree.admesh(grad, plan, err)) return fail(AMR_E_MAXBLOCKS, err);
+    if (int rc = assign_slots(in)) return rc;
+    for (const auto &r : plan.refine)
+      ref.push_back(TreeOp{in.slot[r[0]], {in.slot[r[1]], in.slot[r[2]], in.slot[r[3]], in.slot[r[4]]}, q});
+    for (const auto &c : plan.coarsen)
+      crs.push_back(TreeOp{in.slot[c[0]], {in.slot[c[1]], in.slot[c[2]], in.slot[c[3]], in.slot[c[4]]}, q});
+  }
+  if (ref.empty() && crs.empty()) return AMR_OK;
+  if (int rc = upload_params()) return rc;
+  std::vector<TreeOp> all(ref);
+  all.insert(all.end(), crs.begin(), crs.end());
+  CK(d_treeops_.ensure(sizeof(TreeOp) * all.size()), "alloc");
+  CK(cudaMemcpyAsync(d_treeops_.p, all.data(), sizeof(TreeOp) * all.size(), cudaMemcpyHostToDevice, stream_),
+     "h2d");
+  TreeOpArgs a{};
+  a.ops = d_treeops_.as<TreeOp>();
+  a.inst = d_params_.as<InstParams>();
+  a.U = U_;
+  a.Bi = Bi_;
+  a.err = d_err_.as<DevError>();
+  CK(launch_refine(m_, a, static_cast<int>(ref.size()), stream_), "refine");
+  a.ops = d_treeops_.as<TreeOp>() + ref.size();
+  CK(launch_coarsen(m_, a, static_cast<int>(crs.size()), stream_), "coarsen");
+  return check_device_error();  // also keeps `all` alive until the copy is done
+}
+
+// basegrid + IC2Dtype + W2U + initial admesh (main.cpp:210-229)
+int Engine::init() {
+  if (initialised_) return fail(AMR_E_STATE, "amr_init called twice");
+  if (poisoned_) return fail(AMR_E_STATE, "engine stopped by an earlier error");
+  std::vector<std::vector<double>> grads(inst_.size());
+  for (size_t q = 0; q < inst_.size(); q++) {
+    Instance &in = inst_[q];
+    in.tree.basegrid();
+    if (int rc = assign_slots(in)) return rc;
+    const int nr = in.tree.lastActive;
+    std::vector<double> W(static_cast<size_t>(8) * nn_), U(static_cast<size_t>(nr) * 8 * nn_),
+        B(static_cast<size_t>(nr) * 2 * nn_);
+    grads[q].assign(nr, 0.0);
+    for (int nb = 0; nb < nr; nb++) {
+      IcBlock b{n_, ng_, in.tree.icoord[nb][0], in.tree.icoord[nb][1], in.dx[0], in.dy[0],
+                in.cfg.geometry == 0 ? in.dx[0] : 0.0, in.cfg.geometry == 0 ? in.dy[0] : 0.0};
+      ic_fill(in.ic, in.cfg.ic_param, b, W.data(), B.data() + static_cast<size_t>(nb) * 2 * nn_);
+      prim_to_cons(W.data(), U.data() + static_cast<size_t>(nb) * 8 * nn_, nn_, in.gamma);
+      grads[q][nb] = criteria_grad(W.data(), n_, ng_);
+    }
+    if (int rc = xfer(in, AMR_FIELD_U, U.data(), true)) return rc;
+    if (int rc = xfer(in, AMR_FIELD_BI, B.data(), true)) return rc;
+    in.t = 0.0;
+    in.dt = 0.0;  // dom.dt is read before its first assignment (main.cpp:267 vs :344)
+    in.dtn = 0.0;
+    in.count = 0;
+  }
+  std::vector<int> all(inst_.size());
+  for (size_t q = 0; q < inst_.size(); q++) all[q] = static_cast<int>(q);
+  if (int rc = admesh_all(all, &grads)) return rc;
+  initialised_ = true;
+  return AMR_OK;
+}
+
+int Engine::finish_step() {
+  const size_t nt = tasks_.size();
+  CK(cudaMemcpyAsync(h_lambda_.p, d_lambda_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
+  CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
+  if (int rc = check_device_error()) return rc;
+  const double *hl = h_lambda_.as<double>();
+  for (int a : active_) {
+    Instance &in = inst_[a];
+    double lambda = 1.E6;  // main.cpp:322
+    for (int t = in.task_begin; t < in.task_end; t++) lambda = hl[t] < lambda ? hl[t] : lambda;
+    in.t = in.t + in.dtn;  // main.cpp:344-347
+    in.dt = in.dtn;
+    in.count = in.count + 1;
+    in.dtn = in.cfl * lambda;
+    in.cell_updates += static_cast<int64_t>(in.task_end - in.task_begin) * NI * NI;
+    if (in.dtn < 0 || std::isnan(in.dtn)) return fail(AMR_E_DT, "invalid dt produced");
+  }
+  return admesh_all(active_, nullptr);
+}
+
+// one iteration of main.cpp:241-360 for every instance with t <= t_end
+int Engine::step() {
+  if (!initialised_) return fail(AMR_E_STATE, "amr_init has not been called");
+  if (poisoned_) return fail(AMR_E_STATE, "engine stopped by an earlier error: " + last_error);
+  active_.clear();
+  for (size_t q = 0; q < inst_.size(); q++) {
+    Instance &in = inst_[q];
+    if (!in.done && !(in.t <= in.t_end)) in.done = true;
+    if (!in.done) active_.push_back(static_cast<int>(q));
+  }
+  if (active_.empty()) return AMR_OK;
+  if (int rc = rebuild()) return rc;
+  if (int rc = upload_params()) return rc;
+  if (int rc = enqueue_stage_sequence()) return rc;
+  bool any_amr = false;
+  for (int a : active_) any_amr |= inst_[a].cfg.maxlevs > 1;
+  if (int rc = dt_crit(any_amr)) return rc;
+  return finish_step();
+}
+
+int Engine::run(int64_t max_steps) {
+  for (int64_t s = 0; max_steps < 0 || s < max_steps; s++) {
+    bool any = false;
+    for (const Instance &in : inst_) any |= !in.done && in.t <= in.t_end;
+    if (!any) break;
+    if (int rc = step()) return rc;
+  }
+  return AMR_OK;
+}
+
+int Engine::info(int q, amr_info *o) {
+  if (q < 0 || q >= static_cast<int>(inst_.size()) || !o) return fail(AMR_E_ARG, "bad instance or pointer");
+  const Instance &in = inst_[q];
+  std::memset(o, 0, sizeof(*o));
+  o->t = in.t;
+  o->dt = in.dt;
+  o->dt_next = in.dtn;
+  o->t_end = in.t_end;
+  o->gamma = in.gamma;
+  o->steps = in.count;
+  o->last_active = in.tree.lastActive;
+  int nl = 0;
+  for (int b = 0; b < in.tree.lastActive; b++) nl += in.tree.leafs[b];
+  o->n_leaves = nl;
+  o->nb_leafs = in.tree.nbleafs;
+  o->done = (in.done || !(in.t <= in.t_end)) ? 1 : 0;
+  o->n_instances = static_cast<int>(inst_.size());
+  o->nx_tot = n_;
+  o->ny_tot = n_;
+  o->cell_updates = in.cell_updates;
+  return AMR_OK;
+}
+
+// ------------------------------------------------ reference-function level
+int Engine::api_locate_bounds() {
+  if (!initialised_) return fail(AMR_E_STATE, "amr_init has not been called");
+  active_ = {0};
+  programs_valid_ = false;
+  return rebuild();
+}
+
+int Engine::api_boundary(int field) {
+  if (int rc = api_locate_bounds()) return rc;
+  FillKind k;
+  if (field == AMR_FIELD_U || field == AMR_FIELD_US) k = FILL_CC;
+  else if (field == AMR_FIELD_EMF) k = FILL_EC;
+  else if (field == AMR_FIELD_BI || field == AMR_FIELD_BIS || field == AMR_FIELD_FF || field == AMR_FIELD_GG) k = FILL_FC;
+  else return fail(AMR_E_ARG, "no ghost fill for this field");
+  if (int rc = fill({{k, field}})) return rc;
+  return check_device_error();
+}
+
+int Engine::api_muscl2d_rk(int step) {
+  if (step != 1 && step != 2) return fail(AMR_E_ARG, "step must be 1 or 2");
+  if (int rc = api_locate_bounds()) return rc;
+  if (int rc = upload_params()) return rc;
+  if (int rc = stage(step)) return rc;
+  return check_device_error();
+}
+
+int Engine::api_ct2d(int step) {
+  if (step != 1 && step != 2) return fail(AMR_E_ARG, "step must be 1 or 2");
+  if (int rc = api_locate_bounds()) return rc;
+  if (int rc = upload_params()) return rc;
+  if (int rc = ct2d(step)) return rc;
+  return check_device_error();
+}
+
+int Engine::api_cfl_dt(double *lambda_min) {
+  if (!lambda_min) return fail(AMR_E_ARG, "null pointer");
+  if (int rc = api_locate_bounds()) return rc;
+  if (int rc = upload_params()) return rc;
+  if (int rc = dt_crit(true)) return rc;
+  const size_t nt = tasks_.size();
+  CK(cudaMemcpyAsync(h_lambda_.p, d_lambda_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
+  CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
+  if (int rc = check_device_error()) return rc;
+  double lambda = 1.E6;
+  for (size_t t = 0; t < nt; t++) lambda = h_lambda_.as<double>()[t] < lambda ? h_lambda_.as<double>()[t] : lambda;
+  *lambda_min = lambda;
+  return AMR_OK;
+}
+
+int Engine::api_admesh() {
+  double lam;
+  if (int rc = api_cfl_dt(&lam)) return rc;
+  return admesh_all({0}, nullptr);
+}
+
+// ------------------------------------------------------------ state exchange
+int Engine::get_tree(int q, int32_t *lp, int32_t *icoord, uint8_t *leafs, int32_t cap) {
+  if (q < 0 || q >= static_cast<int>(inst_.size())) return fail(AMR_E_ARG, "bad instance");
+  const Tree &t = inst_[q].tree;
+  if (cap < t.lastActive) return fail(AMR_E_ARG, "capacity smaller than last_active");
+  for (int b = 0; b < t.lastActive; b++) {
+    if (lp) std::memcpy(lp + 8 * b, t.lp[b].data(), 8 * sizeof(int32_t));
+    if (icoord) { icoord[2 * b] = t.icoord[b][0]; icoord[2 * b + 1] = t.icoord[b][1]; }
+    if (leafs) leafs[b] = t.leafs[b];
+  }
+  return AMR_OK;
+}
+
+int Engine::download(int q, int field, double *dst, int64_t count) {
+  if (q < 0 || q >= static_cast<int>(inst_.size()) || !dst) return fail(AMR_E_ARG, "bad instance or pointer");
+  Instance &in = inst_[q];
+  const bool w = field == AMR_FIELD_W;
+  const int f = w ? AMR_FIELD_U : field;
+  if (!field_ptr(f)) return fail(AMR_E_ARG, "unknown field");
+  const int64_t need = static_cast<int64_t>(in.tree.lastActive) * field_nv(f) * nn_;
+  if (count < need) return fail(AMR_E_ARG, "buffer too small");
+  if (int rc = xfer(in, f, dst, false)) return rc;
+  if (w) {  // meshblock.cpp:119-145 on the host
+    const double g = in.gamma;
+    for (int b = 0; b < in.tree.lastActive; b++) {
+      double *u = dst + static_cast<size_t>(b) * 8 * nn_;
+      for (int c = 0; c < nn_; c++) {
+        double x[8];
+        for (int k = 0; k < 8; k++) x[k] = u[k * nn_ + c];
+        const double w1 = x[1] / x[0], w2 = x[2] / x[0], w3 = x[3] / x[0];
+        double p = (g - 1) * (x[4] - 0.5 * x[0] * (w1 * w1 + w2 * w2 + w3 * w3));
+        p = p - (g - 1) * (0.5 * (x[5] * x[5] + x[6] * x[6] + x[7] * x[7]));
+        u[1 * nn_ + c] = w1; u[2 * nn_ + c] = w2; u[3 * nn_ + c] = w3; u[4 * nn_ + c] = p;
+      }
+    }
+  }
+  return AMR_OK;
+}
+
+int Engine::upload(int q, int field, const double *src, int64_t count) {
+  if (q < 0 || q >= static_cast<int>(inst_.size()) || !src) return fail(AMR_E_ARG, "bad instance or pointer");
+  Instance &in = inst_[q];
+  if (!field_ptr(field) || field == AMR_FIELD_W) return fail(AMR_E_ARG, "unknown field");
+  const int64_t need = static_cast<int64_t>(in.tree.lastActive) * field_nv(field) * nn_;
+  if (count < need) return fail(AMR_E_ARG, "buffer too small");
+  return xfer(in, field, const_cast<double *>(src), true);
+}
+
+}  // namespace amr

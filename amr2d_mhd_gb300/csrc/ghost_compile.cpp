@@ -1,0 +1,414 @@
+// Symbolic replay of boundary.cpp / boundaryfc.cpp / boundaryec.cpp /
+// extboundary.cpp; see ghost_compile.hpp.
+#include "ghost_compile.hpp"
+
+#include <algorithm>
+#include <stdexcept>
+#include <unordered_map>
+
+namespace amr {
+
+GhostCompiler::Desc GhostCompiler::get(int blk, int pos) const {
+  const size_t idx = static_cast<size_t>(blk) * nn_ + pos;
+  if (stamp_[idx] == gen_) return cur_[idx];
+  return Desc{blk, static_cast<int16_t>(pos), 0};
+}
+
+void GhostCompiler::set(int blk, int pos, const Desc &d) {
+  const size_t idx = static_cast<size_t>(blk) * nn_ + pos;
+  if (stamp_[idx] != gen_) {
+    stamp_[idx] = gen_;
+    touched_.push_back(static_cast<int>(idx));
+  }
+  cur_[idx] = d;
+}
+
+// One pass over the innerbounds list for one class of variables (the face
+// fill averages k==0 and k>0 along different directions).  The index
+// arithmetic is that of boundary.cpp (identical in the three files).
+void GhostCompiler::run_sequence(const Tree &t, const std::vector<Bound> &bounds, FillKind kind,
+                                 int kclass) {
+  const int n = n_, ng = ng_, nx = n, ny = n;
+  const int nxmin = ng, nxmax = n - 1 - ng, nymin = ng, nymax = n - 1 - ng;
+  const int nxminb = nxmin - 1, nxmaxb = nxmax + 1, nyminb = nymin - 1, nymaxb = nymax + 1;
+  const int nxp1 = nxmaxb, nyp1 = nymaxb;
+  const int nx2 = (n - 1) / 2, ny2 = (n - 1) / 2;
+  const auto &lp = t.lp;
+  const auto &leafs = t.leafs;
+  auto P = [n](int i, int j) { return j * n + i; };
+  auto interior = [&](int i, int j) { return i >= nxmin && i <= nxmax && j >= nymin && j <= nymax; };
+  // plain copy of one cell (all three files)
+  auto C = [&](int db, int di, int dj, int sb, int si, int sj) {
+    set(db, P(di, dj), get(sb, P(si, sj)));
+  };
+  // fine-to-coarse value with lower-left source cell (i1, j1)
+  auto Fv = [&](int db, int di, int dj, int sb, int i1, int j1) {
+    if (kind == FILL_EC) {            // boundaryec.cpp:46-47: injection
+      C(db, di, dj, sb, i1, j1);
+      return;
+    }
+    uint8_t ty;
+    int i2 = i1 + 1, j2 = j1 + 1;
+    if (kind == FILL_CC) ty = GOP_AVG4;
+    else if (kclass == 0) { ty = GOP_AVGJ; i2 = i1; }
+    else { ty = GOP_AVGI; j2 = j1; }
+    // with 4 ghost layers the reference's left / bottom fine-to-coarse
+    // stencils reach one ghost column / row of the fine block (boundary.cpp:43
+    // and :227 give 2i+13 where 2i+12 is meant); such a cell must still hold
+    // its pre-fill value here, and compile() snapshots it if the fill
+    // overwrites it later
+    for (int i = i1; i <= i2; i++)
+      for (int j = j1; j <= j2; j++) {
+        const Desc d = get(sb, P(i, j));
+        if (!interior(i, j) && !(d.type == 0 && d.blk == sb && d.pos == P(i, j)))
+          throw std::logic_error("ghost compile: fine average of an already filled ghost cell");
+      }
+    set(db, P(di, dj), Desc{sb, static_cast<int16_t>(P(i1, j1)), ty});
+  };
+
+  for (const Bound &b : bounds) {
+    const int nbs = b.src;
+    int n1, n2, n3, n4, ii, jj;
+    switch (b.code) {
+      case 1:  // left, same level (boundary.cpp:17-35)
+        n1 = b.dst;
+        for (int j = 0; j < ny; j++) {
+          ii = nxmax - (ng - 1);
+          for (int i = 0; i < ng; i++, ii++) C(nbs, i, j, n1, ii, j);
+          ii = nxmin;
+          for (int i = nxp1; i < nx; i++, ii++) C(n1, i, j, nbs, ii, j);
+        }
+        break;
+      case 2:  // left, finer neighbour (boundary.cpp:36-107)
+        n1 = b.dst;
+        n2 = n1 + 2;
+        for (int j = nymin; j <= ny2; j++) {
+          const int ny2j = ny2 + j - 1 - (ng - 2);
+          for (int i = 0; i < ng; i++) {
+            const int i1 = 2 * (i - ng / 2) - ng / 2 + nxmax, j1 = 2 * j - nymin;
+            Fv(nbs, i, j, n1, i1, j1);
+            Fv(nbs, i, ny2j, n2, i1, j1);
+          }
+        }
+        n3 = lp[lp[n1][1]][6];
+        if (n3 != -1) {
+          if (leafs[n3]) {
+            for (int i = 0; i < ng; i++)
+              for (int j = 0; j < ng; j++) C(nbs, i, j, n3, nxmax - ng + (i + 1), nymax - ng + (j + 1));
+          } else {
+            n3 = lp[n3][2] + 3;
+            if (leafs[n3])
+              for (int i = 0; i < ng; i++)
+                for (int j = 0; j < ng; j++)
+                  Fv(nbs, i, j, n3, nxmax - ng * 2 + 2 * i + 1, nymax - ng * 2 + 2 * j + 1);
+          }
+        }
+        n4 = lp[lp[n2][1]][7];
+        if (n4 != -1) {
+          if (leafs[n4]) {
+            for (int i = 0; i < ng; i++)
+              for (int j = 0; j < ng; j++)
+                C(nbs, i, ny - 1 - j, n4, nxmax - ng + (i + 1), nymin + ng - (j + 1));
+          } else {
+            n4 = lp[n4][2] + 1;
+            if (leafs[n4])
+              for (int i = 0; i < ng; i++)
+                for (int j = 0; j < ng; j++)
+                  Fv(nbs, i, ny - 1 - j, n4, nxmax - ng * 2 + 2 * i + 1, nymin + ng * 2 - 2 * (j + 1));
+          }
+        }
+        for (int i = 1; i <= ng; i++)
+          for (int j = 0; j < ny; j++) {
+            C(n1, i + nxmax, j, nbs, (i + 2 * ng - 1) / 2, (j + ng) / 2);
+            C(n2, i + nxmax, j, nbs, (i + 2 * ng - 1) / 2, (j - ng + 2) / 2 + ny2);
+          }
+        break;
+      case 4:  // right, same level (boundary.cpp:109-127)
+        n1 = b.dst;
+        for (int j = 0; j < ny; j++) {
+          ii = nxmin;
+          for (int i = nxp1; i < nx; i++, ii++) C(nbs, i, j, n1, ii, j);
+          ii = nxmax - (ng - 1);
+          for (int i = 0; i < ng; i++, ii++) C(n1, i, j, nbs, ii, j);
+        }
+        break;
+      case 5:  // right, finer neighbour (boundary.cpp:128-197)
+        n1 = b.dst;
+        n2 = n1 + 2;
+        for (int i = nxp1; i < nx; i++)
+          for (int j = nymin; j <= ny2; j++) {
+            const int i1 = 2 * (i - nxmax + (ng / 2 - 1)), j1 = 2 * j - nymin;
+            const int ny2j = ny2 + j - 1 - (ng - 2);
+            Fv(nbs, i, j, n1, i1, j1);
+            Fv(nbs, i, ny2j, n2, i1, j1);
+          }
+        n3 = lp[lp[n1][1]][6];
+        if (n3 != -1) {
+          if (leafs[n3]) {
+            for (int i = nxmaxb; i < nx; i++)
+              for (int j = 0; j < ng; j++) C(nbs, i, j, n3, nxminb + (i - nxmax), nymax - ng + (j + 1));
+          } else {
+            n3 = lp[n3][2] + 2;
+            if (leafs[n3])
+              for (int i = nxmaxb; i < nx; i++)
+                for (int j = 0; j < ng; j++)
+                  Fv(nbs, i, j, n3, nxminb + 2 * (i - nxmax) - 1, nymax - ng * 2 + 2 * j + 1);
+          }
+        }
+        n4 = lp[lp[n2][1]][7];
+        if (n4 != -1) {
+          if (leafs[n4]) {
+            for (int i = nxmaxb; i < nx; i++)
+              for (int j = 0; j < ng; j++)
+                C(nbs, i, ny - 1 - j, n4, nxminb + (i - nxmax), nymin + ng - (j + 1));
+          } else {
+            n4 = lp[n4][2];
+            if (leafs[n4])
+              for (int i = nxmaxb; i < nx; i++)
+                for (int j = 0; j < ng; j++)
+                  Fv(nbs, i, ny - 1 - j, n4, nxminb + 2 * (i - nxmax) - 1, nymin + ng * 2 - 2 * (j + 1));
+          }
+        }
+        for (int i = 1; i <= ng; i++)
+          for (int j = 0; j < ny; j++) {
+            C(n1, i - 1, j, nbs, (i + 1) / 2 + nxmax - ng / 2, (j + ng) / 2);
+            C(n2, i - 1, j, nbs, (i + 1) / 2 + nxmax - ng / 2, (j - ng + 2) / 2 + ny2);
+          }
+        break;
+      case 7:  // bottom, same level (boundary.cpp:199-217)
+        n1 = b.dst;
+        for (int i = 0; i < nx; i++) {
+          jj = nymax - (ng - 1);
+          for (int j = 0; j < ng; j++, jj++) C(nbs, i, j, n1, i, jj);
+          jj = nymin;
+          for (int j = nyp1; j < ny; j++, jj++) C(n1, i, j, nbs, i, jj);
+        }
+        break;
+      case 8:  // bottom, finer neighbour (boundary.cpp:218-287)
+        n1 = b.dst;
+        n2 = n1 + 1;
+        for (int i = nxmin; i <= nx2; i++) {
+          const int nx2i = nx2 + i - 1 - (ng - 2);
+          for (int j = 0; j < ng; j++) {
+            const int i1 = 2 * i - nxmin, j1 = 2 * (j - ng / 2) - ng / 2 + nymax;
+            Fv(nbs, i, j, n1, i1, j1);
+            Fv(nbs, nx2i, j, n2, i1, j1);
+          }
+        }
+        n3 = lp[lp[n1][1]][4];
+        if (n3 != -1) {
+          if (leafs[n3]) {
+            for (int i = 0; i < ng; i++)
+              for (int j = 0; j < ng; j++) C(nbs, i, j, n3, nxmax - ng + (i + 1), nymax - ng + (j + 1));
+          } else {
+            n3 = lp[n3][2] + 3;
+            if (leafs[n3])
+              for (int i = 0; i < ng; i++)
+                for (int j = 0; j < ng; j++)
+                  Fv(nbs, i, j, n3, nxmax - ng * 2 + 2 * i + 1, nymax - ng * 2 + 2 * j + 1);
+          }
+        }
+        n4 = lp[lp[n2][1]][5];
+        if (n4 != -1) {
+          if (leafs[n4]) {
+            for (int i = 0; i < ng; i++)
+              for (int j = 0; j < ng; j++)
+                C(nbs, nx - 1 - i, j, n4, nxmin + ng - (i + 1), nymax - ng + (j + 1));
+          } else {
+            n4 = lp[n4][2] + 2;
+            if (leafs[n4])
+              for (int i = 0; i < ng; i++)
+                for (int j = 0; j < ng; j++)
+                  Fv(nbs, nx - 1 - i, j, n4, nxmin + ng * 2 - 2 * (i + 1), nymax - ng * 2 + 2 * j + 1);
+          }
+        }
+        for (int j = 1; j <= ng; j++)
+          for (int i = 0; i < nx; i++) {
+            C(n1, i, j + nymax, nbs, (i + ng) / 2, (j + 2 * ng - 1) / 2);
+            C(n2, i, j + nymax, nbs, (i - ng + 2) / 2 + nx2, (j + 2 * ng - 1) / 2);
+          }
+        break;
+      case 10:  // top, same level (boundary.cpp:289-307)
+        n1 = b.dst;
+        for (int i = 0; i < nx; i++) {
+          jj = nymin;
+          for (int j = nyp1; j < ny; j++, jj++) C(nbs, i, j, n1, i, jj);
+          jj = nymax - (ng - 1);
+          for (int j = 0; j < ng; j++, jj++) C(n1, i, j, nbs, i, jj);
+        }
+        break;
+      case 11:  // top, finer neighbour (boundary.cpp:308-377)
+        n1 = b.dst;
+        n2 = n1 + 1;
+        for (int i = nxmin; i <= nx2; i++)
+          for (int j = nyp1; j < ny; j++) {
+            const int i1 = 2 * i - nxmin, j1 = 2 * (j - nymax + (ng / 2 - 1));
+            const int nx2i = nx2 + i - 1 - (ng - 2);
+            Fv(nbs, i, j, n1, i1, j1);
+            Fv(nbs, nx2i, j, n2, i1, j1);
+          }
+        n3 = lp[lp[n1][1]][4];
+        if (n3 != -1) {
+          if (leafs[n3]) {
+            for (int i = 0; i < ng; i++)
+              for (int j = nymaxb; j < ny; j++) C(nbs, i, j, n3, nxmax - ng + (i + 1), nyminb + (j - nymax));
+          } else {
+            n3 = lp[n3][2] + 1;
+            if (leafs[n3])
+              for (int i = 0; i < ng; i++)
+                for (int j = nymaxb; j < ny; j++)
+                  Fv(nbs, i, j, n3, nxmax - ng * 2 + 2 * i + 1, nyminb + 2 * (j - nymax) - 1);
+          }
+        }
+        n4 = lp[lp[n2][1]][5];
+        if (n4 != -1) {
+          if (leafs[n4]) {
+            for (int i = 0; i < ng; i++)
+              for (int j = nymaxb; j < ny; j++)
+                C(nbs, nx - 1 - i, j, n4, nxmin + ng - (i + 1), nyminb + (j - nymax));
+          } else {
+            n4 = lp[n4][2];
+            if (leafs[n4])
+              for (int i = nxmaxb; i < nx; i++)
+                for (int j = nymaxb; j < ny; j++)
+                  Fv(nbs, i, j, n4, nxminb + 2 * (i - nxmax) - 1, nyminb + 2 * (j - nymax) - 1);
+          }
+        }
+        for (int j = 1; j <= ng; j++)
+          for (int i = 0; i < nx; i++) {
+            C(n1, i, j - 1, nbs, (i + ng) / 2, (j + 1) / 2 + nymax - ng / 2);
+            C(n2, i, j - 1, nbs, (i - ng + 2) / 2 + nx2, (j + 1) / 2 + nymax - ng / 2);
+          }
+        break;
+      default:
+        break;
+    }
+  }
+  // extboundary.cpp:5-61: mirror copy at the box, after all internal bounds
+  for (const Bound &b : bounds) {
+    const int nbs = b.src;
+    int ii, jj;
+    switch (b.code) {
+      case -1:
+        ii = nxmin + (ng - 1);
+        for (int i = 0; i < ng; i++, ii--)
+          for (int j = 0; j < ny; j++) C(nbs, i, j, nbs, ii, j);
+        break;
+      case -2:
+        ii = nxmax;
+        for (int i = nxp1; i < nx; i++, ii--)
+          for (int j = 0; j < ny; j++) C(nbs, i, j, nbs, ii, j);
+        break;
+      case -3:
+        jj = nymin + (ng - 1);
+        for (int j = 0; j < ng; j++, jj--)
+          for (int i = 0; i < nx; i++) C(nbs, i, j, nbs, i, jj);
+        break;
+      case -4:
+        jj = nymax;
+        for (int j = nyp1; j < ny; j++, jj--)
+          for (int i = 0; i < nx; i++) C(nbs, i, j, nbs, i, jj);
+        break;
+      default:
+        break;
+    }
+  }
+}
+
+void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, FillKind kind,
+                            int nv, const int *slot, uint8_t field, GhostProgram &out) {
+  nn_ = n_ * n_;
+  const size_t need = static_cast<size_t>(t.lastActive) * nn_;
+  if (stamp_.size() < need) {
+    stamp_.resize(need, 0);
+    cur_.resize(need);
+  }
+  const int nclass = (kind == FILL_FC && nv > 1) ? 2 : 1;
+  for (int kc = 0; kc < nclass; kc++) {
+    int k0 = 0, k1 = nv;
+    if (kind == FILL_FC) { k0 = kc == 0 ? 0 : 1; k1 = kc == 0 ? 1 : nv; }
+    if (++gen_ == 0) {  // stamp wrap-around
+      std::fill(stamp_.begin(), stamp_.end(), 0u);
+      gen_ = 1;
+    }
+    touched_.clear();
+    run_sequence(t, bounds, kind, kc);
+    std::sort(touched_.begin(), touched_.end());
+    std::unordered_map<int, int> snap_of;
+    for (const int idx : touched_) {
+      const Desc &d = cur_[idx];
+      const int blk = idx / nn_, pos = idx % nn_;
+      if (d.type == 0 && d.blk == blk && d.pos == pos) continue;  // unchanged
+      GhostOp op{};
+      op.dst_slot = slot[blk];
+      op.dst_pos = static_cast<int16_t>(pos);
+      op.k0 = static_cast<uint8_t>(k0);
+      op.k1 = static_cast<uint8_t>(k1);
+      op.field = field;
+      if (d.type == 0) {
+        const int sidx = d.blk * nn_ + d.pos;
+        const Desc &s = cur_[sidx];
+        const bool overwritten =
+            stamp_[sidx] == gen_ && !(s.type == 0 && s.blk == d.blk && s.pos == d.pos);
+        if (overwritten) {
+          auto it = snap_of.find(sidx);
+          int si;
+          if (it == snap_of.end()) {
+            si = static_cast<int>(out.snaps.size());
+            GhostSnap sn{};
+            sn.slot = slot[d.blk];
+            sn.pos = d.pos;
+            sn.k0 = op.k0;
+            sn.k1 = op.k1;
+            sn.field = field;
+            out.snaps.push_back(sn);
+            snap_of.emplace(sidx, si);
+          } else {
+            si = it->second;
+          }
+          op.type = GOP_SNAP;
+          op.src_slot = si;
+          op.src_pos = 0;
+        } else {
+          op.type = GOP_COPY;
+          op.src_slot = slot[d.blk];
+          op.src_pos = d.pos;
+        }
+      } else {
+        // stencil of the average in sum_irjr order
+        int cells[4], nc = 0;
+        const int p0 = d.pos;
+        if (d.type == GOP_AVG4) { cells[0] = p0; cells[1] = p0 + n_; cells[2] = p0 + 1; cells[3] = p0 + 1 + n_; nc = 4; }
+        else if (d.type == GOP_AVGJ) { cells[0] = p0; cells[1] = p0 + n_; nc = 2; }
+        else { cells[0] = p0; cells[1] = p0 + 1; nc = 2; }
+        bool hazard = false;
+        for (int q = 0; q < nc; q++) {
+          const int sidx = d.blk * nn_ + cells[q];
+          const Desc &s = cur_[sidx];
+          hazard |= stamp_[sidx] == gen_ && !(s.type == 0 && s.blk == d.blk && s.pos == cells[q]);
+        }
+        if (!hazard) {
+          op.type = d.type;
+          op.src_slot = slot[d.blk];
+          op.src_pos = d.pos;
+        } else {  // average of saved pre-fill values
+          op.type = static_cast<uint8_t>(d.type + (GOP_SAVG4 - GOP_AVG4));
+          op.src_slot = static_cast<int>(out.snaps.size());
+          op.src_pos = 0;
+          for (int q = 0; q < nc; q++) {
+            GhostSnap sn{};
+            sn.slot = slot[d.blk];
+            sn.pos = static_cast<int16_t>(cells[q]);
+            sn.k0 = op.k0;
+            sn.k1 = op.k1;
+            sn.field = field;
+            out.snaps.push_back(sn);
+          }
+        }
+      }
+      out.ops.push_back(op);
+    }
+  }
+}
+
+}  // namespace amr

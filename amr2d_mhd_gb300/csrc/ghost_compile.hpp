@@ -1,0 +1,57 @@
+// Compiles the reference's sequential ghost fills into order-free gather lists.
+//
+// boundary.cpp / boundaryfc.cpp / boundaryec.cpp walk the innerbounds list in
+// order and copy or average cells between blocks; later copies can read ghost
+// cells that earlier ones wrote (full-height column copies include the source's
+// ghost rows, injections read the coarse block's ghost ring), so the result
+// depends on the order.  The compiler replays that order symbolically on the
+// host: every ghost cell ends up as "the pre-fill value of cell X" or "the
+// average of interior cells of block B".  The GPU then applies all gathers at
+// once; pre-fill values of cells the same fill overwrites are saved first
+// (GhostSnap).  The result is bit-identical to the sequential walk.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "amr_common.h"
+#include "tree.hpp"
+
+namespace amr {
+
+enum FillKind { FILL_CC = 0, FILL_FC = 1, FILL_EC = 2 };
+
+struct GhostProgram {
+  std::vector<GhostOp> ops;
+  std::vector<GhostSnap> snaps;
+  void clear() { ops.clear(); snaps.clear(); }
+};
+
+class GhostCompiler {
+ public:
+  // n = block edge with ghosts, ng = ghost layers
+  GhostCompiler(int n, int ng) : n_(n), ng_(ng) {}
+  // Appends the gathers of one fill of a field with `nv` variables of one
+  // instance's tree.  `slot` maps block IDs to physical device slots.
+  void compile(const Tree &t, const std::vector<Bound> &bounds, FillKind kind, int nv,
+               const int *slot, uint8_t field, GhostProgram &out);
+
+ private:
+  struct Desc {
+    int blk;        // block ID (logical)
+    int16_t pos;    // j * n + i
+    uint8_t type;   // 0 = pre-fill value of (blk,pos); GOP_AVG4 / AVGJ / AVGI of interior cells
+  };
+  Desc get(int blk, int pos) const;
+  void set(int blk, int pos, const Desc &d);
+  void run_sequence(const Tree &t, const std::vector<Bound> &bounds, FillKind kind, int kclass);
+
+  int n_, ng_;
+  int nn_ = 0;
+  uint32_t gen_ = 0;
+  std::vector<uint32_t> stamp_;
+  std::vector<Desc> cur_;
+  std::vector<int> touched_;
+};
+
+}  // namespace amr

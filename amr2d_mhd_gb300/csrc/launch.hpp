@@ -1,0 +1,54 @@
+// Host-side launchers of the sm_103a kernels (defined in the .cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "amr_common.h"
+
+namespace amr {
+
+struct StageArgs;
+struct GhostLaunch;
+struct CtArgs;
+struct DtArgs;
+struct TreeOpArgs;
+
+struct Method {
+  int ng;      // ghost layers: 2, or 4 (WENO5)
+  int recon;   // Recon
+  int flux;    // Flux
+  int f32;     // FP32 bulk storage / arithmetic
+};
+
+// true if the (ng, recon, flux, precision) combination is compiled
+bool method_supported(const Method &m);
+
+cudaError_t launch_stage(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s);
+// per-precision, per-flux entry points (one translation unit each)
+#define AMR_DECL_STAGE(P, F) \
+  cudaError_t launch_stage_##P##_##F(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s);
+AMR_DECL_STAGE(f64, rusa)
+AMR_DECL_STAGE(f64, hlle)
+AMR_DECL_STAGE(f64, hllc)
+AMR_DECL_STAGE(f64, hlld)
+AMR_DECL_STAGE(f32, rusa)
+AMR_DECL_STAGE(f32, hlle)
+AMR_DECL_STAGE(f32, hllc)
+AMR_DECL_STAGE(f32, hlld)
+#undef AMR_DECL_STAGE
+
+// ghost fill: snapshot pass (if any snapshots) then the gather pass
+cudaError_t launch_ghost(int ng, const GhostLaunch &g, int nsnaps, int nops, cudaStream_t s);
+cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
+cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
+cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
+cudaError_t launch_dt_crit(const Method &m, const DtArgs &a, int ntasks, cudaStream_t s);
+cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int nops, cudaStream_t s);
+cudaError_t launch_coarsen(const Method &m, const TreeOpArgs &a, int nops, cudaStream_t s);
+
+cudaError_t launch_gather(const int *slots, int nblk, const void *src, int f32, int per, double *dst,
+                          cudaStream_t s);
+cudaError_t launch_scatter(const int *slots, int nblk, void *dst, int f32, int per, const double *src,
+                           cudaStream_t s);
+
+}  // namespace amr

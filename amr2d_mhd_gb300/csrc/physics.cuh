@@ -1,0 +1,413 @@
+// Device physics of the per-face update: slope limiters, WENO weights, MHD
+// wave speeds and the Riemann solvers.  Templated on the arithmetic type T.
+// The double instantiation is compiled without FMA contraction and evaluates
+// every expression in the reference's order, so it reproduces the reference
+// bit for bit; the float instantiation is the FP32 bulk path.
+#pragma once
+
+#include "amr_common.h"
+
+namespace amr {
+
+// defs.hpp:110-111 macros and std::min / std::max (they differ for equal and
+// NaN arguments; each call site uses the form of the reference)
+template <typename T> __device__ __forceinline__ T mmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T mmax(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T smin(T a, T b) { return b < a ? b : a; }
+template <typename T> __device__ __forceinline__ T smax(T a, T b) { return a < b ? b : a; }
+template <typename T> __device__ __forceinline__ T sgn(T v) { return v > T(0) ? T(1) : (v < T(0) ? T(-1) : T(0)); }
+template <typename T> __device__ __forceinline__ T eps_of();
+template <> __device__ __forceinline__ double eps_of<double>() { return 1.0E-15; }
+template <> __device__ __forceinline__ float eps_of<float>() { return 1.0E-6f; }  // defs.hpp:20
+
+// slopelimiter.cpp:6-54
+template <typename T>
+__device__ __forceinline__ T slope_limiter(int lim, T r, T eta) {
+  const T E = eps_of<T>();
+  switch (lim) {
+    case LIM_1ST: return T(0);
+    case LIM_NOSL: return r;
+    case LIM_MINMOD: { T a = mmin(T(1), r); return mmax(T(0), a); }
+    case LIM_VANLEER: return (fabs(r) + r) / (T(1) + fabs(r));
+    case LIM_SUPERBEE: {
+      T a = T(2) * r;
+      T b = mmin(a, T(1));
+      a = mmin(r, T(2));
+      T c = mmax(a, b);
+      return mmax(T(0), c);
+    }
+    case LIM_MC: {
+      T a = T(2) * r, b = T(0.5) * (T(1) + r);
+      T c = mmin(a, b);
+      a = mmin(c, T(2));
+      return mmax(T(0), a);
+    }
+    case LIM_KOREN: {
+      T a = (T(1) + T(2) * r) / T(3);
+      T b = mmin(a, T(2));
+      a = T(2) * r;
+      T c = mmin(a, b);
+      return mmax(T(0), c);
+    }
+    case LIM_CADA3RD: {
+      T a = mmin(T(2) * r, (T(2) + r) / T(3));
+      T b = mmin(a, T(1.6));
+      T ph = mmax(T(-0.5) * r, b);
+      a = mmin((T(2) + r) / T(3), ph);
+      ph = mmax(T(0), a);
+      if (eta <= T(1) - E) return (T(2) + r) / T(3);
+      if (eta >= T(1) + E) return ph;
+      return T(0.5) * ((T(1) - (eta - T(1)) / E) * (T(2) + r) / T(3) + (T(1) + (eta - T(1)) / E) * ph);
+    }
+    default: return T(0);
+  }
+}
+
+// celledges.cpp:38-43 for one variable of one face.  dA = W[i]-W[i-1],
+// dB = W[i+1]-W[i], dC = W[i+2]-W[i+1] around the face i+1/2; returns the
+// left state wxL[i] and right state wxR[i+1].  inv2 = 1/(dx*dx) for Cada3rd.
+template <typename T>
+__device__ __forceinline__ void muscl_face(int lim, T wi, T wip, T dA, T dB, T dC, T h,
+                                           T &left, T &right) {
+  const T E = eps_of<T>();
+  T etaL = T(0), etaR = T(0);
+  if (lim == LIM_CADA3RD) {
+    etaL = (dB * dB + dA * dA) / ((T(1) * h) * (T(1) * h));
+    etaR = (dC * dC + dB * dB) / ((T(1) * h) * (T(1) * h));
+  }
+  T r = dB / (dA + E);
+  T phi = slope_limiter<T>(lim, r, etaL);
+  left = wi + T(0.5) * phi * dA;
+  r = dB / (dC + E);
+  phi = slope_limiter<T>(lim, r, etaR);
+  right = wip - T(0.5) * phi * dC;
+}
+
+// WENO2D_primvar.cpp:43-87: the two WENO3 face values of a cell with
+// neighbours wm, wp.  vR is the value at its left face (wxR), vL at its right
+// face (wxL).
+template <typename T>
+__device__ __forceinline__ void weno3_cell(T wm, T w, T wp, T &vL, T &vR) {
+  const T e = eps_of<T>();
+  {
+    T p0n = T(0.5) * wm + T(0.5) * w, p1n = T(1.5) * w - T(0.5) * wp;
+    T B0n = (w - wm) * (w - wm), B1n = (wp - w) * (wp - w);
+    T d0n = T(2.) / T(3.), d1n = T(1.) / T(3.);
+    T a0n = d0n / ((e + B0n) * (e + B0n)), a1n = d1n / ((e + B1n) * (e + B1n));
+    T asn = a0n + a1n;
+    T w0n = a0n / asn, w1n = a1n / asn;
+    vR = w0n * p0n + w1n * p1n;
+  }
+  {
+    T p0p = T(1.5) * w - T(0.5) * wm, p1p = T(0.5) * wp + T(0.5) * w;
+    T B0p = (w - wm) * (w - wm), B1p = (wp - w) * (wp - w);
+    T d0p = T(1.) / T(3.), d1p = T(2.) / T(3.);
+    T a0p = d0p / ((e + B0p) * (e + B0p)), a1p = d1p / ((e + B1p) * (e + B1p));
+    T asp = a0p + a1p;
+    T w0p = a0p / asp, w1p = a1p / asp;
+    vL = w0p * p0p + w1p * p1p;
+  }
+}
+
+// WENO2D_primvar.cpp:140-193 (beta_1 takes the -2 neighbour, :145,174).
+// RIGHT selects wxR (value at the cell's left face) or wxL.
+template <typename T, bool RIGHT>
+__device__ __forceinline__ T weno5_cell(T wmm, T wm, T w, T wp, T wpp) {
+  const T e = eps_of<T>();
+  const T c13 = T(13.) / T(12.), c14 = T(1.) / T(4.);
+  T t, t2;
+  if (RIGHT) {
+    T p0n = (T(-1) * wmm + T(5) * wm + T(2) * w) / T(6);
+    T p1n = (T(2) * wm + T(5) * w - wp) / T(6);
+    T p2n = (T(11) * w - T(7) * wp + T(2) * wpp) / T(6);
+    t = wmm - T(2) * wm + w; t2 = wmm - T(4) * wm + T(3) * w;
+    T B0 = c13 * (t * t) + c14 * (t2 * t2);
+    t = wmm - T(2) * w + wp; t2 = wm - wp;
+    T B1 = c13 * (t * t) + c14 * (t2 * t2);
+    t = w - T(2) * wp + wpp; t2 = T(3) * w - T(4) * wp + wpp;
+    T B2 = c13 * (t * t) + c14 * (t2 * t2);
+    T d0 = T(1.) / T(10.), d1 = T(6.) / T(10.), d2 = T(3.) / T(10.);
+    T a0 = d0 / ((e + B0) * (e + B0)), a1 = d1 / ((e + B1) * (e + B1)), a2 = d2 / ((e + B2) * (e + B2));
+    T as = a0 + a1 + a2;
+    T w0 = a0 / as, w1 = a1 / as, w2 = a2 / as;
+    return w0 * p0n + w1 * p1n + w2 * p2n;
+  } else {
+    T p0p = (T(2) * wmm - T(7) * wm + T(11) * w) / T(6);
+    T p1p = (T(-1) * wm + T(5) * w + T(2) * wp) / T(6);
+    T p2p = (T(2) * w + T(5) * wp - wpp) / T(6);
+    t = wmm - T(2) * wm + w; t2 = wmm - T(4) * wm + T(3) * w;
+    T B0 = c13 * (t * t) + c14 * (t2 * t2);
+    t = wmm - T(2) * w + wp; t2 = wm - wp;
+    T B1 = c13 * (t * t) + c14 * (t2 * t2);
+    t = w - T(2) * wp + wpp; t2 = T(3) * w - T(4) * wp + wpp;
+    T B2 = c13 * (t * t) + c14 * (t2 * t2);
+    T d0 = T(3.) / T(10.), d1 = T(6.) / T(10.), d2 = T(1.) / T(10.);
+    T a0 = d0 / ((e + B0) * (e + B0)), a1 = d1 / ((e + B1) * (e + B1)), a2 = d2 / ((e + B2) * (e + B2));
+    T as = a0 + a1 + a2;
+    T w0 = a0 / as, w1 = a1 / as, w2 = a2 / as;
+    return w0 * p0p + w1 * p1p + w2 * p2p;
+  }
+}
+
+// misc.cpp:71-79, fast magnetosonic speed along component `norm`
+template <typename T>
+__device__ __forceinline__ T fast_speed(const T *w, T gamma, int norm) {
+  T ca = sqrt((w[5] * w[5] + w[6] * w[6] + w[7] * w[7]) / w[0]);
+  T a = sqrt(gamma * w[4] / w[0]);
+  T can = sqrt((w[norm] * w[norm]) / w[0]);
+  T i0 = (ca * ca) + (a * a);
+  T i1 = (ca * ca) - (a * a);
+  return sqrt(T(0.5) * (i0 + sqrt(i1 * i1 + T(4.) * (a * a) * ((ca * ca) - (can * can)))));
+}
+
+// conserved state, physical flux, enthalpy, total pressure and energy of one
+// side (riemannS.cpp:59-108)
+template <typename T>
+struct Side {
+  T q[8], F[8], H, pt, cf, e;
+};
+
+template <typename T>
+__device__ __forceinline__ void side_state(const T *w, T gamma, Side<T> &s) {
+  s.cf = fast_speed<T>(w, gamma, 5);
+  const T vn = w[1], Bn = w[5];
+  T e = (w[4] / (w[0] * (gamma - T(1)))) + T(0.5) * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]) +
+        T(0.5) * (w[5] * w[5] + w[6] * w[6] + w[7] * w[7]) / w[0];
+  e = e * w[0];
+  s.e = e;
+  s.H = (e + w[4] + T(0.5) * (w[5] * w[5] + w[6] * w[6] + w[7] * w[7])) / w[0];
+#pragma unroll
+  for (int k = 0; k < 8; k++) s.q[k] = w[k];
+  s.q[1] = w[0] * w[1]; s.q[2] = w[0] * w[2]; s.q[3] = w[0] * w[3];
+  s.q[4] = e;
+  const T pt = w[4] + T(0.5) * (w[5] * w[5] + w[6] * w[6] + w[7] * w[7]);
+  s.pt = pt;
+  s.F[0] = w[0] * vn;
+  s.F[1] = w[0] * vn * w[1] + pt - Bn * w[5];
+  s.F[2] = w[0] * vn * w[2] - Bn * w[6];
+  s.F[3] = w[0] * vn * w[3] - Bn * w[7];
+  s.F[4] = w[0] * vn * s.H - Bn * (w[1] * w[5] + w[2] * w[6] + w[3] * w[7]);
+  s.F[5] = vn * w[5] - Bn * w[1];
+  s.F[6] = vn * w[6] - Bn * w[2];
+  s.F[7] = vn * w[7] - Bn * w[3];
+}
+
+// misc.cpp:95-140 Roe averages (sqrt(rhoL + sqrt(rhoR)) denominator as in
+// the reference, :98,100) and the outer eigenvalues lambda_0 / lambda_6
+template <typename T>
+__device__ __forceinline__ void roe_outer(const T *wL, const T *wR, T HL, T HR, T gamma, T &vx,
+                                          T &l0, T &l6) {
+  T v[3], B[3];
+  const T sl = sqrt(wL[0]), sr = sqrt(wR[0]);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    v[i] = (sl * wL[i + 1] + sr * wR[i + 1]) / (sqrt(wL[0] + sr));
+    B[i] = (sl * wL[i + 5] + sr * wR[i + 5]) / (sqrt(wL[0] + sr));
+  }
+  const T RT = sqrt(wR[0] / wL[0]);
+  const T d = sqrt(wR[0] * wL[0]);
+  const T d6 = wL[6] - wR[6], d7 = wL[7] - wR[7];
+  const T Xfac = T(0.5) * (d6 * d6 + d7 * d7) / (sl + sr);
+  const T Yfac = T(0.5) * (wL[0] + wR[0]) / d;
+  const T h = (HL + RT * HR) / (T(1) + RT);
+  const T vsq = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  const T btsq = B[1] * B[1] + B[2] * B[2];
+  const T bt_starsq = (gamma - T(1.) - (gamma - T(2)) * Yfac) * btsq;
+  const T vaxsq = B[0] * B[0] / d;
+  const T hp = h - (vaxsq + btsq / d);
+  T twid_asq = ((gamma - T(1.)) * (hp - T(0.5) * vsq) - (gamma - T(2.)) * Xfac);
+  twid_asq = mmax(twid_asq, eps_of<T>());
+  const T ct2 = bt_starsq / d;
+  const T tsum = vaxsq + ct2 + twid_asq;
+  const T tdif = vaxsq + ct2 - twid_asq;
+  const T cf2_cs2 = sqrt(tdif * tdif + T(4.) * twid_asq * ct2);
+  const T cfsq = T(0.5) * (tsum + cf2_cs2);
+  const T cfast = sqrt(cfsq);
+  vx = v[0];
+  l0 = v[0] - cfast;
+  l6 = v[0] + cfast;
+}
+
+// riemannS.cpp:58-116
+template <typename T>
+__device__ __forceinline__ int flux_rusa(const T *wL, const T *wR, T gamma, T *f) {
+  Side<T> L, R;
+  side_state<T>(wL, gamma, L);
+  side_state<T>(wR, gamma, R);
+  const T a = L.cf + fabs(wL[1]), b = R.cf + fabs(wR[1]);
+  const T im = smax(a, b);
+#pragma unroll
+  for (int k = 0; k < 8; k++) f[k] = T(0.5) * (L.F[k] + R.F[k]) - T(0.5) * im * (R.q[k] - L.q[k]);
+  return 0;
+}
+
+// riemannS.cpp:118-189
+template <typename T>
+__device__ __forceinline__ int flux_hlle(const T *wL, const T *wR, T gamma, T *f) {
+  Side<T> L, R;
+  side_state<T>(wL, gamma, L);
+  side_state<T>(wR, gamma, R);
+  T vx, l0, l6;
+  roe_outer<T>(wL, wR, L.H, R.H, gamma, vx, l0, l6);
+  T SL = smin(wL[1] - L.cf, l0);
+  SL = mmin(SL, T(0.));
+  T SR = smax(wR[1] + R.cf, l6);
+  SR = mmax(SR, T(0.));
+#pragma unroll
+  for (int k = 0; k < 8; k++) f[k] = (SR * L.F[k] - SL * R.F[k] + SL * SR * (R.q[k] - L.q[k])) / (SR - SL);
+  return 0;
+}
+
+// riemannS.cpp:192-295 (Linde 1998 with the heuristic alpha)
+template <typename T>
+__device__ __forceinline__ int flux_hllc(const T *wL, const T *wR, T gamma, T *f) {
+  Side<T> L, R;
+  side_state<T>(wL, gamma, L);
+  side_state<T>(wR, gamma, R);
+  T vx, l0, l6;
+  roe_outer<T>(wL, wR, L.H, R.H, gamma, vx, l0, l6);
+  const T SL = smin(wL[1] - L.cf, l0);
+  const T SR = smax(wR[1] + R.cf, l6);
+  const T SM = vx;
+  T s1 = T(0.), s2 = T(0.);
+#pragma unroll
+  for (int k = 0; k < 8; k++) s1 += fabs(R.q[k] - L.q[k]);
+#pragma unroll
+  for (int k = 0; k < 8; k++) s2 += fabs((R.F[k] - L.F[k]) - vx * (R.q[k] - L.q[k]));
+  const T interm = T(1.) - s2 / (s1 + eps_of<T>());
+  const T alpha = mmax(T(0.), interm);
+  if (alpha > T(1) || alpha < T(0) || isnan(alpha)) return DERR_HLLC;
+  if (SR - SL == T(0)) return DERR_HLLC;
+  int br = -1;
+  if (SL > T(0.)) br = 0;
+  else if (SL <= T(0.) && SM >= T(0.)) br = 1;
+  else if (SM <= T(0.) && SR >= T(0.)) br = 2;
+  else if (SR < T(0.)) br = 3;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    T v = T(0);
+    if (br == 0) v = L.F[k];
+    else if (br == 1)
+      v = ((SL * ((T(1) - alpha) * SR + alpha * vx)) / (SR - SL)) * (R.q[k] - L.q[k]) -
+          (SL / (SR - SL)) * R.F[k] + ((SR) / (SR - SL)) * L.F[k];
+    else if (br == 2)
+      v = ((SR * ((T(1) - alpha) * SL + alpha * vx)) / (SR - SL)) * (R.q[k] - L.q[k]) -
+          (SL / (SR - SL)) * R.F[k] + ((SR) / (SR - SL)) * L.F[k];
+    else if (br == 3) v = R.F[k];
+    f[k] = v;
+  }
+  return 0;
+}
+
+template <typename T>
+__device__ __forceinline__ T dot13_57(T a1, T a2, T a3, T a5, T a6, T a7) {  // misc.cpp:51-61
+  T s = T(0.);
+  s += a1 * a5;
+  s += a2 * a6;
+  s += a3 * a7;
+  return s;
+}
+
+// riemannS.cpp:397-549 (Miyoshi & Kusano).  Only the branch the wave fan
+// selects is assembled; its arithmetic is that of the reference.
+template <typename T>
+__device__ __forceinline__ int flux_hlld(const T *wL, const T *wR, T gamma, T *f) {
+  Side<T> L, R;
+  side_state<T>(wL, gamma, L);
+  side_state<T>(wR, gamma, R);
+  const T vnL = wL[1], vnR = wR[1], ptL = L.pt, ptR = R.pt;
+  const T SL = smin(vnL, vnR) - smax(L.cf, R.cf);
+  const T SR = smax(vnL, vnR) + smax(L.cf, R.cf);
+  const T SM = ((SR - vnR) * wR[0] * vnR - (SL - vnL) * wL[0] * vnL - ptR + ptL) /
+               ((SR - vnR) * wR[0] - (SL - vnL) * wL[0]);
+  const T pts = ((SR - vnR) * wR[0] * ptL - (SL - vnL) * wL[0] * ptR +
+                 wL[0] * wR[0] * (SR - vnR) * (SL - vnL) * (vnR - vnL)) /
+                ((SR - vnR) * wR[0] - (SL - vnL) * wL[0]);
+  // left * state (:467-481)
+  const T rLs = wL[0] * (SL - vnL) / (SL - SM);
+  T vLs, wzLs, byLs, bzLs;
+  if ((wL[0] * (SL - wL[1]) * (SL - SM) - wL[5] * wL[5]) != T(0)) {
+    const T den = wL[0] * (SL - wL[1]) * (SL - SM) - wL[5] * wL[5];
+    vLs = wL[2] - wL[5] * wL[6] * ((SM - wL[1]) / den);
+    wzLs = wL[3] - wL[5] * wL[7] * ((SM - wL[1]) / den);
+    byLs = wL[6] * ((wL[0] * ((SL - wL[1]) * (SL - wL[1])) - wL[5] * wL[5]) / den);
+    bzLs = wL[7] * ((wL[0] * ((SL - wL[1]) * (SL - wL[1])) - wL[5] * wL[5]) / den);
+  } else {
+    vLs = wL[2]; wzLs = wL[3]; byLs = T(0.); bzLs = T(0.);
+  }
+  const T eLs = (((SL - wL[1]) * L.e - ptL * wL[1] + pts * SM +
+                  wL[5] * (dot13_57(wL[1], wL[2], wL[3], wL[5], wL[6], wL[7]) -
+                           dot13_57(SM, vLs, wzLs, wL[5], byLs, bzLs))) /
+                 (SL - SM));
+  // right * state (:483-497)
+  const T rRs = wR[0] * (SR - vnR) / (SR - SM);
+  T vRs, wzRs, byRs, bzRs;
+  if ((wR[0] * (SR - wR[1]) * (SR - SM) - wR[5] * wR[5]) != T(0)) {
+    const T den = wR[0] * (SR - wR[1]) * (SR - SM) - wR[5] * wR[5];
+    vRs = wR[2] - wR[5] * wR[6] * ((SM - wR[1]) / den);
+    wzRs = wR[3] - wR[5] * wR[7] * ((SM - wR[1]) / den);
+    byRs = wR[6] * ((wR[0] * ((SR - wR[1]) * (SR - wR[1])) - wR[5] * wR[5]) / den);
+    bzRs = wR[7] * ((wR[0] * ((SR - wR[1]) * (SR - wR[1])) - wR[5] * wR[5]) / den);
+  } else {
+    vRs = wR[2]; wzRs = wR[3]; byRs = T(0); bzRs = T(0);
+  }
+  const T eRs = (((SR - wR[1]) * R.e - ptR * wR[1] + pts * SM +
+                  wR[5] * (dot13_57(wR[1], wR[2], wR[3], wR[5], wR[6], wR[7]) -
+                           dot13_57(SM, vRs, wzRs, wR[5], byRs, bzRs))) /
+                 (SR - SM));
+  const T sLs = sqrt(rLs), sRs = sqrt(rRs);
+  const T SLs = SM - fabs(wL[5]) / sLs;
+  const T SRs = SM + fabs(wR[5]) / sRs;
+  int br = -1;
+  if (SL > T(0)) br = 0;
+  else if (SL <= T(0.) && SLs >= T(0.)) br = 1;
+  else if (SLs <= T(0.) && SM >= T(0.)) br = 2;
+  else if (SM <= T(0.) && SRs >= T(0.)) br = 3;
+  else if (SRs <= T(0.) && SR >= T(0.)) br = 4;
+  else if (SR < T(0.)) br = 5;
+  // conserved * states (w2u, misc.cpp:82-92; energy replaced, :524,527)
+  const T qLs[8] = {rLs, rLs * SM, rLs * vLs, rLs * wzLs, eLs, wL[5], byLs, bzLs};
+  const T qRs[8] = {rRs, rRs * SM, rRs * vRs, rRs * wzRs, eRs, wR[5], byRs, bzRs};
+  T qss[8];
+  if (br == 2 || br == 3) {
+    // ** states (:501-519); the right ** state is a copy of the left one (:517)
+    const T sg = sgn(wL[5]);
+    const T vss = (sLs * vLs + sRs * vRs + (byRs - byLs) * sg) / (sLs + sRs);
+    const T wss = (sLs * wzLs + sRs * wzRs + (bzRs - bzLs) * sg) / (sLs + sRs);
+    const T byss = (sLs * byRs + sRs * byLs + sqrt(rLs * rRs) * (vRs - vLs) * sg) / (sLs + sRs);
+    const T bzss = (sLs * bzRs + sRs * bzLs + sqrt(rLs * rRs) * (wzRs - wzLs) * sg) / (sLs + sRs);
+    const T dss = dot13_57(SM, vss, wss, wL[5], byss, bzss);
+    T ess;
+    if (br == 2)
+      ess = eLs - sLs * (dot13_57(SM, vLs, wzLs, wL[5], byLs, bzLs) - dss) * sg;
+    else
+      ess = eRs + sRs * (dot13_57(SM, vRs, wzRs, wR[5], byRs, bzRs) - dss) * sgn(wR[5]);
+    qss[0] = rLs; qss[1] = rLs * SM; qss[2] = rLs * vss; qss[3] = rLs * wss;
+    qss[4] = ess; qss[5] = wL[5]; qss[6] = byss; qss[7] = bzss;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    T v = T(0);
+    switch (br) {
+      case 0: v = L.F[k]; break;
+      case 1: v = L.F[k] + SL * qLs[k] - SL * L.q[k]; break;
+      case 2: v = L.F[k] + SLs * qss[k] - (SLs - SL) * qLs[k] - SL * L.q[k]; break;
+      case 3: v = R.F[k] + SRs * qss[k] - (SRs - SR) * qRs[k] - SR * R.q[k]; break;
+      case 4: v = R.F[k] + SR * qRs[k] - SR * R.q[k]; break;
+      case 5: v = R.F[k]; break;
+      default: break;
+    }
+    f[k] = v;
+  }
+  return 0;
+}
+
+template <int FLUX, typename T>
+__device__ __forceinline__ int riemann(const T *wL, const T *wR, T gamma, T *f) {
+  if (FLUX == FLX_RUSA) return flux_rusa<T>(wL, wR, gamma, f);
+  if (FLUX == FLX_HLLE) return flux_hlle<T>(wL, wR, gamma, f);
+  if (FLUX == FLX_HLLC) return flux_hllc<T>(wL, wR, gamma, f);
+  return flux_hlld<T>(wL, wR, gamma, f);
+}
+
+}  // namespace amr

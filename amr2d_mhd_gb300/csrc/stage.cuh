@@ -1,0 +1,218 @@
+// Fused RK stage of one leaf block: MUSCL2D.cpp:13-121 (cons2prim,
+// reconstruction, CT normal-B override, Riemann fluxes) followed by the
+// residual and RK2ndv1 update of main.cpp:260-270 / 292-302.
+//
+// One CTA per leaf block.  Shared memory holds the primitive state of the
+// whole block (with ghosts) and the x / y face fluxes that the residual
+// needs; the fluxes also go to global memory (ff, gg), which the ghost fill
+// and the CT EMF read next.
+#pragma once
+
+#include "amr_common.h"
+#include "physics.cuh"
+
+namespace amr {
+
+template <int NG>
+struct Geo {
+  static constexpr int N = NI + 2 * NG;   // block edge with ghosts (nx of the reference)
+  static constexpr int NN = N * N;
+  static constexpr int LO = NG - 1;       // nxminb
+  static constexpr int HI = NG + NI - 1;  // nxmax
+  static constexpr int NF = NI + 1;       // faces per row computed by MUSCL2D (17)
+  static constexpr int NFX = NI + 2;      // plus the stale face at LO (18)
+};
+
+struct StageArgs {
+  const LeafTask *tasks;
+  const InstParams *inst;
+  const void *qin;    // U (stage 1) or Us (stage 2)
+  void *qout;         // Us (stage 1) or U (stage 2, read-modify-write)
+  const double *B;    // Bi (stage 1) or Bis (stage 2)
+  void *ff;
+  void *gg;
+  DevError *err;
+  int step;
+};
+
+__device__ __forceinline__ void dev_fail(DevError *e, int code, int blk, int i, int j, double v) {
+  if (atomicCAS(&e->code, 0, code) == 0) {
+    e->blk = blk;
+    e->i = i;
+    e->j = j;
+    e->value = v;
+  }
+}
+
+// meshblock.cpp:119-179 for one cell; the FP32 path recovers the pressure in
+// FP64 from the FP32 conserved state.
+template <typename S>
+__device__ __forceinline__ void cons2prim_cell(const S *u, S *w, double gamma);
+
+template <>
+__device__ __forceinline__ void cons2prim_cell<double>(const double *u, double *w, double g) {
+  w[0] = u[0];
+  w[1] = u[1] / u[0];
+  w[2] = u[2] / u[0];
+  w[3] = u[3] / u[0];
+  double p = (g - 1) * (u[4] - 0.5 * w[0] * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]));
+  w[5] = u[5];
+  w[6] = u[6];
+  w[7] = u[7];
+  w[4] = p - (g - 1) * (0.5 * (u[5] * u[5] + u[6] * u[6] + u[7] * u[7]));
+}
+
+template <>
+__device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, double g) {
+  const double r = u[0], mx = u[1], my = u[2], mz = u[3], E = u[4];
+  const double bx = u[5], by = u[6], bz = u[7];
+  const double vx = mx / r, vy = my / r, vz = mz / r;
+  const double p = (g - 1) * (E - 0.5 * r * (vx * vx + vy * vy + vz * vz)) -
+                   (g - 1) * (0.5 * (bx * bx + by * by + bz * bz));
+  w[0] = u[0];
+  w[1] = static_cast<float>(vx);
+  w[2] = static_cast<float>(vy);
+  w[3] = static_cast<float>(vz);
+  w[4] = static_cast<float>(p);
+  w[5] = u[5];
+  w[6] = u[6];
+  w[7] = u[7];
+}
+
+template <int NG, int RECON, int FLUX, typename S>
+__global__ void __launch_bounds__(256) k_stage(StageArgs a) {
+  using G = Geo<NG>;
+  using T = S;
+  constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI, NF = G::NF, NFX = G::NFX;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sW = reinterpret_cast<T *>(smem_raw);   // [8][NN]
+  T *sFx = sW + 8 * NN;                      // [8][NF][NFX]   face i = LO + col, row j = LO + r
+  T *sFy = sFx + 8 * NF * NFX;               // [8][NFX][NF]   face j = LO + row, col i = LO + c
+
+  const LeafTask task = a.tasks[blockIdx.x];
+  const InstParams ip = a.inst[task.inst];
+  const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
+  const S *Q = static_cast<const S *>(a.qin) + base;
+  S *ff = static_cast<S *>(a.ff) + base;
+  S *gg = static_cast<S *>(a.gg) + base;
+  const double *Bx = a.B + static_cast<size_t>(task.slot) * 2 * NN;
+  const double *By = Bx + NN;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+
+  // 1. primitive variables of every cell (U2W / Us2W), with the traps
+  for (int c = tid; c < NN; c += nthr) {
+    S u[8], w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = Q[k * NN + c];
+    cons2prim_cell<S>(u, w, ip.gamma);
+#pragma unroll
+    for (int k = 0; k < 8; k++) sW[k * NN + c] = w[k];
+    const int i = c % N, j = c / N;
+    if (w[4] <= T(0) && i > LO && i < HI + 1 && j > LO && j < HI + 1)
+      dev_fail(a.err, DERR_PRESSURE, task.slot, i, j, static_cast<double>(w[4]));
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 8; k++) bad |= isnan(w[k]);
+    if (bad) dev_fail(a.err, DERR_NAN, task.slot, i, j, 0.0);
+  }
+  // fluxes MUSCL2D does not recompute: the x face at LO and the y face at LO
+  // (their values come from the previous ghost fill of ff / gg)
+  for (int e = tid; e < 8 * NF; e += nthr) {
+    const int k = e / NF, r = e % NF;
+    sFx[(k * NF + r) * NFX + 0] = ff[k * NN + (LO + r) * N + LO];
+    sFy[(k * NFX + 0) * NF + r] = gg[k * NN + LO * N + (LO + r)];
+  }
+  __syncthreads();
+
+  // 2. Riemann fluxes at x faces (i+1/2, j), i in [LO, HI], and y faces
+  const T gamma = static_cast<T>(ip.gamma);
+  const int lim = ip.limiter;
+  for (int f = tid; f < 2 * NF * NF; f += nthr) {
+    const bool yf = f >= NF * NF;
+    const int g = yf ? f - NF * NF : f;
+    const int r = g / NF, c = g % NF;
+    // cell-index stride along the face normal and the left cell of the face
+    int s, cL;
+    if (!yf) { s = 1; cL = (LO + r) * N + (LO + c); }        // face between (LO+c) and (LO+c+1), row LO+r
+    else { s = N; cL = (LO + r) * N + (LO + c); }             // face between rows LO+r and LO+r+1, column LO+c
+    const int kn = yf ? 6 : 5;                                // normal B component
+    T wl[8], wr[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      if (k == kn) continue;
+      const T *w = sW + k * NN + cL;
+      if (RECON == REC_MUSCL) {
+        const T wm = w[-s], w0 = w[0], w1 = w[s], w2 = w[2 * s];
+        muscl_face<T>(lim, w0, w1, w0 - wm, w1 - w0, w2 - w1, static_cast<T>(yf ? task.dy : task.dx),
+                      wl[k], wr[k]);
+      } else if (RECON == REC_WENO3) {
+        T dummy;
+        weno3_cell<T>(w[-s], w[0], w[s], wl[k], dummy);
+        weno3_cell<T>(w[0], w[s], w[2 * s], dummy, wr[k]);
+      } else {
+        wl[k] = weno5_cell<T, false>(w[-2 * s], w[-s], w[0], w[s], w[2 * s]);
+        wr[k] = weno5_cell<T, true>(w[-s], w[0], w[s], w[2 * s], w[3 * s]);
+      }
+    }
+    // CT: the normal component is the face value (MUSCL2D.cpp:48-51)
+    const int fpos = cL + s;  // face index of the reference = the right cell
+    const T bn = static_cast<T>(yf ? By[fpos] : Bx[fpos]);
+    wl[kn] = bn;
+    wr[kn] = bn;
+    T fl[8];
+    int rc;
+    if (!yf) {
+      rc = riemann<FLUX, T>(wl, wr, gamma, fl);
+    } else {  // riemannS.cpp:12-23, 47-55: rotate y into x and back
+      T l2[8], r2[8], f2[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) { l2[k] = wl[k]; r2[k] = wr[k]; }
+      l2[1] = wl[2]; l2[2] = wl[1]; r2[1] = wr[2]; r2[2] = wr[1];
+      l2[5] = wl[6]; l2[6] = wl[5]; r2[5] = wr[6]; r2[6] = wr[5];
+      rc = riemann<FLUX, T>(l2, r2, gamma, f2);
+#pragma unroll
+      for (int k = 0; k < 8; k++) fl[k] = f2[k];
+      fl[1] = f2[2]; fl[2] = f2[1]; fl[5] = f2[6]; fl[6] = f2[5];
+    }
+    if (rc) dev_fail(a.err, rc, task.slot, fpos % N, fpos / N, 0.0);
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      bad |= isnan(fl[k]);
+      if (!yf) {
+        sFx[(k * NF + r) * NFX + (c + 1)] = fl[k];
+        ff[k * NN + fpos] = fl[k];
+      } else {
+        sFy[(k * NFX + (r + 1)) * NF + c] = fl[k];
+        gg[k * NN + fpos] = fl[k];
+      }
+    }
+    if (bad) dev_fail(a.err, DERR_NAN, task.slot, fpos % N, fpos / N, 0.0);
+  }
+  __syncthreads();
+
+  // 3. residual on [LO, HI]^2 (zero elsewhere) and the RK stage on every cell
+  const T dx = static_cast<T>(task.dx), dy = static_cast<T>(task.dy), dt = static_cast<T>(ip.dt);
+  S *out = static_cast<S *>(a.qout) + base;
+  for (int e = tid; e < 8 * NN; e += nthr) {
+    const int k = e / NN, c = e % NN;
+    const int i = c % N, j = c / N;
+    T res = T(0.);
+    if (i >= LO && i <= HI && j >= LO && j <= HI) {
+      const int cx = i - LO, r = j - LO;
+      res = (sFx[(k * NF + r) * NFX + cx + 1] - sFx[(k * NF + r) * NFX + cx]) / dx +
+            (sFy[(k * NFX + r + 1) * NF + cx] - sFy[(k * NFX + r) * NF + cx]) / dy;
+    }
+    const T q = Q[e];
+    if (a.step == 1) out[e] = q - dt * res;                         // Us = U - dt res
+    else out[e] = T(0.5) * (out[e] + q - dt * res);                 // U = (U + Us - dt res)/2
+  }
+}
+
+template <int NG, typename S>
+constexpr int stage_smem_bytes() {
+  using G = Geo<NG>;
+  return static_cast<int>(sizeof(S)) * (8 * G::NN + 2 * 8 * G::NF * G::NFX);
+}
+
+}  // namespace amr

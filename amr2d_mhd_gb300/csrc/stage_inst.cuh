@@ -1,0 +1,43 @@
+// Instantiates the stage kernel of one Riemann solver and one precision for
+// every supported (ghost layers, reconstruction) pair.  Each including .cu
+// file defines AMR_STAGE_PREC (f64 / f32), AMR_STAGE_T and AMR_STAGE_FLUX.
+#pragma once
+
+#include "launch.hpp"
+#include "stage.cuh"
+
+namespace amr {
+
+template <int NG, int RECON, int FLUX, typename S>
+cudaError_t launch_stage_t(const StageArgs &a, int ntasks, cudaStream_t s) {
+  constexpr int smem = stage_smem_bytes<NG, S>();
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_stage<NG, RECON, FLUX, S>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  if (ntasks <= 0) return cudaSuccess;
+  k_stage<NG, RECON, FLUX, S><<<ntasks, 256, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int FLUX, typename S>
+cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s) {
+  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_stage_t<2, REC_MUSCL, FLUX, S>(a, ntasks, s);
+  if (m.ng == 2 && m.recon == REC_WENO3) return launch_stage_t<2, REC_WENO3, FLUX, S>(a, ntasks, s);
+  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_stage_t<4, REC_MUSCL, FLUX, S>(a, ntasks, s);
+  if (m.ng == 4 && m.recon == REC_WENO3) return launch_stage_t<4, REC_WENO3, FLUX, S>(a, ntasks, s);
+  if (m.ng == 4 && m.recon == REC_WENO5) return launch_stage_t<4, REC_WENO5, FLUX, S>(a, ntasks, s);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace amr
+
+#define AMR_STAGE_DEFINE(P, F, FLUXID, T)                                                     \
+  namespace amr {                                                                          \
+  cudaError_t launch_stage_##P##_##F(const Method &m, const StageArgs &a, int n, cudaStream_t s) { \
+    return launch_stage_flux<FLUXID, T>(m, a, n, s);                                        \
+  }                                                                                        \
+  }

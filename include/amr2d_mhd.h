@@ -1,0 +1,152 @@
+/*
+ * amr2d_mhd.h — C ABI of the GB300 (sm_103a) per-block finite-volume update
+ * of a 2-D block-structured AMR ideal-MHD solver (drop-in for the hot path of
+ * spaceauk/AMR2D_MHD).
+ *
+ * The reference has no library API: its seam is the set of free functions
+ * main() calls on a `meshblock&` (main.cpp:241-360).  Each entry point below
+ * names the reference function it replaces.  Conventions:
+ *   - plain C types only; an opaque handle owns one or more AMR problems
+ *     ("instances"); all cell- and face-centred data stay resident on one GPU;
+ *   - every call returns an amr_status (0 = ok, < 0 = error); the reference
+ *     prints and throws on the same conditions, here the message is kept for
+ *     amr_last_error();
+ *   - one host thread per handle; work is issued on the handle's CUDA stream
+ *     (amr_set_stream) and calls that return host data synchronise it.
+ */
+#ifndef AMR2D_MHD_H
+#define AMR2D_MHD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMR_ABI_VERSION 1
+
+typedef enum amr_status {
+  AMR_OK = 0,
+  AMR_E_CONFIG = -1,      /* invalid option (the reference throws, e.g. slopelimiter.cpp:50) */
+  AMR_E_CUDA = -2,        /* CUDA runtime error or no device */
+  AMR_E_OOM = -3,         /* device allocation failed */
+  AMR_E_MAXBLOCKS = -4,   /* admesh.cpp:42-45 "nblocks exceeded max limit" */
+  AMR_E_PRESSURE = -5,    /* meshblock.cpp:136-142 / 164-170 zero or negative pressure */
+  AMR_E_NAN = -6,         /* celledges.cpp:17-21, MUSCL2D.cpp:79-85, meshblock.cpp:171-176 */
+  AMR_E_DT = -7,          /* main.cpp:348-351 invalid dt */
+  AMR_E_HLLC = -8,        /* riemannS.cpp:269-276 */
+  AMR_E_STATE = -9,       /* call out of order (e.g. amr_step before amr_init) */
+  AMR_E_TIMEOUT = -10,    /* a bounded device wait gave up */
+  AMR_E_UNSUPPORTED = -11,/* ROE with a magnetic field (riemannS.cpp:39-40), block size != 16 */
+  AMR_E_ARG = -12         /* bad pointer, size or index */
+} amr_status;
+
+typedef enum amr_precision {
+  AMR_FP64 = 0,           /* plain path: identical arithmetic to the reference */
+  AMR_FP32 = 1            /* FP32 bulk; FP64 pressure recovery, face B, dt and sums */
+} amr_precision;
+
+typedef enum amr_field {
+  AMR_FIELD_U = 0,        /* conserved state U [blocks][8][ny+2g][nx+2g] */
+  AMR_FIELD_US = 1,       /* RK stage state Us */
+  AMR_FIELD_BI = 2,       /* face magnetic field Bi [blocks][2][..][..] (Bx at i-1/2, By at j-1/2) */
+  AMR_FIELD_BIS = 3,      /* RK stage face field Bis */
+  AMR_FIELD_FF = 4,       /* x fluxes ff (face i-1/2) */
+  AMR_FIELD_GG = 5,       /* y fluxes gg (face j-1/2) */
+  AMR_FIELD_EMF = 6,      /* corner EMF [blocks][1][..][..] */
+  AMR_FIELD_W = 7         /* primitive state, computed from U on download */
+} amr_field;
+
+/* One AMR problem.  The first block of fields is input.txt (main.cpp:156-177);
+ * the second block holds the reference's compile-time constants (defs.hpp)
+ * and the extensions, each defaulting to the reference's value. */
+typedef struct amr_config {
+  int32_t struct_size;    /* sizeof(amr_config) */
+  int32_t nx, ny, nvar;   /* interior cells per block and variables: 16 16 8 */
+  double lenx, leny;      /* domain lengths: 1.0 1.0 */
+  double cfl;             /* CFL number */
+  char ic[16];            /* SST SST1 SSTy BWx BWx1 BWy BWy1 rotor | OT blast KH (extensions) */
+  char limiter[16];       /* 1st noSL WENO2D minmod VanLeer Superbee MC Koren Cada3rd WENO3 WENO5 */
+  char flux[16];          /* RUSA HLLE HLLC HLLD ROE */
+  int32_t maxlevs;        /* refinement levels (defs.hpp:28, default 5) */
+  int32_t nghosts;        /* ghost layers (defs.hpp:27, 2; 4 for WENO5) */
+  int32_t nroots_x;       /* root blocks along x (2: defs.hpp:29 nbroots = 4) */
+  int32_t nroots_y;
+  int32_t periodic;       /* extension: periodic box instead of mirror outflow */
+  int32_t geometry;       /* 0 = reference (dx0 = L/(sqrt(nroots)(nx-1)), shifted), 1 = L/cells */
+  double gamma;           /* <= 0: the IC's own value (IC2Dtype.cpp) */
+  double t_end;           /* <= 0: the IC's own value */
+  double ic_param[24];    /* extension ICs (blast: r0, p_in, |B|, theta, xc, yc; KH: a_1..a_16) */
+  int32_t precision;      /* amr_precision */
+  int32_t reserved[7];
+} amr_config;
+
+typedef struct amr_info {
+  double t;               /* simulated time (main.cpp:344) */
+  double dt;              /* dt used by the last step (dom.dt) */
+  double dt_next;         /* dt the next-but-one step will use (main.cpp:347) */
+  double t_end;
+  double gamma;
+  int64_t steps;          /* completed steps (main.cpp:346 count) */
+  int32_t last_active;    /* block IDs in use (dom.lastActive) */
+  int32_t n_leaves;       /* leaf blocks (count of dom.leafs) */
+  int32_t nb_leafs;       /* the reference's own counter dom.nbleafs (updatelpup.cpp:109) */
+  int32_t done;           /* 1 once t > t_end (main.cpp:241) */
+  int32_t n_instances;
+  int32_t nx_tot, ny_tot; /* block size with ghosts */
+  int64_t cell_updates;   /* sum over completed steps of leaf interior cells */
+} amr_info;
+
+typedef struct amr_handle amr_handle;
+
+/* ---- configuration ----------------------------------------------------- */
+/* Defaults = the reference's constants; then parse an input.txt
+ * (main.cpp:156-177: "nx ny nvar / lenx leny / CFL / IC limiter fluxMth"). */
+void amr_config_default(amr_config *cfg);
+int amr_config_from_input(const char *path, amr_config *cfg);
+int amr_abi_version(void);
+const char *amr_status_string(int status);
+
+/* ---- lifetime ------------------------------------------------------------ */
+/* replaces meshblock::setSize / setType (meshblock.cpp:6-116) */
+int amr_create(const amr_config *cfg, amr_handle **out);
+/* several independent problems swept together; each keeps its own tree,
+ * dt and end time */
+int amr_create_batch(const amr_config *cfgs, int32_t n, amr_handle **out);
+int amr_destroy(amr_handle *h);
+int amr_set_stream(amr_handle *h, void *cuda_stream);
+int amr_last_error(const amr_handle *h, char *buf, size_t len);
+
+/* ---- the time loop --------------------------------------------------------- */
+/* basegrid + IC2Dtype + W2U + initial admesh (main.cpp:210-229) */
+int amr_init(amr_handle *h);
+/* one iteration of main.cpp:241-360: ghost fills, two MUSCL2D + RK stages
+ * with CT2D, the CFL dt reduction and admesh.  Instances that are done are
+ * skipped. */
+int amr_step(amr_handle *h);
+/* step until every instance is done, or `max_steps` steps (< 0: no limit) */
+int amr_run(amr_handle *h, int64_t max_steps);
+int amr_get_info(amr_handle *h, int32_t instance, amr_info *info);
+
+/* ---- reference-function entry points (single instance) -------------------- */
+int amr_locate_bounds(amr_handle *h);                        /* locate_bounds.cpp:35 */
+int amr_boundary(amr_handle *h, int32_t field);              /* boundary/boundaryfc/boundaryec */
+int amr_muscl2d_rk(amr_handle *h, int32_t step);             /* MUSCL2D + main.cpp:257-272 / 289-308 */
+int amr_ct2d(amr_handle *h, int32_t step);                   /* CT2D.cpp:11 with its ghost fills */
+int amr_cfl_dt(amr_handle *h, double *lambda_min);           /* main.cpp:322-343 */
+int amr_admesh(amr_handle *h);                               /* admesh.cpp:17 */
+
+/* ---- state exchange with host buffers ----------------------------------- */
+/* Tree of one instance: lp[last_active][8], icoord[last_active][2], leafs[last_active] */
+int amr_get_tree(amr_handle *h, int32_t instance, int32_t *lp, int32_t *icoord, uint8_t *leafs,
+                 int32_t capacity);
+/* field of blocks [0, last_active) of one instance as float64, layout
+ * [block][var][j][i]; `count` = number of doubles the buffer holds */
+int amr_download(amr_handle *h, int32_t instance, int32_t field, double *dst, int64_t count);
+int amr_upload(amr_handle *h, int32_t instance, int32_t field, const double *src, int64_t count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AMR2D_MHD_H */

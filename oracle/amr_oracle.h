@@ -68,6 +68,13 @@ const char *oracle_error(const oracle *o);
 /* overwrite the state arrays of blocks [0, lastActive) (what = U or BI) */
 int oracle_set(oracle *o, int what, const double *src);
 
+/* test hooks: skip the remesh at the end of oracle_step; run admesh alone */
+void oracle_set_remesh(oracle *o, int on);
+int oracle_admesh(oracle *o);
+
+/* the sequential ghost fill of the current tree applied to `field` */
+int oracle_fill(oracle *o, double *field, int nv, int kind);
+
 /* unit-level entry points for known-answer tests */
 double oracle_slopelimiter(int limiter, double r, double eta);
 int oracle_riemann(int flux, const double *wL, const double *wR, double gamma, int dir_y,

@@ -76,6 +76,9 @@ def lib():
         L.oracle_set.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.oracle_error.restype = ctypes.c_char_p
         L.oracle_error.argtypes = [ctypes.c_void_p]
+        L.oracle_set_remesh.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.oracle_admesh.argtypes = [ctypes.c_void_p]
+        L.oracle_fill.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.oracle_slopelimiter.restype = ctypes.c_double
         L.oracle_slopelimiter.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.oracle_riemann.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
@@ -163,6 +166,18 @@ class Oracle:
         a = np.ascontiguousarray(arr, dtype=np.float64)
         self._check(lib().oracle_set(self.h, GET[what], a.ctypes.data))
 
+    def set_remesh(self, on):
+        lib().oracle_set_remesh(self.h, int(on))
+
+    def admesh(self):
+        self._check(lib().oracle_admesh(self.h))
+
+    def fill(self, field, kind):
+        """Sequential ghost fill (kind 0 cell, 1 face, 2 edge) of a copy of `field`."""
+        a = np.array(field, dtype=np.float64, order="C", copy=True)
+        lib().oracle_fill(self.h, a.ctypes.data, a.shape[1], kind)
+        return a
+
     def state(self):
         """Dict in the same form as read_ref_dump()."""
         inf = self.info()
@@ -206,6 +221,24 @@ def read_ref_dump(path):
     return dict(t=t, dt=dt, step=step, lastActive=na, nbleafs=nbleafs, maxlevs=maxlevs,
                 gamma=gamma, dx0=dx0, lp=meta[:, :8].copy(), icoord=meta[:, 8:10].copy(),
                 leafs=meta[:, 10].astype(bool), U=U.copy(), W=W.copy(), Bi=Bi.copy())
+
+
+def criteria_grad(W, ng=2):
+    """criteria.cpp:11-29 per block: max over interior cells of the relative
+    jumps of p, rho, Bx, By (W: [blocks][8][n][n])."""
+    n = W.shape[-1]
+    out = np.zeros(W.shape[0])
+    c = slice(ng, n - ng)
+    for k in (4, 0, 5, 6):
+        w = W[:, k]
+        w0 = w[:, c, c]
+        d = np.abs(w[:, c, ng + 1:n - ng + 1] - w0)
+        d = np.maximum(d, np.abs(w[:, c, ng - 1:n - ng - 1] - w0))
+        d = np.maximum(d, np.abs(w[:, ng + 1:n - ng + 1, c] - w0))
+        d = np.maximum(d, np.abs(w[:, ng - 1:n - ng - 1, c] - w0))
+        r = d / np.maximum(1e-15, np.abs(w0))
+        out = np.maximum(out, r.reshape(W.shape[0], -1).max(axis=1))
+    return out
 
 
 def compare_states(a, b, ng=2):

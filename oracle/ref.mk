@@ -43,6 +43,15 @@ INC  := -I- -I$(OUT) -I$(REF)
 
 all: $(OUT)/main.x
 
+# known-answer harness on the reference's own riemannS / misc / slopelimiter
+kat: $(OUT)/kat.x
+
+$(OUT)/ref_kat.o: $(HERE)ref_kat.cpp $(OUT)/defs.hpp
+	$(CXX) -c $(CFLAGS) $(INC) $< -o $@
+
+$(OUT)/kat.x: $(OUT)/ref_kat.o $(OUT)/riemannS.o $(OUT)/misc.o $(OUT)/slopelimiter.o
+	$(CXX) $(LFLAGS) $^ -o $@
+
 $(OUT)/defs.hpp: $(REF)/defs.hpp
 	@mkdir -p $(OUT)
 	sed -e 's/^const int maxlevs=5;/const int maxlevs=$(MAXLEVS);/' \
@@ -62,4 +71,4 @@ $(OUT)/ref_hook.o: $(HERE)ref_hook.cpp $(OUT)/defs.hpp
 $(OUT)/main.x: $(OBJS)
 	$(CXX) $(LFLAGS) $(OBJS) -o $@
 
-.PHONY: all
+.PHONY: all kat

@@ -1,0 +1,65 @@
+"""CPU shim over the product's host code (ghost-fill compiler and quadtree):
+tests/ghost_shim.cpp compiled together with amr2d_mhd_gb300/csrc/{ghost_compile,tree}.cpp."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(REPO, "amr2d_mhd_gb300", "csrc")
+OUT = os.path.join(HERE, "_build", "ghost_shim.so")
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        srcs = [os.path.join(HERE, "ghost_shim.cpp"), os.path.join(CSRC, "ghost_compile.cpp"),
+                os.path.join(CSRC, "tree.cpp")]
+        deps = srcs + [os.path.join(CSRC, f) for f in ("ghost_compile.hpp", "tree.hpp", "amr_common.h")]
+        if not os.path.exists(OUT) or os.path.getmtime(OUT) < max(os.path.getmtime(d) for d in deps):
+            os.makedirs(os.path.dirname(OUT), exist_ok=True)
+            tmp = OUT + ".%d" % os.getpid()
+            subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+                                   "-I" + CSRC] + srcs + ["-o", tmp])
+            os.replace(tmp, OUT)
+        L = ctypes.CDLL(OUT)
+        L.ghost_shim_apply.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 7 + \
+            [ctypes.c_void_p] * 3
+        L.tree_shim_admesh.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int,
+                                                                                 ctypes.c_void_p, ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def ghost_apply(st, kind, nv, field, maxlevs, ng=2, nroots=(2, 2), periodic=False):
+    a = np.array(field, dtype=np.float64, copy=True)
+    lp = np.ascontiguousarray(st["lp"], np.int32)
+    ic = np.ascontiguousarray(st["icoord"], np.int32)
+    lf = np.ascontiguousarray(st["leafs"].astype(np.uint8))
+    no, ns = ctypes.c_int(), ctypes.c_int()
+    rc = lib().ghost_shim_apply(st["lastActive"], lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, maxlevs,
+                                nroots[0], nroots[1], int(periodic), ng, kind, nv, a.ctypes.data,
+                                ctypes.byref(no), ctypes.byref(ns))
+    assert rc == 0
+    return a, no.value, ns.value
+
+
+def admesh(st, grad, maxlevs, ng=2, nroots=(2, 2), periodic=False, cap=100000):
+    na = ctypes.c_int(st["lastActive"])
+    nbl = ctypes.c_int(st["nbleafs"])
+    lp = np.zeros((cap, 8), np.int32)
+    ic = np.zeros((cap, 2), np.int32)
+    lf = np.zeros(cap, np.uint8)
+    n0 = st["lastActive"]
+    lp[:n0], ic[:n0], lf[:n0] = st["lp"], st["icoord"], st["leafs"]
+    g = np.ascontiguousarray(grad, np.float64)
+    nr, nc = ctypes.c_int(), ctypes.c_int()
+    rc = lib().tree_shim_admesh(ctypes.byref(na), lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, ctypes.byref(nbl),
+                                maxlevs, nroots[0], nroots[1], int(periodic), ng, g.ctypes.data, cap,
+                                ctypes.byref(nr), ctypes.byref(nc))
+    assert rc == 0, rc
+    n = na.value
+    return dict(lastActive=n, nbleafs=nbl.value, lp=lp[:n], icoord=ic[:n], leafs=lf[:n].astype(bool)), nr.value, nc.value

@@ -1,0 +1,44 @@
+"""FP64 CUDA path vs the oracle, step by step, through the C ABI.
+
+The plain FP64 path evaluates the reference's arithmetic operation by
+operation (no FMA contraction), so the bar is bit-identical state and an
+identical block tree; the benchmark spec's tolerance (relative L1 <= 1e-10 per
+conserved variable) is asserted as well, as the weaker fallback statement.
+"""
+import numpy as np
+import pytest
+
+from parity_util import run_pair
+
+L1_TOL = 1e-10
+
+CASES = [
+    dict(ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=4, steps=40),
+    dict(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=5, steps=60),
+    dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, steps=40),
+    dict(ic="BWx", limiter="MC", flux="HLLE", cfl=0.4, maxlevs=4, steps=30),
+    dict(ic="BWx", limiter="MC", flux="HLLC", cfl=0.4, maxlevs=4, steps=30),
+    dict(ic="BWy", limiter="minmod", flux="HLLD", cfl=0.4, maxlevs=3, steps=30),
+    dict(ic="BWx1", limiter="VanLeer", flux="RUSA", cfl=0.4, maxlevs=3, steps=20),
+    dict(ic="SST", limiter="Superbee", flux="HLLE", cfl=0.4, maxlevs=3, steps=20),
+    dict(ic="SSTy", limiter="Koren", flux="RUSA", cfl=0.4, maxlevs=3, steps=20),
+    dict(ic="BWy1", limiter="Cada3rd", flux="RUSA", cfl=0.4, maxlevs=3, steps=20),
+    dict(ic="SST1", limiter="1st", flux="RUSA", cfl=0.4, maxlevs=3, steps=20),
+    dict(ic="BWx", limiter="WENO3", flux="RUSA", cfl=0.4, maxlevs=3, steps=20),
+    dict(ic="BWx", limiter="WENO5", flux="HLLD", cfl=0.4, maxlevs=3, nghosts=4, steps=20),
+    dict(ic="rotor", limiter="WENO5", flux="RUSA", cfl=0.4, maxlevs=3, nghosts=4, steps=20),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "%s-%s-%s-L%d" % (c["ic"], c["limiter"], c["flux"], c["maxlevs"]))
+def test_fp64_matches_oracle(gpu, case):
+    case = dict(case)
+    steps = case.pop("steps")
+    recs, _, _ = run_pair(gpu, steps, check_every=5, **case)
+    last = recs[-1]
+    assert all(r["same_tree"] for r in recs), recs[-1]
+    assert all(r["t_equal"] for r in recs)
+    assert max(np.max(r["rel"]) for r in recs) <= L1_TOL
+    assert all(r["bitwise"] for r in recs), [(r["step"], r["dU"], r["dB"]) for r in recs if not r["bitwise"]][:3]
+    assert last["step"] == steps
