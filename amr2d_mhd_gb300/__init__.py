@@ -29,7 +29,7 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_abi_version", "am
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
-           "amr_upload"]
+           "amr_upload", "amr_profile_enable", "amr_profile_read"]
 
 
 class AmrError(RuntimeError):
@@ -55,6 +55,13 @@ class Info(ctypes.Structure):
                 ("last_active", ctypes.c_int32), ("n_leaves", ctypes.c_int32), ("nb_leafs", ctypes.c_int32),
                 ("done", ctypes.c_int32), ("n_instances", ctypes.c_int32), ("nx_tot", ctypes.c_int32),
                 ("ny_tot", ctypes.c_int32), ("cell_updates", ctypes.c_int64)]
+
+
+class Profile(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_int64), ("stage_launches", ctypes.c_int64), ("stage_ms", ctypes.c_double),
+                ("stage_cells", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
+                ("host_compile_ms", ctypes.c_double), ("host_admesh_ms", ctypes.c_double),
+                ("wait_ms", ctypes.c_double), ("steps", ctypes.c_int64)]
 
 
 _lib = None
@@ -95,6 +102,8 @@ def load(build_if_missing: bool = True):
         "amr_get_tree": (ctypes.c_int, [vp, i32, dp, dp, dp, i32]),
         "amr_download": (ctypes.c_int, [vp, i32, i32, dp, i64]),
         "amr_upload": (ctypes.c_int, [vp, i32, i32, dp, i64]),
+        "amr_profile_enable": (ctypes.c_int, [vp, i32]),
+        "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -219,6 +228,20 @@ class Simulation:
     def upload(self, field, arr, instance=0):
         a = np.ascontiguousarray(arr, np.float64)
         self._ck(load().amr_upload(self.h, instance, FIELDS[field], a.ctypes.data, a.size))
+
+    def set_stream(self, stream_ptr):
+        """Issue this handle's work on an existing CUDA stream (e.g. torch's)."""
+        self._ck(load().amr_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def profile(self, enable=None):
+        """profile(True/False) resets the counters (and turns the stage-kernel
+        events on/off); profile() returns the counters."""
+        if enable is not None:
+            self._ck(load().amr_profile_enable(self.h, int(enable)))
+            return None
+        p = Profile()
+        self._ck(load().amr_profile_read(self.h, ctypes.byref(p)))
+        return {k: getattr(p, k) for k, _ in Profile._fields_}
 
     def state(self, instance=0):
         """Dict in the form the oracle's state() returns."""

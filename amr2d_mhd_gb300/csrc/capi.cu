@@ -151,4 +151,11 @@ int amr_upload(amr_handle *h, int32_t q, int32_t f, const double *s, int64_t n) 
   return guarded(h, [&](amr::Engine &e) { return e.upload(q, f, s, n); });
 }
 
+int amr_profile_enable(amr_handle *h, int32_t on) {
+  return guarded(h, [&](amr::Engine &e) { return e.profile_enable(on != 0); });
+}
+int amr_profile_read(amr_handle *h, amr_profile *o) {
+  return guarded(h, [&](amr::Engine &e) { return e.profile_read(o); });
+}
+
 }  // extern "C"

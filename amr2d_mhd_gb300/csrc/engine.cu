@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 #include <initializer_list>
+#include <chrono>
 #include <string>
 
 #include "aux_kernels.cuh"
@@ -249,6 +250,7 @@ int Engine::rebuild() {
   for (int a : active_)
     if (built_version_[a] != inst_[a].tree.version) need = true;
   if (!need) return AMR_OK;
+  const auto t0 = std::chrono::steady_clock::now();
   tasks_.clear();
   task_blk_.clear();
   for (auto &p : prog_) p.clear();
@@ -298,6 +300,11 @@ int Engine::rebuild() {
   // the host vectors above must outlive the async copies
   CK(cudaStreamSynchronize(stream_), "sync");
   programs_valid_ = true;
+  size_t bytes = sizeof(LeafTask) * nt;
+  for (int p = 0; p < 4; p++) bytes += sizeof(GhostOp) * prog_[p].ops.size() + sizeof(GhostSnap) * prog_[p].snaps.size();
+  prof_.h2d_bytes += static_cast<int64_t>(bytes);
+  prof_.launches += 0;
+  prof_.host_compile_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return AMR_OK;
 }
 
@@ -310,6 +317,7 @@ int Engine::upload_params() {
     p[q].pad = 0;
   }
   CK(cudaMemcpyAsync(d_params_.p, p, sizeof(InstParams) * inst_.size(), cudaMemcpyHostToDevice, stream_), "h2d");
+  prof_.h2d_bytes += sizeof(InstParams) * inst_.size();
   return AMR_OK;
 }
 
@@ -335,6 +343,7 @@ int Engine::fill(std::initializer_list<std::pair<FillKind, int>> what) {
   g.nseg = q;
   g.snapbuf = d_snap_.as<double>();
   CK(launch_ghost(ng_, g, nsnap, nops, stream_), "ghost fill");
+  prof_.launches += (nsnap > 0) + (nops > 0);
   return AMR_OK;
 }
 
@@ -349,7 +358,22 @@ int Engine::stage(int step) {
   a.gg = gg_;
   a.err = d_err_.as<DevError>();
   a.step = step;
+  if (prof_on_) {
+    while (ev_.size() < static_cast<size_t>(ev_used_ + 2)) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e), "event");
+      ev_.push_back(e);
+    }
+    CK(cudaEventRecord(ev_[ev_used_], stream_), "event");
+  }
   CK(launch_stage(m_, a, static_cast<int>(tasks_.size()), stream_), "stage kernel");
+  if (prof_on_) {
+    CK(cudaEventRecord(ev_[ev_used_ + 1], stream_), "event");
+    ev_used_ += 2;
+  }
+  prof_.launches += 1;
+  prof_.stage_launches += 1;
+  stage_cells_pending_ += static_cast<int64_t>(tasks_.size()) * NI * NI;
   return AMR_OK;
 }
 
@@ -372,6 +396,7 @@ int Engine::ct2d(int step) {
   CK(launch_ct_face(m_, a, n, stream_), "ct face");
   if (int rc = fill({{FILL_FC, step == 1 ? AMR_FIELD_BIS : AMR_FIELD_BI}})) return rc;
   CK(launch_ct_cell(m_, a, n, stream_), "ct cell");
+  prof_.launches += 3;
   return AMR_OK;
 }
 
@@ -385,6 +410,7 @@ int Engine::dt_crit(bool want_grad) {
   a.err = d_err_.as<DevError>();
   a.want_grad = want_grad ? 1 : 0;
   CK(launch_dt_crit(m_, a, static_cast<int>(tasks_.size()), stream_), "dt kernel");
+  prof_.launches += 1;
   return AMR_OK;
 }
 
@@ -405,7 +431,11 @@ int Engine::enqueue_stage_sequence() {
 
 int Engine::check_device_error() {
   CK(cudaMemcpyAsync(h_err_.p, d_err_.p, sizeof(DevError), cudaMemcpyDeviceToHost, stream_), "d2h");
+  prof_.d2h_bytes += sizeof(DevError);
+  const auto w0 = std::chrono::steady_clock::now();
   CK(cudaStreamSynchronize(stream_), "sync");
+  prof_.wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+  prof_collect();
   const DevError &e = *h_err_.as<DevError>();
   if (e.code != 0) {
     char msg[256];
@@ -413,6 +443,32 @@ int Engine::check_device_error() {
                   e.blk, e.i, e.j, e.value);
     return fail(map_dev_error(e.code), msg);
   }
+  return AMR_OK;
+}
+
+// ------------------------------------------------------------- profiling
+void Engine::prof_collect() {
+  for (int q = 0; q + 1 < ev_used_; q += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev_[q], ev_[q + 1]) == cudaSuccess) prof_.stage_ms += ms;
+  }
+  ev_used_ = 0;
+  prof_.stage_cells += stage_cells_pending_;
+  stage_cells_pending_ = 0;
+}
+
+int Engine::profile_enable(bool on) {
+  if (stream_) CK(cudaStreamSynchronize(stream_), "sync");
+  prof_ = amr_profile{};
+  ev_used_ = 0;
+  stage_cells_pending_ = 0;
+  prof_on_ = on;
+  return AMR_OK;
+}
+
+int Engine::profile_read(amr_profile *out) {
+  if (!out) return fail(AMR_E_ARG, "null pointer");
+  *out = prof_;
   return AMR_OK;
 }
 

@@ -74,6 +74,9 @@ class Engine {
   int download(int inst, int field, double *dst, int64_t count);
   int upload(int inst, int field, const double *src, int64_t count);
 
+  int profile_enable(bool on);
+  int profile_read(amr_profile *out);
+
   std::string last_error;
 
  private:
@@ -122,6 +125,14 @@ class Engine {
   DevBuf d_treeops_, d_stage_, d_slots_;
   HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_stage_;
   GhostCompiler *gc_ = nullptr;
+
+  // measurement
+  bool prof_on_ = false;
+  amr_profile prof_{};
+  std::vector<cudaEvent_t> ev_;     // start/stop pairs of this step's stage launches
+  int ev_used_ = 0;
+  int64_t stage_cells_pending_ = 0;
+  void prof_collect();
 };
 
 }  // namespace amr

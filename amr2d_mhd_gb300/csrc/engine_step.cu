@@ -1,5 +1,6 @@
 // Engine: initialisation, the time step, remeshing and the reference-function
 // entry points.
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -33,10 +34,15 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
     CK(cudaMemcpyAsync(d_stage_.p, h_stage_.p, bytes, cudaMemcpyHostToDevice, stream_), "h2d");
     CK(launch_scatter(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
        "scatter");
+    prof_.h2d_bytes += static_cast<int64_t>(bytes + sizeof(int) * nblk);
+    prof_.launches += 1;
     CK(cudaStreamSynchronize(stream_), "sync");
   } else {
     CK(launch_gather(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
        "gather");
+    prof_.h2d_bytes += static_cast<int64_t>(sizeof(int) * nblk);
+    prof_.d2h_bytes += static_cast<int64_t>(bytes);
+    prof_.launches += 1;
     CK(cudaMemcpyAsync(h_stage_.p, d_stage_.p, bytes, cudaMemcpyDeviceToHost, stream_), "d2h");
     CK(cudaStreamSynchronize(stream_), "sync");
     std::memcpy(host, h_stage_.p, bytes);
@@ -48,6 +54,7 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
 // device reduction of the last dt_crit (or, at initialisation, from the IC's
 // primitive state on the host)
 int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad) {
+  const auto t0 = std::chrono::steady_clock::now();
   std::vector<TreeOp> ref, crs;
   for (int q : which) {
     Instance &in = inst_[q];
@@ -68,6 +75,7 @@ int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vec
     for (const auto &c : plan.coarsen)
       crs.push_back(TreeOp{in.slot[c[0]], {in.slot[c[1]], in.slot[c[2]], in.slot[c[3]], in.slot[c[4]]}, q});
   }
+  prof_.host_admesh_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (ref.empty() && crs.empty()) return AMR_OK;
   if (int rc = upload_params()) return rc;
   std::vector<TreeOp> all(ref);
@@ -84,6 +92,8 @@ int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vec
   CK(launch_refine(m_, a, static_cast<int>(ref.size()), stream_), "refine");
   a.ops = d_treeops_.as<TreeOp>() + ref.size();
   CK(launch_coarsen(m_, a, static_cast<int>(crs.size()), stream_), "coarsen");
+  prof_.launches += (ref.empty() ? 0 : 1) + (crs.empty() ? 0 : 1);
+  prof_.h2d_bytes += static_cast<int64_t>(sizeof(TreeOp) * all.size());
   return check_device_error();  // also keeps `all` alive until the copy is done
 }
 
@@ -125,6 +135,8 @@ int Engine::finish_step() {
   const size_t nt = tasks_.size();
   CK(cudaMemcpyAsync(h_lambda_.p, d_lambda_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
   CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
+  prof_.d2h_bytes += static_cast<int64_t>(2 * sizeof(double) * nt);
+  prof_.steps += 1;
   if (int rc = check_device_error()) return rc;
   const double *hl = h_lambda_.as<double>();
   for (int a : active_) {

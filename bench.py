@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Throughput of the per-block finite-volume update on the MHD rotor.
+
+Workload: the MHD rotor on [0,1]^2, gamma = 5/3, 4 root blocks of 16x16 cells,
+5 refinement levels, MUSCL with the MC limiter, HLLD fluxes, constrained
+transport, RK2, CFL 0.4, outflow boundaries.  The run is advanced (untimed) to
+t = T0, where the AMR tree is developed; a bench step is then one full time
+step (both RK stages with CT, all ghost fills, the CFL reduction and the
+remesh).  `value` is leaf cell-updates per second of the plain FP64 path, with
+the state resident in HBM; `e2e` is the same through the C ABI with the state
+in host memory (uploaded before and downloaded after every step).  The FP32
+bulk path, its density error against FP64 at t_end, and the CPU baseline
+(the oracle's restatement of the reference, on the host cores) are reported
+beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+T0 = 0.05                 # start of the timed region (simulated time)
+WORKLOAD = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, nghosts=2, nroots=(2, 2),
+                periodic=False, geometry=1, gamma=5.0 / 3.0, t_end=0.0)
+WORKLOAD_NAME = ("MHD rotor [0,1]^2 gamma=5/3, 4 roots of 16x16, 5 levels, MUSCL-MC + HLLD + CT, RK2, "
+                 "CFL 0.4, outflow, time steps from t=%.2f" % T0)
+METRIC = "cell-updates/s"
+# compulsory DRAM bytes of one fused RK-stage launch per interior leaf cell
+# (FP64): stage 1 reads U (8 words) and the face field (2) and writes Us (8);
+# stage 2 reads Us (8), U (8), face field (2) and writes U (8); mean of the two
+STAGE_BYTES_PER_CELL = {"fp64": (18 + 26) / 2 * 8, "fp32": (18 + 26) / 2 * 4 + 2 * 4}
+STEP_BYTES_PER_CELL = {"fp64": 400, "fp32": 240}   # one full RK2 step incl. CT (compulsory)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows)}
+        try:
+            sm = [float(r[1]) for r in self.rows if len(r) >= 9]
+            mx = [float(r[2]) for r in self.rows if len(r) >= 9]
+            if sm:
+                out["sm_mhz"] = statistics.median(sm)
+                out["sm_max_mhz"] = max(mx)
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for q, nm in enumerate(names):
+                if any(r[5 + q].lower() == "active" for r in self.rows if len(r) >= 9):
+                    out["reasons"].append(nm)
+        except (ValueError, IndexError):
+            pass
+        return out
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_summary(name):
+    """Per-cell DRAM bytes / FP64 flops of the stage kernel from the committed ncu summary."""
+    p = os.path.join(REPO, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 rate of this GPU: a cuBLAS DGEMM, best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.mm(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def advance_to(sim, t_stop, chunk=50):
+    while True:
+        inf = sim.info()
+        if inf["done"] or inf["t"] >= t_stop:
+            return inf
+        sim.run(chunk)
+
+
+def uniform_density(sim, level):
+    """Leaf densities painted onto the uniform grid of `level` (piecewise constant)."""
+    lp, ic, lf = sim.tree()
+    U = sim.download("U")
+    ng = 2
+    n = 16 * 2 * 2 ** level
+    out = np.zeros((n, n))
+    for b in np.nonzero(lf)[0]:
+        lev = lp[b, 0]
+        r = 2 ** (level - lev)
+        rho = U[b, 0, ng:-ng, ng:-ng].T   # [i][j]
+        x0, y0 = ic[b, 0] * r, ic[b, 1] * r
+        out[x0:x0 + 16 * r, y0:y0 + 16 * r] = np.kron(rho, np.ones((r, r)))
+    return out
+
+
+def run_ours(args):
+    import torch
+
+    import amr2d_mhd_gb300 as amr
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    K, W = args.steps, args.warmup
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def make(precision):
+        sim = amr.Simulation(precision=precision, **WORKLOAD)
+        sim.set_stream(stream.cuda_stream)
+        return sim.init()
+
+    results = {}
+    for prec in ("fp64", "fp32"):
+        sim = make(prec)
+        advance_to(sim, T0)
+        sim.run(W)
+        clocks = ClockSampler(local) if prec == "fp64" else None
+        if clocks:
+            clocks.start()
+        sim.profile(True)
+        i0 = sim.info()
+        barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        sim.run(K)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = ev0.elapsed_time(ev1)
+        i1 = sim.info()
+        prof = sim.profile()
+        clk = clocks.stop() if clocks else None
+        cells = i1["cell_updates"] - i0["cell_updates"]
+        if world > 1:
+            t = torch.tensor([ms, float(cells)], dtype=torch.float64, device="cuda")
+            mx = t.clone()
+            torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+            ms, cells = float(mx[0]), float(t[1])
+        results[prec] = dict(ms=ms, cells=cells, prof=prof, clocks=clk, leaves=i1["n_leaves"],
+                             steps=i1["steps"] - i0["steps"])
+        if prec == "fp64":
+            # e2e through the C ABI with the state in host memory
+            U = sim.download("U")
+            B = sim.download("Bi")
+            sim.profile(False)
+            j0 = sim.info()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(K):
+                sim.upload("U", U)
+                sim.upload("Bi", B)
+                sim.step()
+                U = sim.download("U")
+                B = sim.download("Bi")
+            torch.cuda.synchronize()
+            e2e_s = time.perf_counter() - t0
+            j1 = sim.info()
+            p2 = sim.profile()
+            results["e2e"] = dict(s=e2e_s, cells=j1["cell_updates"] - j0["cell_updates"],
+                                  h2d=p2["h2d_bytes"] / K, d2h=p2["d2h_bytes"] / K)
+        # accuracy at t_end (untimed): FP32 against FP64
+        advance_to(sim, 1e9, chunk=500)
+        inf = sim.info()
+        results[prec]["t_end"] = inf["t"]
+        results[prec]["rho"] = uniform_density(sim, WORKLOAD["maxlevs"] - 1) if rank == 0 else None
+        sim.close()
+    return results, world, rank
+
+
+def cpu_baseline(steps, threads):
+    """The oracle (the CPU restatement of the reference) on the host cores:
+    the same rotor advanced to T0 (untimed), then `steps` timed steps."""
+    from oracle import pyoracle as P
+    o = P.Oracle(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, geom_ref=False, gamma=5.0 / 3.0,
+                 nthreads=threads).init()
+    while o.info()["t"] < T0:
+        o.step()
+    cells = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        nl = int(o.get("leafs").sum())
+        o.step()
+        cells += nl * 256
+    dt = time.perf_counter() - t0
+    return cells / dt, dict(steps=steps, t0=T0, leaves=int(o.get("leafs").sum()), seconds=dt)
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from oracle import pyoracle as P
+    o = P.Oracle(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, geom_ref=False, gamma=5.0 / 3.0,
+                 nthreads=threads).init()
+    while o.info()["t"] < T0:
+        o.step()
+    for _ in range(args.warmup):
+        o.step()
+    cells = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        nl = int(o.get("leafs").sum())
+        o.step()
+        cells += nl * 256
+    sec = time.perf_counter() - t0
+    v = cells / sec
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (rotor initial condition)",
+            "config": {"workload": WORKLOAD_NAME, "l2": "inputs larger than L2 are not needed: CPU run"},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                             "sample": "%d rotor time steps from t=%.2f on %d threads (oracle/amr_oracle.c, "
+                                       "the C restatement of the reference)" % (args.steps, T0, threads)},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=40, help="steps of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    res, world, rank = run_ours(args)
+    if rank != 0:
+        return 0
+    r64, r32, e2e = res["fp64"], res["fp32"], res["e2e"]
+    value = r64["cells"] / (r64["ms"] * 1e-3)
+    value32 = r32["cells"] / (r32["ms"] * 1e-3)
+    # density error FP32 vs FP64 at t_end on the finest uniform grid
+    a, b = r32["rho"], r64["rho"]
+    l1 = float(np.abs(a - b).sum() / np.abs(b).sum())
+    # roofline of the dominant kernel (fused RK stage, FP64)
+    prof = r64["prof"]
+    stage_ms_avg = prof["stage_ms"] / max(prof["stage_launches"], 1)
+    cells_per_launch = prof["stage_cells"] / max(prof["stage_launches"], 1)
+    alg_bytes = cells_per_launch * STAGE_BYTES_PER_CELL["fp64"]
+    achieved = alg_bytes / (stage_ms_avg * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    ps = profile_summary("stage_fp64_rotor_hlld.json")
+    traffic = ps["dram_bytes_per_cell"] * cells_per_launch if ps else None
+    fp64 = {}
+    try:
+        fp64["peak_tflops_dgemm"] = fp64_peak_tflops(torch)
+        if ps and "dp_flops_per_cell" in ps:
+            fp64["achieved_tflops"] = ps["dp_flops_per_cell"] * cells_per_launch / (stage_ms_avg * 1e-3) / 1e12
+            fp64["frac"] = fp64["achieved_tflops"] / fp64["peak_tflops_dgemm"]
+    except Exception as ex:  # noqa: BLE001
+        fp64["error"] = str(ex)
+    cpu = None
+    if not args.no_cpu and world == 1:
+        threads = os.cpu_count() or 1
+        v, info = cpu_baseline(args.cpu_steps, threads)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+               "sample": "%d rotor time steps from t=%.2f (%d leaves), oracle/amr_oracle.c on %d threads"
+                         % (info["steps"], T0, info["leaves"], threads)}
+    clk = r64["clocks"] or {}
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r64["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (rotor initial condition)",
+        "config": {"workload": WORKLOAD_NAME, "leaves": r64["leaves"], "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "no flush: every step reads and writes the whole state (~%d MB FP64, below the 129 MB L2)"
+                         % int(r64["leaves"] * 1.25 * 8 * 400 * 8 / 1e6)},
+        "e2e": {"value": e2e["cells"] / e2e["s"], "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(e2e["h2d"]), "d2h_bytes_per_step": int(e2e["d2h"])},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic, "kernel": "k_stage<2,MUSCL,HLLD,double>",
+                     "bytes_per_launch": alg_bytes, "launch_ms": stage_ms_avg},
+        "fp64_pipe": fp64,
+        "fp32": {"value": value32, "speedup_vs_fp64": value32 / value, "l1_rel_density_vs_fp64_at_t_end": l1,
+                 "t_end_fp32": r32["t_end"], "t_end_fp64": r64["t_end"], "ms_per_step": r32["ms"] / args.steps},
+        "cpu_baseline": cpu,
+        "clocks": {"sm_mhz": clk.get("sm_mhz"), "sm_max_mhz": clk.get("sm_max_mhz"), "reasons": clk.get("reasons", [])},
+        "gpu_launches": int(prof["launches"]),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

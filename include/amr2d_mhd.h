@@ -146,6 +146,24 @@ int amr_get_tree(amr_handle *h, int32_t instance, int32_t *lp, int32_t *icoord, 
 int amr_download(amr_handle *h, int32_t instance, int32_t field, double *dst, int64_t count);
 int amr_upload(amr_handle *h, int32_t instance, int32_t field, const double *src, int64_t count);
 
+/* ---- measurement (no counterpart in the reference, which only has coarse
+ * OpenMP wall-clock timers, main.cpp:237-369) ------------------------------ */
+typedef struct amr_profile {
+  int64_t launches;        /* kernels launched since the last enable/reset */
+  int64_t stage_launches;  /* of which fused RK-stage kernels */
+  double stage_ms;         /* CUDA-event time of the stage kernels, on the launch stream */
+  int64_t stage_cells;     /* leaf interior cells those launches updated */
+  int64_t h2d_bytes;       /* host -> device bytes copied by the handle */
+  int64_t d2h_bytes;
+  double host_compile_ms;  /* host: leaf lists and ghost-fill compilation */
+  double host_admesh_ms;   /* host: quadtree admesh */
+  double wait_ms;          /* host: waiting for the device at step end */
+  int64_t steps;
+} amr_profile;
+/* on != 0 starts recording events around the stage kernels; both reset the counters */
+int amr_profile_enable(amr_handle *h, int32_t on);
+int amr_profile_read(amr_handle *h, amr_profile *out);
+
 #ifdef __cplusplus
 }
 #endif

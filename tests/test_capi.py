@@ -1,0 +1,56 @@
+"""The C-ABI library: it loads without a GPU and exports every entry point
+include/amr2d_mhd.h declares; configuration parsing and argument checks."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import amr2d_mhd_gb300 as amr
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared():
+    src = open(os.path.join(REPO, "include", "amr2d_mhd.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(amr_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_exports_every_declared_symbol():
+    L = amr.load()
+    names = declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    assert sorted(amr.EXPORTS) == names
+
+
+def test_abi_version_and_status_strings():
+    L = amr.load()
+    assert L.amr_abi_version() == 1
+    assert L.amr_status_string(-5) == b"zero or negative pressure"
+
+
+def test_config_from_input_txt(tmp_path):
+    p = tmp_path / "input.txt"
+    p.write_text("16 16 8\n1.0 1.0 \n0.5\nrotor MC RUSA\n")  # the reference's shipped input.txt
+    c = amr.make_config(input_txt=str(p))
+    assert (c.nx, c.ny, c.nvar, c.cfl) == (16, 16, 8, 0.5)
+    assert (c.ic, c.limiter, c.flux) == (b"rotor", b"MC", b"RUSA")
+    assert c.maxlevs == 5 and c.nghosts == 2 and c.nroots_x == 2
+
+
+def test_missing_input_txt(tmp_path):
+    with pytest.raises(amr.AmrError) as e:
+        amr.make_config(input_txt=str(tmp_path / "nope.txt"))
+    assert e.value.code == -1
+
+
+def test_create_rejects_bad_options_before_touching_the_gpu():
+    L = amr.load()
+    h = ctypes.c_void_p()
+    for kw, code in [(dict(limiter="bogus"), -1), (dict(flux="ROE"), -11), (dict(flux="XYZ"), -1),
+                     (dict(limiter="WENO5", nghosts=2), -1), (dict(nx=8, ny=8), -11), (dict(ic="nope"), -1)]:
+        c = amr.make_config(**kw)
+        assert L.amr_create(ctypes.byref(c), ctypes.byref(h)) == code, kw

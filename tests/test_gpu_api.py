@@ -1,0 +1,114 @@
+"""C-ABI behaviour on the GPU: the reference-function entry points, state
+exchange, error reporting, batches and the FP32 path."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as P
+from parity_util import to_gpu_cfg
+
+
+@pytest.mark.gpu
+def test_individual_calls_reproduce_one_step(gpu):
+    """main.cpp:241-315 issued call by call equals amr_step (first step, dt = 0)."""
+    kw = to_gpu_cfg(dict(ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=3))
+    a = gpu.Simulation(**kw).init()
+    b = gpu.Simulation(**kw).init()
+    a.step()
+    b.locate_bounds()
+    b.boundary("U")
+    b.boundary("Bi")
+    b.MUSCL2D(1)
+    b.boundary("Bi")
+    b.boundary("ff")
+    b.boundary("gg")
+    b.CT2D(1)
+    b.boundary("Us")
+    b.MUSCL2D(2)
+    b.boundary("ff")
+    b.boundary("gg")
+    b.CT2D(2)
+    b.boundary("U")
+    lam = b.cfl_dt()
+    assert lam > 0
+    for f in ("U", "Bi", "Us", "Bis"):
+        assert np.array_equal(a.download(f), b.download(f)), f
+
+
+@pytest.mark.gpu
+def test_upload_download_roundtrip(gpu):
+    sim = gpu.Simulation(**to_gpu_cfg(dict(ic="rotor", limiter="MC", flux="RUSA", maxlevs=3))).init()
+    sim.run(3)
+    U = sim.download("U")
+    B = sim.download("Bi")
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal(U.shape)
+    sim.upload("U", X)
+    assert np.array_equal(sim.download("U"), X)
+    sim.upload("U", U)
+    sim.upload("Bi", B)
+    W = sim.download("W")
+    o = P.Oracle(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=3).init()
+    o.run(3)
+    assert np.allclose(W[o.get("leafs")], o.get("W")[o.get("leafs")], rtol=0, atol=0)
+
+
+@pytest.mark.gpu
+def test_negative_pressure_is_reported(gpu):
+    """meshblock.cpp:136-142: a non-positive interior pressure stops the run
+    with AMR_E_PRESSURE (the state is prepared on the host)."""
+    sim = gpu.Simulation(**to_gpu_cfg(dict(ic="BWx", limiter="MC", flux="RUSA", maxlevs=2))).init()
+    U = sim.download("U")
+    lp, ic, lf = sim.tree()
+    b = int(np.nonzero(lf)[0][0])
+    U[b, 4, 8, 8] = 0.5 * (U[b, 1, 8, 8] ** 2 + U[b, 2, 8, 8] ** 2) / U[b, 0, 8, 8] - 1.0  # E below kinetic+magnetic
+    sim.upload("U", U)
+    with pytest.raises(gpu.AmrError) as e:
+        sim.step()
+    assert e.value.code == -5
+    with pytest.raises(gpu.AmrError) as e:   # the handle stays stopped
+        sim.step()
+    assert e.value.code == -9
+
+
+@pytest.mark.gpu
+def test_step_before_init(gpu):
+    sim = gpu.Simulation(**to_gpu_cfg(dict(ic="BWx", maxlevs=2)))
+    with pytest.raises(gpu.AmrError) as e:
+        sim.step()
+    assert e.value.code == -9
+
+
+@pytest.mark.gpu
+def test_batch_matches_single_instances(gpu):
+    """A batch sweeps independent problems in the same launches; each instance
+    is bit-identical to running it alone."""
+    cfgs = [dict(ic="BWx", maxlevs=3), dict(ic="rotor", maxlevs=4), dict(ic="SSTy", limiter="MC", maxlevs=2)]
+    full = [to_gpu_cfg(dict(flux="RUSA", cfl=0.4, **c)) for c in cfgs]
+    batch = gpu.Simulation([gpu.make_config(**c) for c in full]).init()
+    singles = [gpu.Simulation(**c).init() for c in full]
+    for _ in range(15):
+        batch.step()
+        for s in singles:
+            s.step()
+    for q, s in enumerate(singles):
+        assert batch.info(q)["t"] == s.info()["t"]
+        assert np.array_equal(batch.download("U", q), s.download("U"))
+        assert np.array_equal(batch.download("Bi", q), s.download("Bi"))
+
+
+@pytest.mark.gpu
+def test_fp32_density_close_to_fp64(gpu):
+    """FP32 bulk vs the FP64 path on the rotor after 200 steps: relative L1
+    density error on leaf interiors (same tree required for the comparison)."""
+    kw = to_gpu_cfg(dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4))
+    a = gpu.Simulation(**kw).init()
+    kw["precision"] = "fp32"
+    b = gpu.Simulation(**kw).init()
+    a.run(200)
+    b.run(200)
+    sa, sb = a.state(), b.state()
+    assert np.array_equal(sa["leafs"], sb["leafs"])
+    lf = sa["leafs"]
+    ra, rb = sa["U"][lf][:, 0, 2:-2, 2:-2], sb["U"][lf][:, 0, 2:-2, 2:-2]
+    err = np.abs(ra - rb).sum() / np.abs(ra).sum()
+    assert err < 1e-4, err
