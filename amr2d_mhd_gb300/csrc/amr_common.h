@@ -41,33 +41,32 @@ struct InstParams {
   int pad;
 };
 
-// One gather of a compiled ghost fill (see ghost_compile.cpp).
+// One gather of a compiled ghost fill (see ghost_compile.cpp).  The same op
+// list serves the cell, face and edge fills: only the fine-to-coarse value
+// depends on the kind of field, and the kernel applies it per kind.
 //   COPY:   dst <- src                      (value before the fill)
-//   SNAP:   dst <- snapshot[src_slot]       (a pre-fill value of a cell that the
+//   SNAP:   dst <- snapshot row src_slot    (a pre-fill value of a cell the
 //                                            same fill overwrites; saved first)
-//   AVG4:   dst <- 0.25*(s(i,j)+s(i,j+1)+s(i+1,j)+s(i+1,j+1))     boundary.cpp:48
-//   AVGJ:   dst <- 0.5*(s(i,j)+s(i,j+1))                          boundaryfc.cpp:48, k==0
-//   AVGI:   dst <- 0.5*(s(i,j)+s(i+1,j))                          boundaryfc.cpp:48, k>0
-//   SAVG4 / SAVGJ / SAVGI: the same averages of saved pre-fill values (rows
-//                          src_slot.. of the snapshot buffer, in stencil order)
-enum GhostOpType : uint8_t { GOP_COPY = 0, GOP_SNAP = 1, GOP_AVG4 = 2, GOP_AVGJ = 3, GOP_AVGI = 4,
-                             GOP_SAVG4 = 5, GOP_SAVGJ = 6, GOP_SAVGI = 7 };
+//   FINE:   dst <- fine-to-coarse value of the 2x2 patch with lower-left src:
+//             cell  0.25*(s(i,j)+s(i,j+1)+s(i+1,j)+s(i+1,j+1))   boundary.cpp:48
+//             face  0.5*(s(i,j)+s(i,j+1)) for k==0,
+//                   0.5*(s(i,j)+s(i+1,j)) for k>0                boundaryfc.cpp:48
+//             edge  s(i,j)                                       boundaryec.cpp:46
+//   SFINE:  the same from four saved pre-fill values (snapshot rows src_slot..
+//           src_slot+3 in the order (i,j) (i,j+1) (i+1,j) (i+1,j+1))
+enum GhostOpType : uint8_t { GOP_COPY = 0, GOP_SNAP = 1, GOP_FINE = 2, GOP_SFINE = 3 };
 struct GhostOp {
   int dst_slot;
-  int src_slot;     // for GOP_SNAP: index into the snapshot buffer (times nvar)
+  int src_slot;     // physical slot, or first snapshot row for SNAP / SFINE
   int16_t dst_pos;  // j * N + i within the block plane
   int16_t src_pos;
-  uint8_t type;
-  uint8_t k0, k1;   // variables [k0, k1) this gather applies to
-  uint8_t field;    // which field of a merged fill (index into the field table)
+  uint8_t type;     // GhostOpType
+  uint8_t pad[3];
 };
-// A pre-fill value that must be saved before a fill runs.
+// A pre-fill cell saved before a fill runs (all variables of the field).
 struct GhostSnap {
   int slot;
-  int16_t pos;
-  uint8_t k0, k1;
-  uint8_t field;
-  uint8_t pad[3];
+  int pos;
 };
 
 // refine (dad -> 4 sons) or coarsen (4 sons -> dad) in physical slots

@@ -3,6 +3,7 @@
 // FP64 instantiations reproduce the reference's arithmetic.
 #include "aux_kernels.cuh"
 #include "launch.hpp"
+#include "stage_split.cuh"
 
 namespace amr {
 
@@ -31,15 +32,58 @@ cudaError_t launch_stage(const Method &m, const StageArgs &a, int n, cudaStream_
   }
 }
 
-cudaError_t launch_ghost(int ng, const GhostLaunch &g, int nsnaps, int nops, cudaStream_t s) {
-  constexpr int B = 256;
-  if (nsnaps > 0) {
-    if (ng == 2) k_ghost_snap<Geo<2>::N><<<(nsnaps + B - 1) / B, B, 0, s>>>(g);
-    else k_ghost_snap<Geo<4>::N><<<(nsnaps + B - 1) / B, B, 0, s>>>(g);
+cudaError_t launch_faces(const Method &m, const SplitArgs &a, cudaStream_t s) {
+  if (!method_supported(m)) return cudaErrorInvalidValue;
+  if (!m.f32) {
+    switch (m.flux) {
+      case FLX_RUSA: return launch_faces_f64_rusa(m, a, s);
+      case FLX_HLLE: return launch_faces_f64_hlle(m, a, s);
+      case FLX_HLLC: return launch_faces_f64_hllc(m, a, s);
+      default: return launch_faces_f64_hlld(m, a, s);
+    }
   }
-  if (nops > 0) {
-    if (ng == 2) k_ghost_apply<Geo<2>::N><<<(nops + B - 1) / B, B, 0, s>>>(g);
-    else k_ghost_apply<Geo<4>::N><<<(nops + B - 1) / B, B, 0, s>>>(g);
+  switch (m.flux) {
+    case FLX_RUSA: return launch_faces_f32_rusa(m, a, s);
+    case FLX_HLLE: return launch_faces_f32_hlle(m, a, s);
+    case FLX_HLLC: return launch_faces_f32_hllc(m, a, s);
+    default: return launch_faces_f32_hlld(m, a, s);
+  }
+}
+
+cudaError_t launch_prim(const Method &m, const SplitArgs &a, cudaStream_t s) {
+  const int nn = m.ng == 2 ? Geo<2>::NN : Geo<4>::NN;
+  const size_t n = static_cast<size_t>(a.ntasks) * nn;
+  if (n == 0) return cudaSuccess;
+  const unsigned g = static_cast<unsigned>((n + 255) / 256);
+  if (m.ng == 2 && !m.f32) k_prim<2, double><<<g, 256, 0, s>>>(a);
+  else if (m.ng == 2) k_prim<2, float><<<g, 256, 0, s>>>(a);
+  else if (!m.f32) k_prim<4, double><<<g, 256, 0, s>>>(a);
+  else k_prim<4, float><<<g, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resid(const Method &m, const SplitArgs &a, cudaStream_t s) {
+  const int nn = m.ng == 2 ? Geo<2>::NN : Geo<4>::NN;
+  const size_t n = static_cast<size_t>(a.ntasks) * 8 * nn;
+  if (n == 0) return cudaSuccess;
+  const unsigned g = static_cast<unsigned>((n + 255) / 256);
+  if (m.ng == 2 && !m.f32) k_resid<2, double><<<g, 256, 0, s>>>(a);
+  else if (m.ng == 2) k_resid<2, float><<<g, 256, 0, s>>>(a);
+  else if (!m.f32) k_resid<4, double><<<g, 256, 0, s>>>(a);
+  else k_resid<4, float><<<g, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ghost(int ng, const GhostLaunch &g, cudaStream_t s) {
+  constexpr int B = 256;
+  const int ns = g.nsnaps * g.nseg, no = g.nops * g.nseg;
+  if (ns > 0) {
+    if (ng == 2) k_ghost_snap<Geo<2>::N><<<(ns + B - 1) / B, B, 0, s>>>(g);
+    else k_ghost_snap<Geo<4>::N><<<(ns + B - 1) / B, B, 0, s>>>(g);
+  }
+  if (no > 0) {
+    if (ng == 2) k_ghost_apply<Geo<2>::N><<<(no + B - 1) / B, B, 0, s>>>(g);
+    else k_ghost_apply<Geo<4>::N><<<(no + B - 1) / B, B, 0, s>>>(g);
   }
   return cudaGetLastError();
 }

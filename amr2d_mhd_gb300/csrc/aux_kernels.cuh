@@ -9,93 +9,89 @@
 namespace amr {
 
 // ------------------------------------------------------------ ghost fills
-// A launch applies up to kMaxSeg (program, field) segments.
+// One compiled program (ops + snapshots) serves every field; a launch applies
+// it to up to kMaxSeg fields at once.
 constexpr int kMaxSeg = 3;
 struct GhostSeg {
-  const GhostOp *ops;
-  const GhostSnap *snaps;
-  int nops, nsnaps;
-  int snap_off;       // first snapshot row of this segment
   void *field;
   int nv;
+  int kind;           // FILL_CC / FILL_FC / FILL_EC (ghost_compile.hpp)
   int f32;            // field stored as float
 };
 struct GhostLaunch {
+  const GhostOp *ops;
+  const GhostSnap *snaps;
+  int nops, nsnaps;
   GhostSeg seg[kMaxSeg];
   int nseg;
-  double *snapbuf;    // [total snaps][8]
+  double *snapbuf;    // [nseg][nsnaps][8]
 };
 
-template <int N>
-__device__ __forceinline__ double gload(const GhostSeg &s, int slot, int k, int pos) {
-  const size_t idx = (static_cast<size_t>(slot) * s.nv + k) * (N * N) + pos;
-  return s.f32 ? static_cast<double>(static_cast<const float *>(s.field)[idx])
-               : static_cast<const double *>(s.field)[idx];
+template <int N, typename F>
+__device__ __forceinline__ void ghost_snap_one(const GhostSeg &s, const GhostSnap &sn, double *row) {
+  const F *f = static_cast<const F *>(s.field) + static_cast<size_t>(sn.slot) * s.nv * (N * N) + sn.pos;
+  for (int k = 0; k < s.nv; k++) row[k] = static_cast<double>(f[k * N * N]);
 }
 
 // save the pre-fill values the same fill overwrites
 template <int N>
 __global__ void k_ghost_snap(GhostLaunch g) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int q = 0; q < g.nseg; q++) {
-    const GhostSeg &s = g.seg[q];
-    if (t < s.nsnaps) {
-      const GhostSnap sn = s.snaps[t];
-      for (int k = sn.k0; k < sn.k1; k++)
-        g.snapbuf[static_cast<size_t>(s.snap_off + t) * 8 + k] = gload<N>(s, sn.slot, k, sn.pos);
-      return;
-    }
-    t -= s.nsnaps;
-  }
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nsnaps * g.nseg) return;
+  const int q = t / g.nsnaps, r = t % g.nsnaps;
+  const GhostSeg &s = g.seg[q];
+  double *row = g.snapbuf + (static_cast<size_t>(q) * g.nsnaps + r) * 8;
+  if (s.f32) ghost_snap_one<N, float>(s, g.snaps[r], row);
+  else ghost_snap_one<N, double>(s, g.snaps[r], row);
 }
 
-// boundary.cpp / boundaryfc.cpp / boundaryec.cpp as compiled gathers
+// fine-to-coarse value of one variable from the patch (i,j) (i,j+1) (i+1,j)
+// (i+1,j+1): boundary.cpp:48 / boundaryfc.cpp:48 / boundaryec.cpp:46
+template <typename F>
+__device__ __forceinline__ F fine_value(int kind, int k, F a00, F a01, F a10, F a11) {
+  F v = F(0.);
+  if (kind == 0) {
+    v += a00; v += a01; v += a10; v += a11;
+    return F(0.25) * v;
+  }
+  if (kind == 1) {
+    v += a00;
+    v += k == 0 ? a01 : a10;
+    return F(0.5) * v;
+  }
+  return a00;
+}
+
 template <int N, typename F>
-__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, const double *snapbuf) {
+__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, const double *snap) {
   constexpr int NN = N * N;
   F *fld = static_cast<F *>(s.field);
-  const F *src = fld + static_cast<size_t>(op.src_slot) * s.nv * NN + op.src_pos;
   F *dst = fld + static_cast<size_t>(op.dst_slot) * s.nv * NN + op.dst_pos;
-  for (int k = op.k0; k < op.k1; k++) {
-    F v;
-    switch (op.type) {
-      case GOP_COPY: v = src[k * NN]; break;
-      case GOP_SNAP: v = static_cast<F>(snapbuf[static_cast<size_t>(s.snap_off + op.src_slot) * 8 + k]); break;
-      case GOP_AVG4: {  // sum_irjr order: (i,j) (i,j+1) (i+1,j) (i+1,j+1)
-        F a = F(0.);
-        a += src[k * NN];
-        a += src[k * NN + N];
-        a += src[k * NN + 1];
-        a += src[k * NN + 1 + N];
-        v = F(0.25) * a;
-      } break;
-      case GOP_AVGJ: { F a = F(0.); a += src[k * NN]; a += src[k * NN + N]; v = F(0.5) * a; } break;
-      case GOP_AVGI: { F a = F(0.); a += src[k * NN]; a += src[k * NN + 1]; v = F(0.5) * a; } break;
-      default: {  // SAVG4 / SAVGJ / SAVGI
-        const double *sv = snapbuf + static_cast<size_t>(s.snap_off + op.src_slot) * 8 + k;
-        const int nc = op.type == GOP_SAVG4 ? 4 : 2;
-        F a = F(0.);
-        for (int q = 0; q < nc; q++) a += static_cast<F>(sv[q * 8]);
-        v = (op.type == GOP_SAVG4 ? F(0.25) : F(0.5)) * a;
-      } break;
+  if (op.type == GOP_COPY || op.type == GOP_FINE) {
+    const F *src = fld + static_cast<size_t>(op.src_slot) * s.nv * NN + op.src_pos;
+    for (int k = 0; k < s.nv; k++) {
+      const F *c = src + k * NN;
+      dst[k * NN] = op.type == GOP_COPY ? c[0] : fine_value<F>(s.kind, k, c[0], c[N], c[1], c[1 + N]);
     }
-    dst[k * NN] = v;
+  } else {
+    const double *r = snap + static_cast<size_t>(op.src_slot) * 8;
+    for (int k = 0; k < s.nv; k++) {
+      if (op.type == GOP_SNAP) dst[k * NN] = static_cast<F>(r[k]);
+      else dst[k * NN] = fine_value<F>(s.kind, k, static_cast<F>(r[k]), static_cast<F>(r[8 + k]),
+                                       static_cast<F>(r[16 + k]), static_cast<F>(r[24 + k]));
+    }
   }
 }
 
 template <int N>
 __global__ void k_ghost_apply(GhostLaunch g) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int q = 0; q < g.nseg; q++) {
-    const GhostSeg &s = g.seg[q];
-    if (t < s.nops) {
-      const GhostOp op = s.ops[t];
-      if (s.f32) ghost_apply_one<N, float>(s, op, g.snapbuf);
-      else ghost_apply_one<N, double>(s, op, g.snapbuf);
-      return;
-    }
-    t -= s.nops;
-  }
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nops * g.nseg) return;
+  const int q = t / g.nops, r = t % g.nops;
+  const GhostSeg &s = g.seg[q];
+  const double *snap = g.snapbuf + static_cast<size_t>(q) * g.nsnaps * 8;
+  if (s.f32) ghost_apply_one<N, float>(s, g.ops[r], snap);
+  else ghost_apply_one<N, double>(s, g.ops[r], snap);
 }
 
 // ------------------------------------------------------------- CT2D.cpp
@@ -207,6 +203,7 @@ __global__ void __launch_bounds__(256) k_dt_crit(DtArgs a) {
 #pragma unroll
     for (int k = 0; k < 8; k++) u[k] = static_cast<double>(U[k * NN + c]);
     cons2prim_cell<double>(u, w, g);
+    if (sizeof(S) == sizeof(float) && !(w[4] > kPressureFloor)) w[4] = kPressureFloor;  // FP32 path
     sW[0][c] = w[0]; sW[1][c] = w[1]; sW[2][c] = w[4]; sW[3][c] = w[5]; sW[4][c] = w[6];
     const int i = c % N, j = c / N;
     if (w[4] <= 0 && i > G::LO && i < G::HI + 1 && j > G::LO && j < G::HI + 1)

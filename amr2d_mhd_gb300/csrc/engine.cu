@@ -2,12 +2,14 @@
 #include "engine.hpp"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <initializer_list>
 #include <chrono>
 #include <string>
 
 #include "aux_kernels.cuh"
+#include "stage_split.cuh"
 
 namespace amr {
 
@@ -67,11 +69,12 @@ int map_dev_error(int code) {
 
 Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
-  for (void *p : {U_, Us_, ff_, gg_}) if (p) cudaFree(p);
+  for (void *p : {U_, Us_, ff_, gg_, W_}) if (p) cudaFree(p);
   for (double *p : {Bi_, Bis_, EMF_}) if (p) cudaFree(p);
   for (DevBuf *b : {&d_tasks_, &d_params_, &d_lambda_, &d_grad_, &d_err_, &d_snap_, &d_treeops_, &d_stage_, &d_slots_})
     b->release();
-  for (int i = 0; i < 4; i++) { d_ops_[i].release(); d_snaps_[i].release(); }
+  d_ops_.release();
+  d_snaps_.release();
   for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_}) b->release();
   if (own_stream_ && stream_) cudaStreamDestroy(stream_);
   delete gc_;
@@ -128,6 +131,7 @@ int Engine::create(const amr_config *cfgs, int n) {
   m_.f32 = c0.precision == AMR_FP32 ? 1 : 0;
   if (!method_supported(m_)) return fail(AMR_E_UNSUPPORTED, "method not compiled");
   f32_ = m_.f32 != 0;
+  if (const char *k = std::getenv("AMR2D_STAGE_KERNEL")) split_ = std::strcmp(k, "fused") != 0;
   ng_ = m_.ng;
   n_ = NI + 2 * ng_;
   nn_ = n_ * n_;
@@ -208,7 +212,7 @@ int Engine::ensure_slots(int needed) {
   CK(cudaStreamSynchronize(stream_), "sync");
   const size_t cell = static_cast<size_t>(8) * nn_, face = static_cast<size_t>(2) * nn_, edge = nn_;
   const size_t se = f32_ ? sizeof(float) : sizeof(double);
-  void **cells[4] = {&U_, &Us_, &ff_, &gg_};
+  void **cells[5] = {&U_, &Us_, &ff_, &gg_, &W_};
   for (void **pp : cells) {
     void *np = nullptr;
     CK(cudaMalloc(&np, cap * cell * se), "pool alloc");
@@ -253,7 +257,7 @@ int Engine::rebuild() {
   const auto t0 = std::chrono::steady_clock::now();
   tasks_.clear();
   task_blk_.clear();
-  for (auto &p : prog_) p.clear();
+  prog_.clear();
   std::vector<Bound> bounds;
   for (int a : active_) {
     Instance &in = inst_[a];
@@ -267,10 +271,7 @@ int Engine::rebuild() {
     in.task_end = static_cast<int>(tasks_.size());
     in.tree.locate_bounds(bounds);
     try {
-      gc_->compile(in.tree, bounds, FILL_CC, 8, in.slot.data(), 0, prog_[0]);
-      gc_->compile(in.tree, bounds, FILL_FC, 2, in.slot.data(), 0, prog_[1]);
-      gc_->compile(in.tree, bounds, FILL_FC, 8, in.slot.data(), 0, prog_[2]);
-      gc_->compile(in.tree, bounds, FILL_EC, 1, in.slot.data(), 0, prog_[3]);
+      gc_->compile(in.tree, bounds, in.slot.data(), prog_);
     } catch (const std::exception &ex) {
       return fail(AMR_E_STATE, ex.what());
     }
@@ -284,24 +285,21 @@ int Engine::rebuild() {
   CK(d_grad_.ensure(sizeof(double) * nt), "alloc");
   CK(h_lambda_.ensure(sizeof(double) * nt), "alloc");
   CK(h_grad_.ensure(sizeof(double) * nt), "alloc");
-  size_t nsnap = 0;
-  for (int p = 0; p < 4; p++) {
-    CK(d_ops_[p].ensure(sizeof(GhostOp) * prog_[p].ops.size()), "alloc");
-    CK(d_snaps_[p].ensure(sizeof(GhostSnap) * prog_[p].snaps.size()), "alloc");
-    if (!prog_[p].ops.empty())
-      CK(cudaMemcpyAsync(d_ops_[p].p, prog_[p].ops.data(), sizeof(GhostOp) * prog_[p].ops.size(),
-                         cudaMemcpyHostToDevice, stream_), "h2d");
-    if (!prog_[p].snaps.empty())
-      CK(cudaMemcpyAsync(d_snaps_[p].p, prog_[p].snaps.data(), sizeof(GhostSnap) * prog_[p].snaps.size(),
-                         cudaMemcpyHostToDevice, stream_), "h2d");
-    nsnap += 2 * prog_[p].snaps.size();
-  }
+  CK(d_ops_.ensure(sizeof(GhostOp) * prog_.ops.size()), "alloc");
+  CK(d_snaps_.ensure(sizeof(GhostSnap) * prog_.snaps.size()), "alloc");
+  if (!prog_.ops.empty())
+    CK(cudaMemcpyAsync(d_ops_.p, prog_.ops.data(), sizeof(GhostOp) * prog_.ops.size(), cudaMemcpyHostToDevice,
+                       stream_), "h2d");
+  if (!prog_.snaps.empty())
+    CK(cudaMemcpyAsync(d_snaps_.p, prog_.snaps.data(), sizeof(GhostSnap) * prog_.snaps.size(),
+                       cudaMemcpyHostToDevice, stream_), "h2d");
+  const size_t nsnap = static_cast<size_t>(kMaxSeg) * prog_.snaps.size();
   CK(d_snap_.ensure(sizeof(double) * 8 * (nsnap + 1)), "alloc");
   // the host vectors above must outlive the async copies
   CK(cudaStreamSynchronize(stream_), "sync");
   programs_valid_ = true;
   size_t bytes = sizeof(LeafTask) * nt;
-  for (int p = 0; p < 4; p++) bytes += sizeof(GhostOp) * prog_[p].ops.size() + sizeof(GhostSnap) * prog_[p].snaps.size();
+  bytes += sizeof(GhostOp) * prog_.ops.size() + sizeof(GhostSnap) * prog_.snaps.size();
   prof_.h2d_bytes += static_cast<int64_t>(bytes);
   prof_.launches += 0;
   prof_.host_compile_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -324,56 +322,82 @@ int Engine::upload_params() {
 // ------------------------------------------------------------- kernels
 int Engine::fill(std::initializer_list<std::pair<FillKind, int>> what) {
   GhostLaunch g{};
-  int nsnap = 0, nops = 0, q = 0;
+  g.ops = d_ops_.as<GhostOp>();
+  g.snaps = d_snaps_.as<GhostSnap>();
+  g.nops = static_cast<int>(prog_.ops.size());
+  g.nsnaps = static_cast<int>(prog_.snaps.size());
+  int q = 0;
   for (const auto &w : what) {
-    const int nv = field_nv(w.second);
-    const int p = w.first == FILL_CC ? 0 : (w.first == FILL_EC ? 3 : (nv == 2 ? 1 : 2));
     GhostSeg &s = g.seg[q++];
-    s.ops = d_ops_[p].as<GhostOp>();
-    s.snaps = d_snaps_[p].as<GhostSnap>();
-    s.nops = static_cast<int>(prog_[p].ops.size());
-    s.nsnaps = static_cast<int>(prog_[p].snaps.size());
-    s.snap_off = nsnap;
     s.field = field_ptr(w.second);
-    s.nv = nv;
+    s.nv = field_nv(w.second);
+    s.kind = w.first;
     s.f32 = field_f32(w.second) ? 1 : 0;
-    nsnap += s.nsnaps;
-    nops += s.nops;
   }
   g.nseg = q;
   g.snapbuf = d_snap_.as<double>();
-  CK(launch_ghost(ng_, g, nsnap, nops, stream_), "ghost fill");
-  prof_.launches += (nsnap > 0) + (nops > 0);
+  CK(launch_ghost(ng_, g, stream_), "ghost fill");
+  prof_.launches += (g.nsnaps > 0) + (g.nops > 0);
   return AMR_OK;
 }
 
 int Engine::stage(int step) {
-  StageArgs a{};
-  a.tasks = d_tasks_.as<LeafTask>();
-  a.inst = d_params_.as<InstParams>();
-  a.qin = step == 1 ? U_ : Us_;
-  a.qout = step == 1 ? Us_ : U_;
-  a.B = step == 1 ? Bi_ : Bis_;
-  a.ff = ff_;
-  a.gg = gg_;
-  a.err = d_err_.as<DevError>();
-  a.step = step;
-  if (prof_on_) {
+  // profiling events bracket the dominant kernel: the face-flux kernel of the
+  // split stage, or the fused stage kernel
+  auto ev_begin = [&]() -> int {
+    if (!prof_on_) return AMR_OK;
     while (ev_.size() < static_cast<size_t>(ev_used_ + 2)) {
       cudaEvent_t e;
       CK(cudaEventCreate(&e), "event");
       ev_.push_back(e);
     }
     CK(cudaEventRecord(ev_[ev_used_], stream_), "event");
-  }
-  CK(launch_stage(m_, a, static_cast<int>(tasks_.size()), stream_), "stage kernel");
-  if (prof_on_) {
+    return AMR_OK;
+  };
+  auto ev_end = [&]() -> int {
+    if (!prof_on_) return AMR_OK;
     CK(cudaEventRecord(ev_[ev_used_ + 1], stream_), "event");
     ev_used_ += 2;
+    return AMR_OK;
+  };
+  const int n = static_cast<int>(tasks_.size());
+  if (split_) {
+    SplitArgs a{};
+    a.tasks = d_tasks_.as<LeafTask>();
+    a.inst = d_params_.as<InstParams>();
+    a.qin = step == 1 ? U_ : Us_;
+    a.qout = step == 1 ? Us_ : U_;
+    a.W = W_;
+    a.B = step == 1 ? Bi_ : Bis_;
+    a.ff = ff_;
+    a.gg = gg_;
+    a.err = d_err_.as<DevError>();
+    a.step = step;
+    a.ntasks = n;
+    CK(launch_prim(m_, a, stream_), "prim kernel");
+    if (int rc = ev_begin()) return rc;
+    CK(launch_faces(m_, a, stream_), "face kernel");
+    if (int rc = ev_end()) return rc;
+    CK(launch_resid(m_, a, stream_), "residual kernel");
+    prof_.launches += 3;
+  } else {
+    StageArgs a{};
+    a.tasks = d_tasks_.as<LeafTask>();
+    a.inst = d_params_.as<InstParams>();
+    a.qin = step == 1 ? U_ : Us_;
+    a.qout = step == 1 ? Us_ : U_;
+    a.B = step == 1 ? Bi_ : Bis_;
+    a.ff = ff_;
+    a.gg = gg_;
+    a.err = d_err_.as<DevError>();
+    a.step = step;
+    if (int rc = ev_begin()) return rc;
+    CK(launch_stage(m_, a, n, stream_), "stage kernel");
+    if (int rc = ev_end()) return rc;
+    prof_.launches += 1;
   }
-  prof_.launches += 1;
   prof_.stage_launches += 1;
-  stage_cells_pending_ += static_cast<int64_t>(tasks_.size()) * NI * NI;
+  stage_cells_pending_ += static_cast<int64_t>(n) * NI * NI;
   return AMR_OK;
 }
 

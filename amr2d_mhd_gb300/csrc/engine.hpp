@@ -103,6 +103,7 @@ class Engine {
   Method m_{};
   int ng_ = 2, n_ = 20, nn_ = 400;
   bool f32_ = false;
+  bool split_ = true;              // stage as prim / faces / resid kernels (else fused k_stage)
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
   bool initialised_ = false;
@@ -110,7 +111,7 @@ class Engine {
 
   // block pool
   int cap_slots_ = 0, used_slots_ = 0;
-  void *U_ = nullptr, *Us_ = nullptr, *ff_ = nullptr, *gg_ = nullptr;
+  void *U_ = nullptr, *Us_ = nullptr, *ff_ = nullptr, *gg_ = nullptr, *W_ = nullptr;
   double *Bi_ = nullptr, *Bis_ = nullptr, *EMF_ = nullptr;
 
   // active set and compiled programs
@@ -120,8 +121,8 @@ class Engine {
   bool programs_valid_ = false;
   std::vector<LeafTask> tasks_;
   std::vector<int> task_blk_;      // block ID of each task
-  GhostProgram prog_[4];           // cc8, fc2, fc8, ec1
-  DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_[4], d_snaps_[4];
+  GhostProgram prog_;              // ghost fill of the active set (all fields)
+  DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_, d_snaps_;
   DevBuf d_treeops_, d_stage_, d_slots_;
   HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_stage_;
   GhostCompiler *gc_ = nullptr;

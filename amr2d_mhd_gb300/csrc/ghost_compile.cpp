@@ -23,11 +23,10 @@ void GhostCompiler::set(int blk, int pos, const Desc &d) {
   cur_[idx] = d;
 }
 
-// One pass over the innerbounds list for one class of variables (the face
-// fill averages k==0 and k>0 along different directions).  The index
-// arithmetic is that of boundary.cpp (identical in the three files).
-void GhostCompiler::run_sequence(const Tree &t, const std::vector<Bound> &bounds, FillKind kind,
-                                 int kclass) {
+// One pass over the innerbounds list.  The index arithmetic is that of
+// boundary.cpp, identical in the three files; the fine-to-coarse value is kept
+// symbolic (GOP_FINE) and made concrete per kind of field by the kernel.
+void GhostCompiler::run_sequence(const Tree &t, const std::vector<Bound> &bounds) {
   const int n = n_, ng = ng_, nx = n, ny = n;
   const int nxmin = ng, nxmax = n - 1 - ng, nymin = ng, nymax = n - 1 - ng;
   const int nxminb = nxmin - 1, nxmaxb = nxmax + 1, nyminb = nymin - 1, nymaxb = nymax + 1;
@@ -41,29 +40,20 @@ void GhostCompiler::run_sequence(const Tree &t, const std::vector<Bound> &bounds
   auto C = [&](int db, int di, int dj, int sb, int si, int sj) {
     set(db, P(di, dj), get(sb, P(si, sj)));
   };
-  // fine-to-coarse value with lower-left source cell (i1, j1)
+  // fine-to-coarse value with lower-left source cell (i1, j1).  With 4 ghost
+  // layers the reference's left / bottom stencils reach one ghost column /
+  // row of the fine block (boundary.cpp:43 and :227 give 2i+13 where 2i+12 is
+  // meant); such a cell must still hold its pre-fill value here, and
+  // compile() saves it first if the fill overwrites it later.
   auto Fv = [&](int db, int di, int dj, int sb, int i1, int j1) {
-    if (kind == FILL_EC) {            // boundaryec.cpp:46-47: injection
-      C(db, di, dj, sb, i1, j1);
-      return;
-    }
-    uint8_t ty;
-    int i2 = i1 + 1, j2 = j1 + 1;
-    if (kind == FILL_CC) ty = GOP_AVG4;
-    else if (kclass == 0) { ty = GOP_AVGJ; i2 = i1; }
-    else { ty = GOP_AVGI; j2 = j1; }
-    // with 4 ghost layers the reference's left / bottom fine-to-coarse
-    // stencils reach one ghost column / row of the fine block (boundary.cpp:43
-    // and :227 give 2i+13 where 2i+12 is meant); such a cell must still hold
-    // its pre-fill value here, and compile() snapshots it if the fill
-    // overwrites it later
-    for (int i = i1; i <= i2; i++)
-      for (int j = j1; j <= j2; j++) {
+    for (int i = i1; i <= i1 + 1; i++)
+      for (int j = j1; j <= j1 + 1; j++) {
+        if (interior(i, j)) continue;
         const Desc d = get(sb, P(i, j));
-        if (!interior(i, j) && !(d.type == 0 && d.blk == sb && d.pos == P(i, j)))
+        if (!(d.type == GOP_COPY && d.blk == sb && d.pos == P(i, j)))
           throw std::logic_error("ghost compile: fine average of an already filled ghost cell");
       }
-    set(db, P(di, dj), Desc{sb, static_cast<int16_t>(P(i1, j1)), ty});
+    set(db, P(di, dj), Desc{sb, static_cast<int16_t>(P(i1, j1)), GOP_FINE});
   };
 
   for (const Bound &b : bounds) {
@@ -315,99 +305,71 @@ void GhostCompiler::run_sequence(const Tree &t, const std::vector<Bound> &bounds
   }
 }
 
-void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, FillKind kind,
-                            int nv, const int *slot, uint8_t field, GhostProgram &out) {
+bool GhostCompiler::overwritten(int blk, int pos) const {
+  const size_t idx = static_cast<size_t>(blk) * nn_ + pos;
+  if (stamp_[idx] != gen_) return false;
+  const Desc &s = cur_[idx];
+  return !(s.type == GOP_COPY && s.blk == blk && s.pos == pos);
+}
+
+void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, const int *slot, GhostProgram &out) {
   nn_ = n_ * n_;
   const size_t need = static_cast<size_t>(t.lastActive) * nn_;
   if (stamp_.size() < need) {
     stamp_.resize(need, 0);
     cur_.resize(need);
+    snap_stamp_.resize(need, 0);
+    snap_row_.resize(need);
   }
-  const int nclass = (kind == FILL_FC && nv > 1) ? 2 : 1;
-  for (int kc = 0; kc < nclass; kc++) {
-    int k0 = 0, k1 = nv;
-    if (kind == FILL_FC) { k0 = kc == 0 ? 0 : 1; k1 = kc == 0 ? 1 : nv; }
-    if (++gen_ == 0) {  // stamp wrap-around
-      std::fill(stamp_.begin(), stamp_.end(), 0u);
-      gen_ = 1;
+  if (++gen_ == 0) {  // stamp wrap-around
+    std::fill(stamp_.begin(), stamp_.end(), 0u);
+    std::fill(snap_stamp_.begin(), snap_stamp_.end(), 0u);
+    gen_ = 1;
+  }
+  touched_.clear();
+  run_sequence(t, bounds);
+  // a pre-fill value that the fill overwrites is read from a saved copy
+  auto snap_of = [&](int blk, int pos) {
+    const size_t idx = static_cast<size_t>(blk) * nn_ + pos;
+    if (snap_stamp_[idx] != gen_) {
+      snap_stamp_[idx] = gen_;
+      snap_row_[idx] = static_cast<int>(out.snaps.size());
+      out.snaps.push_back(GhostSnap{slot[blk], pos});
     }
-    touched_.clear();
-    run_sequence(t, bounds, kind, kc);
-    std::sort(touched_.begin(), touched_.end());
-    std::unordered_map<int, int> snap_of;
-    for (const int idx : touched_) {
-      const Desc &d = cur_[idx];
-      const int blk = idx / nn_, pos = idx % nn_;
-      if (d.type == 0 && d.blk == blk && d.pos == pos) continue;  // unchanged
-      GhostOp op{};
-      op.dst_slot = slot[blk];
-      op.dst_pos = static_cast<int16_t>(pos);
-      op.k0 = static_cast<uint8_t>(k0);
-      op.k1 = static_cast<uint8_t>(k1);
-      op.field = field;
-      if (d.type == 0) {
-        const int sidx = d.blk * nn_ + d.pos;
-        const Desc &s = cur_[sidx];
-        const bool overwritten =
-            stamp_[sidx] == gen_ && !(s.type == 0 && s.blk == d.blk && s.pos == d.pos);
-        if (overwritten) {
-          auto it = snap_of.find(sidx);
-          int si;
-          if (it == snap_of.end()) {
-            si = static_cast<int>(out.snaps.size());
-            GhostSnap sn{};
-            sn.slot = slot[d.blk];
-            sn.pos = d.pos;
-            sn.k0 = op.k0;
-            sn.k1 = op.k1;
-            sn.field = field;
-            out.snaps.push_back(sn);
-            snap_of.emplace(sidx, si);
-          } else {
-            si = it->second;
-          }
-          op.type = GOP_SNAP;
-          op.src_slot = si;
-          op.src_pos = 0;
-        } else {
-          op.type = GOP_COPY;
-          op.src_slot = slot[d.blk];
-          op.src_pos = d.pos;
-        }
+    return snap_row_[idx];
+  };
+  out.ops.reserve(out.ops.size() + touched_.size());
+  for (const int idx : touched_) {
+    const Desc &d = cur_[idx];
+    const int blk = idx / nn_, pos = idx % nn_;
+    if (d.type == GOP_COPY && d.blk == blk && d.pos == pos) continue;  // unchanged
+    GhostOp op{};
+    op.dst_slot = slot[blk];
+    op.dst_pos = static_cast<int16_t>(pos);
+    if (d.type == GOP_COPY) {
+      if (overwritten(d.blk, d.pos)) {
+        op.type = GOP_SNAP;
+        op.src_slot = snap_of(d.blk, d.pos);
       } else {
-        // stencil of the average in sum_irjr order
-        int cells[4], nc = 0;
-        const int p0 = d.pos;
-        if (d.type == GOP_AVG4) { cells[0] = p0; cells[1] = p0 + n_; cells[2] = p0 + 1; cells[3] = p0 + 1 + n_; nc = 4; }
-        else if (d.type == GOP_AVGJ) { cells[0] = p0; cells[1] = p0 + n_; nc = 2; }
-        else { cells[0] = p0; cells[1] = p0 + 1; nc = 2; }
-        bool hazard = false;
-        for (int q = 0; q < nc; q++) {
-          const int sidx = d.blk * nn_ + cells[q];
-          const Desc &s = cur_[sidx];
-          hazard |= stamp_[sidx] == gen_ && !(s.type == 0 && s.blk == d.blk && s.pos == cells[q]);
-        }
-        if (!hazard) {
-          op.type = d.type;
-          op.src_slot = slot[d.blk];
-          op.src_pos = d.pos;
-        } else {  // average of saved pre-fill values
-          op.type = static_cast<uint8_t>(d.type + (GOP_SAVG4 - GOP_AVG4));
-          op.src_slot = static_cast<int>(out.snaps.size());
-          op.src_pos = 0;
-          for (int q = 0; q < nc; q++) {
-            GhostSnap sn{};
-            sn.slot = slot[d.blk];
-            sn.pos = static_cast<int16_t>(cells[q]);
-            sn.k0 = op.k0;
-            sn.k1 = op.k1;
-            sn.field = field;
-            out.snaps.push_back(sn);
-          }
-        }
+        op.type = GOP_COPY;
+        op.src_slot = slot[d.blk];
+        op.src_pos = d.pos;
       }
-      out.ops.push_back(op);
+    } else {
+      const int c[4] = {d.pos, d.pos + n_, d.pos + 1, d.pos + 1 + n_};  // sum_irjr order
+      bool hazard = false;
+      for (int q = 0; q < 4; q++) hazard |= overwritten(d.blk, c[q]);
+      if (!hazard) {
+        op.type = GOP_FINE;
+        op.src_slot = slot[d.blk];
+        op.src_pos = d.pos;
+      } else {  // four consecutive rows, whether or not each was saved before
+        op.type = GOP_SFINE;
+        op.src_slot = static_cast<int>(out.snaps.size());
+        for (int q = 0; q < 4; q++) out.snaps.push_back(GhostSnap{slot[d.blk], c[q]});
+      }
     }
+    out.ops.push_back(op);
   }
 }
 

@@ -19,6 +19,8 @@
 
 namespace amr {
 
+// cell centred (boundary.cpp), face centred (boundaryfc.cpp), edge centred
+// (boundaryec.cpp)
 enum FillKind { FILL_CC = 0, FILL_FC = 1, FILL_EC = 2 };
 
 struct GhostProgram {
@@ -31,20 +33,20 @@ class GhostCompiler {
  public:
   // n = block edge with ghosts, ng = ghost layers
   GhostCompiler(int n, int ng) : n_(n), ng_(ng) {}
-  // Appends the gathers of one fill of a field with `nv` variables of one
-  // instance's tree.  `slot` maps block IDs to physical device slots.
-  void compile(const Tree &t, const std::vector<Bound> &bounds, FillKind kind, int nv,
-               const int *slot, uint8_t field, GhostProgram &out);
+  // Appends the gathers of one instance's ghost fill (any kind of field) to
+  // `out`.  `slot` maps block IDs to physical device slots.
+  void compile(const Tree &t, const std::vector<Bound> &bounds, const int *slot, GhostProgram &out);
 
  private:
   struct Desc {
     int blk;        // block ID (logical)
     int16_t pos;    // j * n + i
-    uint8_t type;   // 0 = pre-fill value of (blk,pos); GOP_AVG4 / AVGJ / AVGI of interior cells
+    uint8_t type;   // GOP_COPY: pre-fill value of (blk,pos); GOP_FINE: 2x2 patch at (blk,pos)
   };
   Desc get(int blk, int pos) const;
   void set(int blk, int pos, const Desc &d);
-  void run_sequence(const Tree &t, const std::vector<Bound> &bounds, FillKind kind, int kclass);
+  void run_sequence(const Tree &t, const std::vector<Bound> &bounds);
+  bool overwritten(int blk, int pos) const;
 
   int n_, ng_;
   int nn_ = 0;
@@ -52,6 +54,8 @@ class GhostCompiler {
   std::vector<uint32_t> stamp_;
   std::vector<Desc> cur_;
   std::vector<int> touched_;
+  std::vector<uint32_t> snap_stamp_;
+  std::vector<int> snap_row_;
 };
 
 }  // namespace amr

@@ -12,6 +12,7 @@ struct GhostLaunch;
 struct CtArgs;
 struct DtArgs;
 struct TreeOpArgs;
+struct SplitArgs;
 
 struct Method {
   int ng;      // ghost layers: 2, or 4 (WENO5)
@@ -25,8 +26,9 @@ bool method_supported(const Method &m);
 
 cudaError_t launch_stage(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s);
 // per-precision, per-flux entry points (one translation unit each)
-#define AMR_DECL_STAGE(P, F) \
-  cudaError_t launch_stage_##P##_##F(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s);
+#define AMR_DECL_STAGE(P, F)                                                                        \
+  cudaError_t launch_stage_##P##_##F(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s); \
+  cudaError_t launch_faces_##P##_##F(const Method &m, const SplitArgs &a, cudaStream_t s);
 AMR_DECL_STAGE(f64, rusa)
 AMR_DECL_STAGE(f64, hlle)
 AMR_DECL_STAGE(f64, hllc)
@@ -37,8 +39,13 @@ AMR_DECL_STAGE(f32, hllc)
 AMR_DECL_STAGE(f32, hlld)
 #undef AMR_DECL_STAGE
 
+// the split stage: primitive variables, face fluxes, residual + RK
+cudaError_t launch_prim(const Method &m, const SplitArgs &a, cudaStream_t s);
+cudaError_t launch_faces(const Method &m, const SplitArgs &a, cudaStream_t s);
+cudaError_t launch_resid(const Method &m, const SplitArgs &a, cudaStream_t s);
+
 // ghost fill: snapshot pass (if any snapshots) then the gather pass
-cudaError_t launch_ghost(int ng, const GhostLaunch &g, int nsnaps, int nops, cudaStream_t s);
+cudaError_t launch_ghost(int ng, const GhostLaunch &g, cudaStream_t s);
 cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);

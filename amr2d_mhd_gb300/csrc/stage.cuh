@@ -44,8 +44,11 @@ __device__ __forceinline__ void dev_fail(DevError *e, int code, int blk, int i, 
   }
 }
 
+// floor of the pressure recovered by the FP32 path (code units)
+constexpr double kPressureFloor = 1.0e-10;
+
 // meshblock.cpp:119-179 for one cell; the FP32 path recovers the pressure in
-// FP64 from the FP32 conserved state.
+// FP64 from the FP32 conserved state and floors it (positivity fix).
 template <typename S>
 __device__ __forceinline__ void cons2prim_cell(const S *u, S *w, double gamma);
 
@@ -67,8 +70,11 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
   const double r = u[0], mx = u[1], my = u[2], mz = u[3], E = u[4];
   const double bx = u[5], by = u[6], bz = u[7];
   const double vx = mx / r, vy = my / r, vz = mz / r;
-  const double p = (g - 1) * (E - 0.5 * r * (vx * vx + vy * vy + vz * vz)) -
-                   (g - 1) * (0.5 * (bx * bx + by * by + bz * bz));
+  double p = (g - 1) * (E - 0.5 * r * (vx * vx + vy * vy + vz * vz)) -
+             (g - 1) * (0.5 * (bx * bx + by * by + bz * bz));
+  // positivity fix of the FP32 path: the FP32 conserved state can put the
+  // recovered pressure below zero where the FP64 path stays positive
+  if (!(p > kPressureFloor)) p = kPressureFloor;
   w[0] = u[0];
   w[1] = static_cast<float>(vx);
   w[2] = static_cast<float>(vy);

@@ -5,6 +5,7 @@
 
 #include "launch.hpp"
 #include "stage.cuh"
+#include "stage_split.cuh"
 
 namespace amr {
 
@@ -33,11 +34,37 @@ cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, c
   return cudaErrorInvalidValue;
 }
 
+#ifndef AMR_FACES_MINB
+#define AMR_FACES_MINB 3
+#endif
+
+template <int NG, int RECON, int FLUX, typename S>
+cudaError_t launch_faces_t(const SplitArgs &a, cudaStream_t s) {
+  constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
+  const size_t n = static_cast<size_t>(a.ntasks) * PER;
+  if (n == 0) return cudaSuccess;
+  k_faces<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int FLUX, typename S>
+cudaError_t launch_faces_flux(const Method &m, const SplitArgs &a, cudaStream_t s) {
+  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, s);
+  if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, s);
+  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, s);
+  if (m.ng == 4 && m.recon == REC_WENO3) return launch_faces_t<4, REC_WENO3, FLUX, S>(a, s);
+  if (m.ng == 4 && m.recon == REC_WENO5) return launch_faces_t<4, REC_WENO5, FLUX, S>(a, s);
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace amr
 
 #define AMR_STAGE_DEFINE(P, F, FLUXID, T)                                                     \
   namespace amr {                                                                          \
   cudaError_t launch_stage_##P##_##F(const Method &m, const StageArgs &a, int n, cudaStream_t s) { \
     return launch_stage_flux<FLUXID, T>(m, a, n, s);                                        \
+  }                                                                                        \
+  cudaError_t launch_faces_##P##_##F(const Method &m, const SplitArgs &a, cudaStream_t s) {  \
+    return launch_faces_flux<FLUXID, T>(m, a, s);                                           \
   }                                                                                        \
   }

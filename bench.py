@@ -37,10 +37,10 @@ WORKLOAD = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, nghos
 WORKLOAD_NAME = ("MHD rotor [0,1]^2 gamma=5/3, 4 roots of 16x16, 5 levels, MUSCL-MC + HLLD + CT, RK2, "
                  "CFL 0.4, outflow, time steps from t=%.2f" % T0)
 METRIC = "cell-updates/s"
-# compulsory DRAM bytes of one fused RK-stage launch per interior leaf cell
-# (FP64): stage 1 reads U (8 words) and the face field (2) and writes Us (8);
-# stage 2 reads Us (8), U (8), face field (2) and writes U (8); mean of the two
-STAGE_BYTES_PER_CELL = {"fp64": (18 + 26) / 2 * 8, "fp32": (18 + 26) / 2 * 4 + 2 * 4}
+# compulsory DRAM bytes per interior leaf cell of one launch of the face-flux
+# kernel (the dominant kernel): it reads the primitive state (8 words) and the
+# normal face field (2 words) and writes the x and y fluxes (2 x 8 words)
+FACE_BYTES_PER_CELL = {"fp64": 26 * 8, "fp32": 24 * 4 + 2 * 8}
 STEP_BYTES_PER_CELL = {"fp64": 400, "fp32": 240}   # one full RK2 step incl. CT (compulsory)
 
 
@@ -320,10 +320,10 @@ def main():
     prof = r64["prof"]
     stage_ms_avg = prof["stage_ms"] / max(prof["stage_launches"], 1)
     cells_per_launch = prof["stage_cells"] / max(prof["stage_launches"], 1)
-    alg_bytes = cells_per_launch * STAGE_BYTES_PER_CELL["fp64"]
+    alg_bytes = cells_per_launch * FACE_BYTES_PER_CELL["fp64"]
     achieved = alg_bytes / (stage_ms_avg * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    ps = profile_summary("stage_fp64_rotor_hlld.json")
+    ps = profile_summary("faces_fp64_rotor_hlld.json")
     traffic = ps["dram_bytes_per_cell"] * cells_per_launch if ps else None
     fp64 = {}
     try:
@@ -351,7 +351,7 @@ def main():
         "e2e": {"value": e2e["cells"] / e2e["s"], "unit": "cell-updates/s",
                 "h2d_bytes_per_step": int(e2e["h2d"]), "d2h_bytes_per_step": int(e2e["d2h"])},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": traffic, "kernel": "k_stage<2,MUSCL,HLLD,double>",
+                     "peak_source": peak_kind, "traffic": traffic, "kernel": "k_faces<2,MUSCL,HLLD,double>",
                      "bytes_per_launch": alg_bytes, "launch_ms": stage_ms_avg},
         "fp64_pipe": fp64,
         "fp32": {"value": value32, "speedup_vs_fp64": value32 / value, "l1_rel_density_vs_fp64_at_t_end": l1,

@@ -150,8 +150,9 @@ int amr_upload(amr_handle *h, int32_t instance, int32_t field, const double *src
  * OpenMP wall-clock timers, main.cpp:237-369) ------------------------------ */
 typedef struct amr_profile {
   int64_t launches;        /* kernels launched since the last enable/reset */
-  int64_t stage_launches;  /* of which fused RK-stage kernels */
-  double stage_ms;         /* CUDA-event time of the stage kernels, on the launch stream */
+  int64_t stage_launches;  /* RK stages issued */
+  double stage_ms;         /* CUDA-event time, on the launch stream, of each stage's dominant
+                              kernel: the face-flux kernel (split stage) or the fused stage kernel */
   int64_t stage_cells;     /* leaf interior cells those launches updated */
   int64_t h2d_bytes;       /* host -> device bytes copied by the handle */
   int64_t d2h_bytes;

@@ -28,33 +28,35 @@ extern "C" int ghost_shim_apply(int last_active, const int *lp, const int *icoor
   for (int b = 0; b < last_active; b++) slot[b] = b;
   GhostCompiler gc(n, ng);
   GhostProgram p;
-  gc.compile(t, bounds, static_cast<FillKind>(kind), nv, slot.data(), 0, p);
+  gc.compile(t, bounds, slot.data(), p);
   std::vector<double> snap(p.snaps.size() * 8);
   for (size_t i = 0; i < p.snaps.size(); i++)
-    for (int k = p.snaps[i].k0; k < p.snaps[i].k1; k++)
+    for (int k = 0; k < nv; k++)
       snap[i * 8 + k] = field[(static_cast<size_t>(p.snaps[i].slot) * nv + k) * nn + p.snaps[i].pos];
+  // the fine-to-coarse value per kind of field (boundary.cpp:48,
+  // boundaryfc.cpp:48, boundaryec.cpp:46)
+  auto fine = [&](int k, double a00, double a01, double a10, double a11) {
+    double v = 0.;
+    if (kind == FILL_CC) { v += a00; v += a01; v += a10; v += a11; return 0.25 * v; }
+    if (kind == FILL_FC) { v += a00; v += k == 0 ? a01 : a10; return 0.5 * v; }
+    return a00;
+  };
   // gathers read only pre-fill values: evaluate all, then write
   std::vector<double> out;
   for (const GhostOp &op : p.ops)
-    for (int k = op.k0; k < op.k1; k++) {
+    for (int k = 0; k < nv; k++) {
       const double *src = field + (static_cast<size_t>(op.src_slot) * nv + k) * nn + op.src_pos;
+      const double *r = snap.data() + static_cast<size_t>(op.src_slot) * 8 + k;
       double v;
       if (op.type == GOP_COPY) v = src[0];
-      else if (op.type == GOP_SNAP) v = snap[static_cast<size_t>(op.src_slot) * 8 + k];
-      else if (op.type == GOP_AVG4) { double a = 0.; a += src[0]; a += src[n]; a += src[1]; a += src[1 + n]; v = 0.25 * a; }
-      else if (op.type == GOP_AVGJ) { double a = 0.; a += src[0]; a += src[n]; v = 0.5 * a; }
-      else if (op.type == GOP_AVGI) { double a = 0.; a += src[0]; a += src[1]; v = 0.5 * a; }
-      else {
-        const int nc = op.type == GOP_SAVG4 ? 4 : 2;
-        double a = 0.;
-        for (int c = 0; c < nc; c++) a += snap[(static_cast<size_t>(op.src_slot) + c) * 8 + k];
-        v = (op.type == GOP_SAVG4 ? 0.25 : 0.5) * a;
-      }
+      else if (op.type == GOP_SNAP) v = r[0];
+      else if (op.type == GOP_FINE) v = fine(k, src[0], src[n], src[1], src[1 + n]);
+      else v = fine(k, r[0], r[8], r[16], r[24]);
       out.push_back(v);
     }
   size_t q = 0;
   for (const GhostOp &op : p.ops)
-    for (int k = op.k0; k < op.k1; k++)
+    for (int k = 0; k < nv; k++)
       field[(static_cast<size_t>(op.dst_slot) * nv + k) * nn + op.dst_pos] = out[q++];
   *n_ops = static_cast<int>(p.ops.size());
   *n_snaps = static_cast<int>(p.snaps.size());

@@ -9,7 +9,7 @@ from parity_util import to_gpu_cfg
 
 @pytest.mark.gpu
 def test_individual_calls_reproduce_one_step(gpu):
-    """main.cpp:241-315 issued call by call equals amr_step (first step, dt = 0)."""
+    """main.cpp:241-359 issued call by call equals amr_step (first step, dt = 0)."""
     kw = to_gpu_cfg(dict(ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=3))
     a = gpu.Simulation(**kw).init()
     b = gpu.Simulation(**kw).init()
@@ -30,6 +30,8 @@ def test_individual_calls_reproduce_one_step(gpu):
     b.boundary("U")
     lam = b.cfl_dt()
     assert lam > 0
+    b.admesh()
+    assert np.array_equal(a.tree()[0], b.tree()[0])
     for f in ("U", "Bi", "Us", "Bis"):
         assert np.array_equal(a.download(f), b.download(f)), f
 
