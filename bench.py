@@ -301,7 +301,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=40, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ncu-case", type=int, default=0,
+                    help="profiling case: the rotor from its initial condition for this many steps, then exit")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="precision of --ncu-case")
     args = ap.parse_args()
+    if args.ncu_case:
+        import amr2d_mhd_gb300 as amr
+        sim = amr.Simulation(precision=args.precision, **WORKLOAD).init()
+        sim.run(args.ncu_case)
+        print(json.dumps(sim.info()))
+        return 0
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
