@@ -22,14 +22,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 FIELDS = dict(U=0, Us=1, Bi=2, Bis=3, ff=4, gg=5, EMF=6, W=7)
 STATUS = {0: "AMR_OK", -1: "AMR_E_CONFIG", -2: "AMR_E_CUDA", -3: "AMR_E_OOM", -4: "AMR_E_MAXBLOCKS",
           -5: "AMR_E_PRESSURE", -6: "AMR_E_NAN", -7: "AMR_E_DT", -8: "AMR_E_HLLC", -9: "AMR_E_STATE",
-          -10: "AMR_E_TIMEOUT", -11: "AMR_E_UNSUPPORTED", -12: "AMR_E_ARG"}
+          -10: "AMR_E_TIMEOUT", -11: "AMR_E_UNSUPPORTED", -12: "AMR_E_ARG", -13: "AMR_E_TOO_LARGE"}
 
 # every entry point declared in include/amr2d_mhd.h
 EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_abi_version", "amr_status_string",
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read"]
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static"]
 
 
 class AmrError(RuntimeError):
@@ -104,6 +104,7 @@ def load(build_if_missing: bool = True):
         "amr_upload": (ctypes.c_int, [vp, i32, i32, dp, i64]),
         "amr_profile_enable": (ctypes.c_int, [vp, i32]),
         "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
+        "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -1,8 +1,8 @@
 """Build of the sm_103a library libamr2d_mhd.so (in-tree, amr2d_mhd_gb300/_build/).
 
-Every translation unit compiles in parallel with nvcc for sm_103a only.  The
-FP64 kernels (stage_f64_*.cu, aux.cu) are compiled with -fmad=false and the
-host code with -ffp-contract=off: that path reproduces the reference's
+Every translation unit compiles in parallel with nvcc for sm_103a only.  Every
+translation unit but the FP32 stage kernels (stage_f32_*.cu) is compiled with
+-fmad=false and the host code with -ffp-contract=off: that path reproduces the reference's
 floating-point operations one by one, so nothing may be fused.
 """
 from __future__ import annotations
@@ -36,7 +36,7 @@ def _flags(src: str):
               "-I" + CSRC]
     if src.endswith(".cpp"):
         return ["-x", "cu"] + ARCH + common
-    fmad = ["-fmad=false"] if (src.startswith("stage_f64") or src == "aux.cu") else []
+    fmad = [] if src.startswith("stage_f32") else ["-fmad=false"]
     return ARCH + common + fmad
 
 

@@ -51,6 +51,7 @@ const char *amr_status_string(int s) {
     case AMR_E_TIMEOUT: return "device wait timed out";
     case AMR_E_UNSUPPORTED: return "unsupported option";
     case AMR_E_ARG: return "bad argument";
+    case AMR_E_TOO_LARGE: return "size above a fixed scratch capacity";
     default: return "unknown status";
   }
 }

@@ -39,7 +39,8 @@ typedef enum amr_status {
   AMR_E_STATE = -9,       /* call out of order (e.g. amr_step before amr_init) */
   AMR_E_TIMEOUT = -10,    /* a bounded device wait gave up */
   AMR_E_UNSUPPORTED = -11,/* ROE with a magnetic field (riemannS.cpp:39-40), block size != 16 */
-  AMR_E_ARG = -12         /* bad pointer, size or index */
+  AMR_E_ARG = -12,        /* bad pointer, size or index */
+  AMR_E_TOO_LARGE = -13   /* more blocks than a fixed-size scratch array holds */
 } amr_status;
 
 typedef enum amr_precision {
@@ -164,6 +165,25 @@ typedef struct amr_profile {
 /* on != 0 starts recording events around the stage kernels; both reset the counters */
 int amr_profile_enable(amr_handle *h, int32_t on);
 int amr_profile_read(amr_handle *h, amr_profile *out);
+
+/* ---- allocation-free CFL reduction (no counterpart in the reference) ------
+ * For callers that may not allocate device memory (inside a captured CUDA
+ * graph, in allocator-free real-time loops, or in frameworks that own every
+ * device allocation).  Same arithmetic as amr_cfl_dt (main.cpp:322-341) on the
+ * caller's device arrays:
+ *   U          [nblocks][8][16+2g][16+2g] float64 conserved state (leaf blocks)
+ *   dxdy       [nblocks][2] float64 cell sizes (dx, dy) of each block
+ *   lambda_out one float64 on the device: min(1e6, min over blocks of
+ *              min(dx,dy) / max(|rho| + c_f,x, |u| + c_f,y)); NaN if a block's
+ *              wave speed is NaN (this variant has no pressure trap)
+ * The per-block scratch is a fixed file-scope device array of 65536 doubles
+ * (512 KiB on every GPU that loads the library, kept until exit); nblocks
+ * above 65536 returns AMR_E_TOO_LARGE.  The first call on a device looks up
+ * that array's address; make it before any stream capture.  Calls share the
+ * array, so calls that overlap on the GPU (different streams) race.  Work is
+ * enqueued on `cuda_stream`; the call does not synchronise. */
+int amr_cfl_dt_static(const double *U, int32_t nblocks, int32_t nghosts, const double *dxdy, double gamma,
+                      double *lambda_out, void *cuda_stream);
 
 #ifdef __cplusplus
 }
