@@ -30,7 +30,17 @@ struct LeafTask {
   int slot;
   int inst;
   double dx, dy;
+  // 1/dx and 1/dy when dx, dy are powers of two (then x/dx == x*(1/dx)
+  // exactly, and the residual multiplies instead of dividing); 0 otherwise
+  double inv_dx, inv_dy;
 };
+
+// 1/v if v is a power of two (exact reciprocal), else 0
+inline double exact_reciprocal(double v) {
+  int e = 0;
+  const double m = __builtin_frexp(v, &e);
+  return (m == 0.5) ? 1.0 / v : 0.0;
+}
 
 // Per-instance scalars read by the kernels (kept in device memory so that a
 // captured CUDA graph sees the values of the current step).

@@ -115,9 +115,9 @@ cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int n, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_dt_crit(const Method &m, const DtArgs &a, int n, cudaStream_t s) {
+cudaError_t launch_dt_cell(const Method &m, const DtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  AMR_DISPATCH_NG_S(m, k_dt_crit, n, 256, 0, s, a);
+  AMR_DISPATCH_NG_S(m, k_dt_cell, n, 256, 0, s, a);
   return cudaGetLastError();
 }
 

@@ -167,18 +167,10 @@ __global__ void k_ct_cell(CtArgs a) {
 }
 
 // --------------------------------------------- dt (main.cpp:322-343) and
-// refinement criterion (criteria.cpp:6-44) of every leaf, one CTA per leaf.
-// Computed in FP64 for both storage types.
-struct DtArgs {
-  const LeafTask *tasks;
-  const InstParams *inst;
-  const void *U;
-  double *lambda;   // per task: min(dx,dy) / max(lambda1, lambda2)
-  double *grad;     // per task: max relative jump
-  DevError *err;
-  int want_grad;
-};
-
+// refinement criterion (criteria.cpp:6-44) of every leaf: one CTA per leaf,
+// one thread per interior cell, reading the primitive state that k_prim wrote
+// for U (FP64 for the FP64 path; the FP32 path computes the cell values in
+// FP32 and reduces them in FP64).
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -188,64 +180,68 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+struct DtArgs {
+  const LeafTask *tasks;
+  const InstParams *inst;
+  const void *W;    // primitive state of U
+  double *lambda;   // per task: max over cells of max(|rho| + c_f,x, |u| + c_f,y)
+  double *grad;     // per task: max relative jump
+  int want_grad;
+};
+
 template <int NG, typename S>
-__global__ void __launch_bounds__(256) k_dt_crit(DtArgs a) {
+__global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
   using G = Geo<NG>;
+  using T = S;
   constexpr int N = G::N, NN = G::NN;
-  __shared__ double sW[5][NN];   // rho, u, p, Bx, By (the criterion's variables + u)
+  static_assert(NI * NI == 256, "one thread per interior cell");
   __shared__ double red[2][8];
   const LeafTask t = a.tasks[blockIdx.x];
-  const double g = a.inst[t.inst].gamma;
-  const S *U = static_cast<const S *>(a.U) + static_cast<size_t>(t.slot) * 8 * NN;
-  double l1 = 0., l2 = 0.;
-  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
-    double u[8], w[8];
+  const T g = static_cast<T>(a.inst[t.inst].gamma);
+  const int i = NG + threadIdx.x % NI, j = NG + threadIdx.x / NI, c = j * N + i;
+  const S *W = static_cast<const S *>(a.W) + static_cast<size_t>(t.slot) * 8 * NN;
+  T w[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) u[k] = static_cast<double>(U[k * NN + c]);
-    cons2prim_cell<double>(u, w, g);
-    if (sizeof(S) == sizeof(float) && !(w[4] > kPressureFloor)) w[4] = kPressureFloor;  // FP32 path
-    sW[0][c] = w[0]; sW[1][c] = w[1]; sW[2][c] = w[4]; sW[3][c] = w[5]; sW[4][c] = w[6];
-    const int i = c % N, j = c / N;
-    if (w[4] <= 0 && i > G::LO && i < G::HI + 1 && j > G::LO && j < G::HI + 1)
-      dev_fail(a.err, DERR_PRESSURE, t.slot, i, j, w[4]);
-    if (i >= NG && i <= G::HI && j >= NG && j <= G::HI) {
-      // note lambda1 takes |rho| (W[..][0], main.cpp:335), lambda2 |u| (:337)
-      l1 = smax(l1, fabs(w[0]) + fast_speed<double>(w, g, 5));
-      l2 = smax(l2, fabs(w[1]) + fast_speed<double>(w, g, 6));
-    }
+  for (int k = 0; k < 8; k++) w[k] = W[k * NN + c];
+  // wavespeeds (misc.cpp:71-79) for norm 5 and 6; ca and a are the same
+  // values in both calls.  lambda1 takes |rho| (main.cpp:335), lambda2 |u|.
+  const T ca = sqrt((w[5] * w[5] + w[6] * w[6] + w[7] * w[7]) / w[0]);
+  const T as = sqrt(g * w[4] / w[0]);
+  T cf[2];
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const T can = sqrt((w[5 + q] * w[5 + q]) / w[0]);
+    const T i0 = (ca * ca) + (as * as), i1 = (ca * ca) - (as * as);
+    cf[q] = sqrt(T(0.5) * (i0 + sqrt(i1 * i1 + T(4.) * (as * as) * ((ca * ca) - (can * can)))));
   }
-  __syncthreads();
+  double lam = smax(static_cast<double>(fabs(w[0]) + cf[0]), static_cast<double>(fabs(w[1]) + cf[1]));
   double gr = 0.;
   if (a.want_grad) {
-    for (int c = threadIdx.x; c < NN; c += blockDim.x) {
-      const int i = c % N, j = c / N;
-      if (i < NG || i > G::HI || j < NG || j > G::HI) continue;
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int v = q == 0 ? 2 : (q == 1 ? 0 : q + 1);   // p, rho, Bx, By
-        const double c0 = sW[v][c];
-        const double dm = mmax(EPS, fabs(c0));
-        double d1 = fabs(sW[v][c + 1] - c0);
-        double d2 = mmax(d1, fabs(sW[v][c - 1] - c0));
-        d1 = mmax(d2, fabs(sW[v][c + N] - c0));
-        d2 = mmax(d1, fabs(sW[v][c - N] - c0));
-        gr = mmax(gr, d2 / dm);
-      }
+    for (int q = 0; q < 4; q++) {
+      const int v = q == 0 ? 4 : (q == 1 ? 0 : q + 3);   // p, rho, Bx, By
+      const S *x = W + v * NN + c;
+      const T c0 = x[0];
+      const T dm = mmax(static_cast<T>(EPS), fabs(c0));
+      T d1 = fabs(x[1] - c0);
+      T d2 = mmax(d1, fabs(x[-1] - c0));
+      d1 = mmax(d2, fabs(x[N] - c0));
+      d2 = mmax(d1, fabs(x[-N] - c0));
+      gr = mmax(gr, static_cast<double>(d2 / dm));
     }
   }
-  double m = smax(l1, l2);
-  m = warp_max(m);
+  lam = warp_max(lam);
   gr = warp_max(gr);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) { red[0][wid] = m; red[1][wid] = gr; }
+  if (lane == 0) { red[0][wid] = lam; red[1][wid] = gr; }
   __syncthreads();
   if (threadIdx.x == 0) {
     double mm = red[0][0], gg = red[1][0];
-    for (int q = 1; q < static_cast<int>(blockDim.x >> 5); q++) {
+    for (int q = 1; q < 8; q++) {
       mm = mm < red[0][q] ? red[0][q] : mm;
       gg = gg < red[1][q] ? red[1][q] : gg;
     }
-    a.lambda[blockIdx.x] = smin(t.dx, t.dy) / mm;
+    a.lambda[blockIdx.x] = mm;
     a.grad[blockIdx.x] = gg;
   }
 }

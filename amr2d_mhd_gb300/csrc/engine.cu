@@ -77,6 +77,9 @@ Engine::~Engine() {
   d_snaps_.release();
   for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_}) b->release();
   if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+  if (exec_) cudaGraphExecDestroy(exec_);
+  if (cap_stream_) cudaStreamDestroy(cap_stream_);
+  for (cudaEvent_t e : ev_) cudaEventDestroy(e);
   delete gc_;
 }
 
@@ -132,6 +135,7 @@ int Engine::create(const amr_config *cfgs, int n) {
   if (!method_supported(m_)) return fail(AMR_E_UNSUPPORTED, "method not compiled");
   f32_ = m_.f32 != 0;
   if (const char *k = std::getenv("AMR2D_STAGE_KERNEL")) split_ = std::strcmp(k, "fused") != 0;
+  if (const char *g = std::getenv("AMR2D_GRAPHS")) graph_on_ = std::strcmp(g, "0") != 0;
   ng_ = m_.ng;
   n_ = NI + 2 * ng_;
   nn_ = n_ * n_;
@@ -140,6 +144,7 @@ int Engine::create(const amr_config *cfgs, int n) {
   if (e != cudaSuccess || ndev == 0) return fail(AMR_E_CUDA, "no CUDA device");
   CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
   own_stream_ = true;
+  CK(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking), "stream");
   gc_ = new GhostCompiler(n_, ng_);
   inst_.reserve(n);
   for (int q = 0; q < n; q++) {
@@ -239,6 +244,7 @@ int Engine::ensure_slots(int needed) {
     *dbl[q] = np;
   }
   cap_slots_ = cap;
+  gen_++;
   return AMR_OK;
 }
 
@@ -254,6 +260,7 @@ int Engine::rebuild() {
   for (int a : active_)
     if (built_version_[a] != inst_[a].tree.version) need = true;
   if (!need) return AMR_OK;
+  gen_++;
   const auto t0 = std::chrono::steady_clock::now();
   tasks_.clear();
   task_blk_.clear();
@@ -265,7 +272,8 @@ int Engine::rebuild() {
     for (int nb = 0; nb < in.tree.lastActive; nb++) {
       if (!in.tree.leafs[nb]) continue;
       const int lev = in.tree.lp[nb][0];
-      tasks_.push_back(LeafTask{in.slot[nb], a, in.dx[lev], in.dy[lev]});
+      tasks_.push_back(LeafTask{in.slot[nb], a, in.dx[lev], in.dy[lev], exact_reciprocal(in.dx[lev]),
+                                exact_reciprocal(in.dy[lev])});
       task_blk_.push_back(nb);
     }
     in.task_end = static_cast<int>(tasks_.size());
@@ -306,7 +314,7 @@ int Engine::rebuild() {
   return AMR_OK;
 }
 
-int Engine::upload_params() {
+void Engine::fill_params_host() {
   InstParams *p = h_params_.as<InstParams>();
   for (size_t q = 0; q < inst_.size(); q++) {
     p[q].gamma = inst_[q].gamma;
@@ -314,6 +322,11 @@ int Engine::upload_params() {
     p[q].limiter = inst_[q].limiter;
     p[q].pad = 0;
   }
+}
+
+int Engine::upload_params() {
+  fill_params_host();
+  InstParams *p = h_params_.as<InstParams>();
   CK(cudaMemcpyAsync(d_params_.p, p, sizeof(InstParams) * inst_.size(), cudaMemcpyHostToDevice, stream_), "h2d");
   prof_.h2d_bytes += sizeof(InstParams) * inst_.size();
   return AMR_OK;
@@ -424,17 +437,26 @@ int Engine::ct2d(int step) {
   return AMR_OK;
 }
 
+// primitive state of U (with the pressure / NaN traps of U2W("main")), then
+// the per-leaf wave-speed maximum and refinement criterion
 int Engine::dt_crit(bool want_grad) {
+  SplitArgs p{};
+  p.tasks = d_tasks_.as<LeafTask>();
+  p.inst = d_params_.as<InstParams>();
+  p.qin = U_;
+  p.W = W_;
+  p.err = d_err_.as<DevError>();
+  p.ntasks = static_cast<int>(tasks_.size());
+  CK(launch_prim(m_, p, stream_), "prim kernel");
   DtArgs a{};
   a.tasks = d_tasks_.as<LeafTask>();
   a.inst = d_params_.as<InstParams>();
-  a.U = U_;
+  a.W = W_;
   a.lambda = d_lambda_.as<double>();
   a.grad = d_grad_.as<double>();
-  a.err = d_err_.as<DevError>();
   a.want_grad = want_grad ? 1 : 0;
-  CK(launch_dt_crit(m_, a, static_cast<int>(tasks_.size()), stream_), "dt kernel");
-  prof_.launches += 1;
+  CK(launch_dt_cell(m_, a, static_cast<int>(tasks_.size()), stream_), "dt kernel");
+  prof_.launches += 2;
   return AMR_OK;
 }
 
@@ -450,6 +472,72 @@ int Engine::enqueue_stage_sequence() {
   if ((rc = fill({{FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}}))) return rc;
   if ((rc = ct2d(2))) return rc;
   if ((rc = fill({{FILL_CC, AMR_FIELD_U}}))) return rc;
+  return AMR_OK;
+}
+
+int Engine::enqueue_step() {
+  if (int rc = upload_params()) return rc;
+  if (int rc = enqueue_stage_sequence()) return rc;
+  bool any_amr = false;
+  for (int a : active_) any_amr |= inst_[a].cfg.maxlevs > 1;
+  if (int rc = dt_crit(any_amr)) return rc;
+  const size_t nt = tasks_.size();
+  CK(cudaMemcpyAsync(h_lambda_.p, d_lambda_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
+  CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
+  return AMR_OK;
+}
+
+int Engine::launch_step() {
+  const int64_t launches0 = prof_.launches;
+  if (!graph_on_) return enqueue_step();
+  if (!exec_ || captured_gen_ != gen_) {
+    // capture on a private stream; the graph is then launched on stream_
+    cudaStream_t user = stream_;
+    stream_ = cap_stream_;
+    const int ev0 = ev_used_;
+    // events are created outside the capture
+    if (prof_on_)
+      while (ev_.size() < static_cast<size_t>(ev0 + 4)) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e), "event");
+        ev_.push_back(e);
+      }
+    cudaError_t e = cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) { stream_ = user; return cuda_fail(e, "graph capture"); }
+    int rc = enqueue_step();
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(cap_stream_, &g);
+    stream_ = user;
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+    graph_ev_used_ = ev_used_ - ev0;
+    ev_used_ = ev0;
+    bool updated = false;
+    if (exec_) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(exec_, g, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+      }
+    }
+    if (!updated) {
+      e = cudaGraphInstantiate(&exec_, g, 0);
+      if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(e, "graph instantiate"); }
+    }
+    cudaGraphDestroy(g);
+    captured_gen_ = gen_;
+    graph_launches_ = prof_.launches - launches0;
+  } else {
+    fill_params_host();  // the graph's first node copies these to the device
+    prof_.launches += graph_launches_;
+    prof_.stage_launches += 2;
+    stage_cells_pending_ += 2 * static_cast<int64_t>(tasks_.size()) * NI * NI;
+    prof_.h2d_bytes += sizeof(InstParams) * inst_.size();
+  }
+  ev_used_ += graph_ev_used_;
+  CK(cudaGraphLaunch(exec_, stream_), "graph launch");
   return AMR_OK;
 }
 
@@ -486,6 +574,7 @@ int Engine::profile_enable(bool on) {
   prof_ = amr_profile{};
   ev_used_ = 0;
   stage_cells_pending_ = 0;
+  if (prof_on_ != on) gen_++;
   prof_on_ = on;
   return AMR_OK;
 }

@@ -87,7 +87,10 @@ class Engine {
   int assign_slots(Instance &in);
   int rebuild();               // leaf tasks + ghost programs for the active set
   int upload_params();
+  void fill_params_host();
   int enqueue_stage_sequence();
+  int enqueue_step();              // params upload, stage sequence, dt kernels, result copies
+  int launch_step();               // enqueue_step directly or as a replayed CUDA graph
   int fill(std::initializer_list<std::pair<FillKind, int>> what);
   int stage(int step);
   int ct2d(int step);
@@ -126,6 +129,14 @@ class Engine {
   DevBuf d_treeops_, d_stage_, d_slots_;
   HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_stage_;
   GhostCompiler *gc_ = nullptr;
+
+  // CUDA graph of one step, re-captured when gen_ moves (tree, pool, profiling)
+  bool graph_on_ = true;
+  cudaStream_t cap_stream_ = nullptr;
+  cudaGraphExec_t exec_ = nullptr;
+  uint64_t gen_ = 1, captured_gen_ = 0;
+  int graph_ev_used_ = 0;
+  int64_t graph_launches_ = 0;
 
   // measurement
   bool prof_on_ = false;

@@ -133,16 +133,17 @@ int Engine::init() {
 
 int Engine::finish_step() {
   const size_t nt = tasks_.size();
-  CK(cudaMemcpyAsync(h_lambda_.p, d_lambda_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
-  CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
   prof_.d2h_bytes += static_cast<int64_t>(2 * sizeof(double) * nt);
   prof_.steps += 1;
   if (int rc = check_device_error()) return rc;
   const double *hl = h_lambda_.as<double>();
   for (int a : active_) {
     Instance &in = inst_[a];
-    double lambda = 1.E6;  // main.cpp:322
-    for (int t = in.task_begin; t < in.task_end; t++) lambda = hl[t] < lambda ? hl[t] : lambda;
+    double lambda = 1.E6;  // main.cpp:322, 341
+    for (int t = in.task_begin; t < in.task_end; t++) {
+      const double v = (tasks_[t].dx < tasks_[t].dy ? tasks_[t].dx : tasks_[t].dy) / hl[t];
+      lambda = v < lambda ? v : lambda;
+    }
     in.t = in.t + in.dtn;  // main.cpp:344-347
     in.dt = in.dtn;
     in.count = in.count + 1;
@@ -165,11 +166,7 @@ int Engine::step() {
   }
   if (active_.empty()) return AMR_OK;
   if (int rc = rebuild()) return rc;
-  if (int rc = upload_params()) return rc;
-  if (int rc = enqueue_stage_sequence()) return rc;
-  bool any_amr = false;
-  for (int a : active_) any_amr |= inst_[a].cfg.maxlevs > 1;
-  if (int rc = dt_crit(any_amr)) return rc;
+  if (int rc = launch_step()) return rc;
   return finish_step();
 }
 
@@ -251,7 +248,10 @@ int Engine::api_cfl_dt(double *lambda_min) {
   CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
   if (int rc = check_device_error()) return rc;
   double lambda = 1.E6;
-  for (size_t t = 0; t < nt; t++) lambda = h_lambda_.as<double>()[t] < lambda ? h_lambda_.as<double>()[t] : lambda;
+  for (size_t t = 0; t < nt; t++) {
+    const double v = (tasks_[t].dx < tasks_[t].dy ? tasks_[t].dx : tasks_[t].dy) / h_lambda_.as<double>()[t];
+    lambda = v < lambda ? v : lambda;
+  }
   *lambda_min = lambda;
   return AMR_OK;
 }

@@ -49,7 +49,8 @@ cudaError_t launch_ghost(int ng, const GhostLaunch &g, cudaStream_t s);
 cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
-cudaError_t launch_dt_crit(const Method &m, const DtArgs &a, int ntasks, cudaStream_t s);
+// per-leaf max wave speed and refinement criterion from the primitive state
+cudaError_t launch_dt_cell(const Method &m, const DtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int nops, cudaStream_t s);
 cudaError_t launch_coarsen(const Method &m, const TreeOpArgs &a, int nops, cudaStream_t s);
 

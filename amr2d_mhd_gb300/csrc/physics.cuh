@@ -63,6 +63,21 @@ __device__ __forceinline__ T slope_limiter(int lim, T r, T eta) {
   }
 }
 
+// The limiter ratio num/den (celledges.cpp:38,41), skipping the division when
+// the limiter's value does not need it: num = +-0 gives r = +-0 exactly (sign
+// rule of IEEE division), and for minmod, MC, Superbee and Koren every
+// negative r gives phi = +0, so any negative stand-in does; "1st" ignores r.
+template <typename T>
+__device__ __forceinline__ T limiter_ratio(int lim, T num, T den) {
+  if (lim == LIM_1ST) return T(0);
+  if (den != T(0) && isfinite(den) && isfinite(num)) {
+    const bool neg = signbit(num) != signbit(den);
+    if (num == T(0)) return neg ? T(-0.0) : T(0.0);
+    if (neg && (lim == LIM_MINMOD || lim == LIM_MC || lim == LIM_SUPERBEE || lim == LIM_KOREN)) return T(-1);
+  }
+  return num / den;
+}
+
 // celledges.cpp:38-43 for one variable of one face.  dA = W[i]-W[i-1],
 // dB = W[i+1]-W[i], dC = W[i+2]-W[i+1] around the face i+1/2; returns the
 // left state wxL[i] and right state wxR[i+1].  inv2 = 1/(dx*dx) for Cada3rd.
@@ -75,10 +90,10 @@ __device__ __forceinline__ void muscl_face(int lim, T wi, T wip, T dA, T dB, T d
     etaL = (dB * dB + dA * dA) / ((T(1) * h) * (T(1) * h));
     etaR = (dC * dC + dB * dB) / ((T(1) * h) * (T(1) * h));
   }
-  T r = dB / (dA + E);
+  T r = limiter_ratio<T>(lim, dB, dA + E);
   T phi = slope_limiter<T>(lim, r, etaL);
   left = wi + T(0.5) * phi * dA;
-  r = dB / (dC + E);
+  r = limiter_ratio<T>(lim, dB, dC + E);
   phi = slope_limiter<T>(lim, r, etaR);
   right = wip - T(0.5) * phi * dC;
 }

@@ -139,7 +139,10 @@ __global__ void __launch_bounds__(256) k_resid(SplitArgs a) {
   if (i >= LO && i <= HI && j >= LO && j <= HI) {
     const S *ff = static_cast<const S *>(a.ff) + idx;
     const S *gg = static_cast<const S *>(a.gg) + idx;
-    res = (ff[1] - ff[0]) / static_cast<T>(task.dx) + (gg[N] - gg[0]) / static_cast<T>(task.dy);
+    if (task.inv_dx != 0.0 && task.inv_dy != 0.0)  // power-of-two cells: exact reciprocal
+      res = (ff[1] - ff[0]) * static_cast<T>(task.inv_dx) + (gg[N] - gg[0]) * static_cast<T>(task.inv_dy);
+    else
+      res = (ff[1] - ff[0]) / static_cast<T>(task.dx) + (gg[N] - gg[0]) / static_cast<T>(task.dy);
   }
   const T dt = static_cast<T>(a.inst[task.inst].dt);
   const T q = static_cast<const S *>(a.qin)[idx];
