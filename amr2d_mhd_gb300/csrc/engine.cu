@@ -364,12 +364,13 @@ int Engine::stage(int step) {
       CK(cudaEventCreate(&e), "event");
       ev_.push_back(e);
     }
-    CK(cudaEventRecord(ev_[ev_used_], stream_), "event");
+    // inside a graph capture the events must be external nodes to be timed
+    CK(cudaEventRecordWithFlags(ev_[ev_used_], stream_, capturing_ ? cudaEventRecordExternal : 0), "event");
     return AMR_OK;
   };
   auto ev_end = [&]() -> int {
     if (!prof_on_) return AMR_OK;
-    CK(cudaEventRecord(ev_[ev_used_ + 1], stream_), "event");
+    CK(cudaEventRecordWithFlags(ev_[ev_used_ + 1], stream_, capturing_ ? cudaEventRecordExternal : 0), "event");
     ev_used_ += 2;
     return AMR_OK;
   };
@@ -504,7 +505,9 @@ int Engine::launch_step() {
       }
     cudaError_t e = cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) { stream_ = user; return cuda_fail(e, "graph capture"); }
+    capturing_ = true;
     int rc = enqueue_step();
+    capturing_ = false;
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(cap_stream_, &g);
     stream_ = user;
@@ -563,6 +566,7 @@ void Engine::prof_collect() {
   for (int q = 0; q + 1 < ev_used_; q += 2) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ev_[q], ev_[q + 1]) == cudaSuccess) prof_.stage_ms += ms;
+    else cudaGetLastError();  // a failed timing query must not surface in a later launch check
   }
   ev_used_ = 0;
   prof_.stage_cells += stage_cells_pending_;

@@ -137,6 +137,7 @@ class Engine {
   uint64_t gen_ = 1, captured_gen_ = 0;
   int graph_ev_used_ = 0;
   int64_t graph_launches_ = 0;
+  bool capturing_ = false;
 
   // measurement
   bool prof_on_ = false;

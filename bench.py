@@ -327,7 +327,7 @@ def main():
     l1 = float(np.abs(a - b).sum() / np.abs(b).sum())
     # roofline of the dominant kernel (fused RK stage, FP64)
     prof = r64["prof"]
-    stage_ms_avg = prof["stage_ms"] / max(prof["stage_launches"], 1)
+    stage_ms_avg = max(prof["stage_ms"] / max(prof["stage_launches"], 1), 1e-9)
     cells_per_launch = prof["stage_cells"] / max(prof["stage_launches"], 1)
     alg_bytes = cells_per_launch * FACE_BYTES_PER_CELL["fp64"]
     achieved = alg_bytes / (stage_ms_avg * 1e-3) / 1e9
