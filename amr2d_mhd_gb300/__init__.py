@@ -25,7 +25,7 @@ STATUS = {0: "AMR_OK", -1: "AMR_E_CONFIG", -2: "AMR_E_CUDA", -3: "AMR_E_OOM", -4
           -10: "AMR_E_TIMEOUT", -11: "AMR_E_UNSUPPORTED", -12: "AMR_E_ARG", -13: "AMR_E_TOO_LARGE"}
 
 # every entry point declared in include/amr2d_mhd.h
-EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_abi_version", "amr_status_string",
+EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "amr_config_kh", "amr_abi_version", "amr_status_string",
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
@@ -46,7 +46,7 @@ class Config(ctypes.Structure):
                 ("nroots_x", ctypes.c_int32), ("nroots_y", ctypes.c_int32), ("periodic", ctypes.c_int32),
                 ("geometry", ctypes.c_int32), ("gamma", ctypes.c_double), ("t_end", ctypes.c_double),
                 ("ic_param", ctypes.c_double * 24), ("precision", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 7)]
+                ("reserved0", ctypes.c_int32), ("dt_fixed", ctypes.c_double), ("reserved", ctypes.c_int32 * 4)]
 
 
 class Info(ctypes.Structure):
@@ -82,6 +82,8 @@ def load(build_if_missing: bool = True):
     sig = {
         "amr_config_default": (None, [ctypes.POINTER(Config)]),
         "amr_config_from_input": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Config)]),
+        "amr_config_blast": (ctypes.c_int, [ctypes.c_uint64, i32, ctypes.POINTER(Config)]),
+        "amr_config_kh": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(Config)]),
         "amr_abi_version": (ctypes.c_int, []),
         "amr_status_string": (ctypes.c_char_p, [ctypes.c_int]),
         "amr_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(vp)]),
@@ -138,6 +140,26 @@ def make_config(ic="rotor", limiter="MC", flux="RUSA", cfl=0.5, maxlevs=5, nghos
     return c
 
 
+def blast_config(seed, index, precision="fp64") -> Config:
+    """Instance `index` of the seeded cylindrical blast batch (amr_config_blast)."""
+    c = Config()
+    rc = load().amr_config_blast(seed, index, ctypes.byref(c))
+    if rc:
+        raise AmrError(rc, "amr_config_blast")
+    c.precision = {"fp64": 0, "fp32": 1}[precision]
+    return c
+
+
+def kh_config(seed, precision="fp64") -> Config:
+    """The frozen-mesh Kelvin-Helmholtz problem of amr_config_kh."""
+    c = Config()
+    rc = load().amr_config_kh(seed, ctypes.byref(c))
+    if rc:
+        raise AmrError(rc, "amr_config_kh")
+    c.precision = {"fp64": 0, "fp32": 1}[precision]
+    return c
+
+
 class Simulation:
     """One handle: an AMR problem (or a batch of them) resident on the GPU.
 
@@ -159,6 +181,7 @@ class Simulation:
             raise AmrError(rc, "amr_create failed")
         self.h = h
         self.n = len(configs)
+        self.configs = [Config.from_buffer_copy(c) for c in configs]
 
     def close(self):
         if getattr(self, "h", None):
@@ -243,6 +266,26 @@ class Simulation:
         p = Profile()
         self._ck(load().amr_profile_read(self.h, ctypes.byref(p)))
         return {k: getattr(p, k) for k, _ in Profile._fields_}
+
+    def uniform(self, var=0, level=None, instance=0, field="U"):
+        """Variable `var` of the leaf blocks painted piecewise constant onto
+        the uniform grid of `level` (default: the finest level); [i][j]."""
+        c = self.configs[instance]
+        ng = c.nghosts
+        lp, ic, lf = self.tree(instance)
+        if level is None:
+            level = c.maxlevs - 1
+        a = self.download(field, instance)
+        nx, ny = c.nx * c.nroots_x * 2 ** level, c.ny * c.nroots_y * 2 ** level
+        out = np.zeros((nx, ny))
+        for b in np.nonzero(lf)[0]:
+            r = 2 ** (level - lp[b, 0])
+            if r < 1:
+                raise ValueError("level is coarser than a leaf")
+            v = a[b, var, ng:-ng, ng:-ng].T
+            x0, y0 = ic[b, 0] * r, ic[b, 1] * r
+            out[x0:x0 + c.nx * r, y0:y0 + c.ny * r] = np.kron(v, np.ones((r, r)))
+        return out
 
     def state(self, instance=0):
         """Dict in the form the oracle's state() returns."""

@@ -64,7 +64,7 @@ struct InstParams {
 //             edge  s(i,j)                                       boundaryec.cpp:46
 //   SFINE:  the same from four saved pre-fill values (snapshot rows src_slot..
 //           src_slot+3 in the order (i,j) (i,j+1) (i+1,j) (i+1,j+1))
-enum GhostOpType : uint8_t { GOP_COPY = 0, GOP_SNAP = 1, GOP_FINE = 2, GOP_SFINE = 3 };
+enum GhostOpType : uint8_t { GOP_COPY = 0, GOP_SNAP = 1, GOP_FINE = 2, GOP_SFINE = 3, GOP_NOP = 4 };
 struct GhostOp {
   int dst_slot;
   int src_slot;     // physical slot, or first snapshot row for SNAP / SFINE

@@ -40,6 +40,7 @@ __global__ void k_ghost_snap(GhostLaunch g) {
   if (t >= g.nsnaps * g.nseg) return;
   const int q = t / g.nsnaps, r = t % g.nsnaps;
   const GhostSeg &s = g.seg[q];
+  if (g.snaps[r].slot < 0) return;  // padding of an instance's range
   double *row = g.snapbuf + (static_cast<size_t>(q) * g.nsnaps + r) * 8;
   if (s.f32) ghost_snap_one<N, float>(s, g.snaps[r], row);
   else ghost_snap_one<N, double>(s, g.snaps[r], row);
@@ -65,6 +66,7 @@ __device__ __forceinline__ F fine_value(int kind, int k, F a00, F a01, F a10, F 
 template <int N, typename F>
 __device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, const double *snap) {
   constexpr int NN = N * N;
+  if (op.type == GOP_NOP) return;  // padding of an instance's range
   F *fld = static_cast<F *>(s.field);
   F *dst = fld + static_cast<size_t>(op.dst_slot) * s.nv * NN + op.dst_pos;
   if (op.type == GOP_COPY || op.type == GOP_FINE) {

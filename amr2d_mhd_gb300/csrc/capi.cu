@@ -95,6 +95,40 @@ int amr_config_from_input(const char *path, amr_config *c) {
   return AMR_OK;
 }
 
+int amr_config_blast(uint64_t seed, int32_t index, amr_config *c) {
+  if (!c || index < 0) return AMR_E_ARG;
+  amr_config_default(c);
+  copy_name(c->ic, "blast");
+  copy_name(c->limiter, "MC");
+  copy_name(c->flux, "HLLE");
+  c->cfl = 0.2;
+  c->geometry = 1;
+  c->gamma = 1.4;
+  c->t_end = 0.1;
+  int maxlevs = 3;
+  amr::blast_draw(seed, index, c->ic_param, maxlevs);
+  c->maxlevs = maxlevs;
+  return AMR_OK;
+}
+
+int amr_config_kh(uint64_t seed, amr_config *c) {
+  if (!c) return AMR_E_ARG;
+  amr_config_default(c);
+  copy_name(c->ic, "KH");
+  copy_name(c->limiter, "MC");
+  copy_name(c->flux, "RUSA");
+  c->maxlevs = 1;
+  c->nroots_x = 16;
+  c->nroots_y = 16;
+  c->periodic = 1;
+  c->geometry = 1;
+  c->gamma = 5.0 / 3.0;
+  c->dt_fixed = 2e-4;
+  c->t_end = 1.0;
+  amr::kh_draw(seed, c->ic_param);
+  return AMR_OK;
+}
+
 int amr_create_batch(const amr_config *cfgs, int32_t n, amr_handle **out) {
   if (!cfgs || !out || n <= 0) return AMR_E_ARG;
   *out = nullptr;

@@ -4,9 +4,12 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
-#include <initializer_list>
+#include <atomic>
 #include <chrono>
+#include <initializer_list>
+#include <mutex>
 #include <string>
+#include <thread>
 
 #include "aux_kernels.cuh"
 #include "stage_split.cuh"
@@ -75,12 +78,13 @@ Engine::~Engine() {
     b->release();
   d_ops_.release();
   d_snaps_.release();
-  for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_}) b->release();
+  for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_, &h_ops_, &h_snaps_, &h_tasks_})
+    b->release();
   if (own_stream_ && stream_) cudaStreamDestroy(stream_);
   if (exec_) cudaGraphExecDestroy(exec_);
   if (cap_stream_) cudaStreamDestroy(cap_stream_);
   for (cudaEvent_t e : ev_) cudaEventDestroy(e);
-  delete gc_;
+  for (GhostCompiler *g : gcs_) delete g;
 }
 
 int Engine::fail(int code, const std::string &msg) {
@@ -145,7 +149,6 @@ int Engine::create(const amr_config *cfgs, int n) {
   CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
   own_stream_ = true;
   CK(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking), "stream");
-  gc_ = new GhostCompiler(n_, ng_);
   inst_.reserve(n);
   for (int q = 0; q < n; q++) {
     const amr_config &c = cfgs[q];
@@ -255,6 +258,179 @@ int Engine::assign_slots(Instance &in) {
 }
 
 // ------------------------------------------------------------- programs
+// Recompiles the ghost fill of every active instance whose tree changed since
+// its last compile, spread over host threads (one compiler each).
+int Engine::compile_programs() {
+  std::vector<int> todo;
+  size_t blocks = 0;
+  for (int a : active_)
+    if (inst_[a].prog_version != inst_[a].tree.version) {
+      todo.push_back(a);
+      blocks += static_cast<size_t>(inst_[a].tree.lastActive);
+    }
+  if (todo.empty()) return AMR_OK;
+  unsigned hw = std::thread::hardware_concurrency();
+  size_t nth = hw ? hw : 1;
+  if (nth > 32) nth = 32;
+  if (nth > todo.size()) nth = todo.size();
+  if (blocks < 2048) nth = 1;  // thread start-up would cost more than the compile
+  while (gcs_.size() < nth) gcs_.push_back(new GhostCompiler(n_, ng_));
+  std::atomic<size_t> next{0};
+  std::mutex mu;
+  std::string err;
+  auto work = [&](size_t w) {
+    std::vector<Bound> bounds;
+    for (;;) {
+      const size_t q = next.fetch_add(1);
+      if (q >= todo.size()) break;
+      Instance &in = inst_[todo[q]];
+      try {
+        in.tree.locate_bounds(bounds);
+        in.prog.clear();
+        gcs_[w]->compile(in.tree, bounds, in.slot.data(), in.prog);
+        in.prog_version = in.tree.version;
+        in.prog_dirty = true;
+      } catch (const std::exception &ex) {
+        std::lock_guard<std::mutex> g(mu);
+        if (err.empty()) err = ex.what();
+      }
+    }
+  };
+  if (nth == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (size_t w = 1; w < nth; w++) th.emplace_back(work, w);
+    work(0);
+    for (auto &t : th) t.join();
+  }
+  if (!err.empty()) return fail(AMR_E_STATE, err);
+  return AMR_OK;
+}
+
+namespace {
+// grow a device buffer keeping its first `keep` bytes
+cudaError_t grow_keep(DevBuf &b, size_t n, size_t keep, cudaStream_t s) {
+  if (n <= b.bytes && b.p) return cudaSuccess;
+  DevBuf nb;
+  cudaError_t e = nb.ensure(n + n / 2);
+  if (e != cudaSuccess) return e;
+  if (b.p && keep) {
+    e = cudaMemcpyAsync(nb.p, b.p, keep, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { nb.release(); return e; }
+  }
+  b.release();
+  b = nb;
+  return cudaSuccess;
+}
+cudaError_t grow_keep(HostBuf &b, size_t n, size_t keep) {
+  if (n <= b.bytes && b.p) return cudaSuccess;
+  HostBuf nb;
+  cudaError_t e = nb.ensure(n + n / 2);
+  if (e != cudaSuccess) return e;
+  if (b.p && keep) std::memcpy(nb.p, b.p, keep);
+  b.release();
+  b = nb;
+  return cudaSuccess;
+}
+}  // namespace
+
+// Places every active instance's program in its own padded range of the
+// device program (a pinned host mirror holds the whole layout) and uploads
+// the ranges that changed.  A program that outgrows its range moves to the
+// end and leaves a no-op hole; a full relayout compacts the holes once they
+// are half of the program, and runs whenever the active set changes.
+int Engine::layout_programs(bool relayout) {
+  auto pad = [](int64_t n) { return n + n / 4 + 64; };
+  std::vector<std::pair<int64_t, int64_t>> op_holes, snap_holes;
+  int64_t o = nops_, sn = nsnaps_;
+  if (!relayout) {
+    for (int a : active_) {
+      Instance &in = inst_[a];
+      if (static_cast<int64_t>(in.prog.ops.size()) <= in.ops_cap &&
+          static_cast<int64_t>(in.prog.snaps.size()) <= in.snaps_cap)
+        continue;
+      op_holes.emplace_back(in.ops_off, in.ops_cap);
+      snap_holes.emplace_back(in.snaps_off, in.snaps_cap);
+      hole_ops_ += in.ops_cap;
+      in.ops_off = o;
+      in.ops_cap = pad(static_cast<int64_t>(in.prog.ops.size()));
+      o += in.ops_cap;
+      in.snaps_off = sn;
+      in.snaps_cap = pad(static_cast<int64_t>(in.prog.snaps.size()));
+      sn += in.snaps_cap;
+      in.prog_dirty = true;
+    }
+    if (hole_ops_ > o / 2) relayout = true;
+  }
+  if (relayout) {
+    o = sn = 0;
+    op_holes.clear();
+    snap_holes.clear();
+    hole_ops_ = 0;
+    for (int a : active_) {
+      Instance &in = inst_[a];
+      in.ops_off = o;
+      in.ops_cap = pad(static_cast<int64_t>(in.prog.ops.size()));
+      o += in.ops_cap;
+      in.snaps_off = sn;
+      in.snaps_cap = pad(static_cast<int64_t>(in.prog.snaps.size()));
+      sn += in.snaps_cap;
+      in.prog_dirty = true;
+    }
+  }
+  const size_t keep_o = relayout ? 0 : sizeof(GhostOp) * nops_;
+  const size_t keep_s = relayout ? 0 : sizeof(GhostSnap) * nsnaps_;
+  CK(grow_keep(d_ops_, sizeof(GhostOp) * o, keep_o, stream_), "alloc");
+  CK(grow_keep(d_snaps_, sizeof(GhostSnap) * sn, keep_s, stream_), "alloc");
+  CK(grow_keep(h_ops_, sizeof(GhostOp) * o, keep_o), "alloc");
+  CK(grow_keep(h_snaps_, sizeof(GhostSnap) * sn, keep_s), "alloc");
+  nops_ = o;
+  nsnaps_ = sn;
+  CK(d_snap_.ensure(sizeof(double) * 8 * (static_cast<size_t>(kMaxSeg) * nsnaps_ + 1)), "alloc");
+  GhostOp *ho = h_ops_.as<GhostOp>();
+  GhostSnap *hs = h_snaps_.as<GhostSnap>();
+  const GhostOp nop{0, 0, 0, 0, GOP_NOP, {0, 0, 0}};
+  const GhostSnap nosnap{-1, 0};
+  int64_t bytes = 0;
+  auto put = [&](int64_t off, int64_t cnt, bool ops) -> int {
+    if (cnt <= 0) return AMR_OK;
+    const size_t sz = ops ? sizeof(GhostOp) : sizeof(GhostSnap);
+    char *dst = static_cast<char *>(ops ? d_ops_.p : d_snaps_.p) + sz * off;
+    const char *src = (ops ? reinterpret_cast<const char *>(ho) : reinterpret_cast<const char *>(hs)) + sz * off;
+    CK(cudaMemcpyAsync(dst, src, sz * cnt, cudaMemcpyHostToDevice, stream_), "h2d");
+    bytes += static_cast<int64_t>(sz * cnt);
+    return AMR_OK;
+  };
+  for (const auto &h : op_holes) {
+    for (int64_t q = 0; q < h.second; q++) ho[h.first + q] = nop;
+    if (int rc = put(h.first, h.second, true)) return rc;
+  }
+  for (const auto &h : snap_holes) {
+    for (int64_t q = 0; q < h.second; q++) hs[h.first + q] = nosnap;
+    if (int rc = put(h.first, h.second, false)) return rc;
+  }
+  for (int a : active_) {
+    Instance &in = inst_[a];
+    if (!in.prog_dirty) continue;
+    const int64_t no = static_cast<int64_t>(in.prog.ops.size()), ns = static_cast<int64_t>(in.prog.snaps.size());
+    GhostOp *d = ho + in.ops_off;
+    for (int64_t q = 0; q < no; q++) {
+      d[q] = in.prog.ops[q];
+      if (d[q].type == GOP_SNAP || d[q].type == GOP_SFINE) d[q].src_slot += static_cast<int32_t>(in.snaps_off);
+    }
+    for (int64_t q = no; q < in.ops_cap; q++) d[q] = nop;
+    if (ns) std::memcpy(hs + in.snaps_off, in.prog.snaps.data(), sizeof(GhostSnap) * ns);
+    for (int64_t q = ns; q < in.snaps_cap; q++) hs[in.snaps_off + q] = nosnap;
+    if (int rc = put(in.ops_off, in.ops_cap, true)) return rc;
+    if (int rc = put(in.snaps_off, in.snaps_cap, false)) return rc;
+    in.prog_dirty = false;
+  }
+  prof_.h2d_bytes += bytes;
+  return AMR_OK;
+}
+
 int Engine::rebuild() {
   bool need = !programs_valid_ || built_active_ != active_;
   for (int a : active_)
@@ -262,10 +438,10 @@ int Engine::rebuild() {
   if (!need) return AMR_OK;
   gen_++;
   const auto t0 = std::chrono::steady_clock::now();
+  const bool relayout = !programs_valid_ || built_active_ != active_;
+  if (int rc = compile_programs()) return rc;
   tasks_.clear();
   task_blk_.clear();
-  prog_.clear();
-  std::vector<Bound> bounds;
   for (int a : active_) {
     Instance &in = inst_[a];
     in.task_begin = static_cast<int>(tasks_.size());
@@ -277,39 +453,23 @@ int Engine::rebuild() {
       task_blk_.push_back(nb);
     }
     in.task_end = static_cast<int>(tasks_.size());
-    in.tree.locate_bounds(bounds);
-    try {
-      gc_->compile(in.tree, bounds, in.slot.data(), prog_);
-    } catch (const std::exception &ex) {
-      return fail(AMR_E_STATE, ex.what());
-    }
     built_version_[a] = in.tree.version;
   }
   built_active_ = active_;
+  if (int rc = layout_programs(relayout)) return rc;
   const size_t nt = tasks_.size();
   CK(d_tasks_.ensure(sizeof(LeafTask) * nt), "alloc");
-  CK(cudaMemcpyAsync(d_tasks_.p, tasks_.data(), sizeof(LeafTask) * nt, cudaMemcpyHostToDevice, stream_), "h2d");
+  CK(h_tasks_.ensure(sizeof(LeafTask) * nt), "alloc");
+  std::memcpy(h_tasks_.p, tasks_.data(), sizeof(LeafTask) * nt);
+  CK(cudaMemcpyAsync(d_tasks_.p, h_tasks_.p, sizeof(LeafTask) * nt, cudaMemcpyHostToDevice, stream_), "h2d");
   CK(d_lambda_.ensure(sizeof(double) * nt), "alloc");
   CK(d_grad_.ensure(sizeof(double) * nt), "alloc");
   CK(h_lambda_.ensure(sizeof(double) * nt), "alloc");
   CK(h_grad_.ensure(sizeof(double) * nt), "alloc");
-  CK(d_ops_.ensure(sizeof(GhostOp) * prog_.ops.size()), "alloc");
-  CK(d_snaps_.ensure(sizeof(GhostSnap) * prog_.snaps.size()), "alloc");
-  if (!prog_.ops.empty())
-    CK(cudaMemcpyAsync(d_ops_.p, prog_.ops.data(), sizeof(GhostOp) * prog_.ops.size(), cudaMemcpyHostToDevice,
-                       stream_), "h2d");
-  if (!prog_.snaps.empty())
-    CK(cudaMemcpyAsync(d_snaps_.p, prog_.snaps.data(), sizeof(GhostSnap) * prog_.snaps.size(),
-                       cudaMemcpyHostToDevice, stream_), "h2d");
-  const size_t nsnap = static_cast<size_t>(kMaxSeg) * prog_.snaps.size();
-  CK(d_snap_.ensure(sizeof(double) * 8 * (nsnap + 1)), "alloc");
-  // the host vectors above must outlive the async copies
+  // the pinned mirrors above must not change before the copies have run
   CK(cudaStreamSynchronize(stream_), "sync");
   programs_valid_ = true;
-  size_t bytes = sizeof(LeafTask) * nt;
-  bytes += sizeof(GhostOp) * prog_.ops.size() + sizeof(GhostSnap) * prog_.snaps.size();
-  prof_.h2d_bytes += static_cast<int64_t>(bytes);
-  prof_.launches += 0;
+  prof_.h2d_bytes += static_cast<int64_t>(sizeof(LeafTask) * nt);
   prof_.host_compile_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return AMR_OK;
 }
@@ -337,8 +497,8 @@ int Engine::fill(std::initializer_list<std::pair<FillKind, int>> what) {
   GhostLaunch g{};
   g.ops = d_ops_.as<GhostOp>();
   g.snaps = d_snaps_.as<GhostSnap>();
-  g.nops = static_cast<int>(prog_.ops.size());
-  g.nsnaps = static_cast<int>(prog_.snaps.size());
+  g.nops = static_cast<int>(nops_);
+  g.nsnaps = static_cast<int>(nsnaps_);
   int q = 0;
   for (const auto &w : what) {
     GhostSeg &s = g.seg[q++];

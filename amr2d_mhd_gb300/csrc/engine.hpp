@@ -49,6 +49,12 @@ struct Instance {
   std::vector<int> slot;      // block ID -> physical slot, -1 if none yet
   double dx[16] = {0}, dy[16] = {0};
   int task_begin = 0, task_end = 0;  // this instance's leaves in the task list
+  // compiled ghost fill of the current tree (snapshot rows numbered from 0)
+  // and its range in the device program
+  GhostProgram prog;
+  uint64_t prog_version = ~0ull;
+  bool prog_dirty = true;            // range not yet uploaded
+  int64_t ops_off = 0, ops_cap = 0, snaps_off = 0, snaps_cap = 0;
   explicit Instance(const TreeShape &s) : tree(s) {}
 };
 
@@ -124,11 +130,16 @@ class Engine {
   bool programs_valid_ = false;
   std::vector<LeafTask> tasks_;
   std::vector<int> task_blk_;      // block ID of each task
-  GhostProgram prog_;              // ghost fill of the active set (all fields)
+  // ghost fill of the active set: the instances' programs side by side, each
+  // in a range padded with no-op entries so a changed tree re-uploads only
+  // its own range
+  int64_t nops_ = 0, nsnaps_ = 0, hole_ops_ = 0;
+  int compile_programs();          // recompile changed instances (host threads)
+  int layout_programs(bool relayout);
   DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_, d_snaps_;
   DevBuf d_treeops_, d_stage_, d_slots_;
-  HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_stage_;
-  GhostCompiler *gc_ = nullptr;
+  HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_stage_, h_ops_, h_snaps_, h_tasks_;
+  std::vector<GhostCompiler *> gcs_;  // one per compile thread
 
   // CUDA graph of one step, re-captured when gen_ moves (tree, pool, profiling)
   bool graph_on_ = true;

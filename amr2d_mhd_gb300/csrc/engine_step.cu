@@ -122,6 +122,7 @@ int Engine::init() {
     in.t = 0.0;
     in.dt = 0.0;  // dom.dt is read before its first assignment (main.cpp:267 vs :344)
     in.dtn = 0.0;
+    if (in.cfg.dt_fixed > 0) in.dt = in.dtn = in.cfg.dt_fixed;
     in.count = 0;
   }
   std::vector<int> all(inst_.size());
@@ -144,11 +145,15 @@ int Engine::finish_step() {
       const double v = (tasks_[t].dx < tasks_[t].dy ? tasks_[t].dx : tasks_[t].dy) / hl[t];
       lambda = v < lambda ? v : lambda;
     }
+    in.count = in.count + 1;
+    in.cell_updates += static_cast<int64_t>(in.task_end - in.task_begin) * NI * NI;
+    if (in.cfg.dt_fixed > 0) {  // fixed step: t advances by the dt this step used
+      in.t = in.t + in.cfg.dt_fixed;
+      continue;
+    }
     in.t = in.t + in.dtn;  // main.cpp:344-347
     in.dt = in.dtn;
-    in.count = in.count + 1;
     in.dtn = in.cfl * lambda;
-    in.cell_updates += static_cast<int64_t>(in.task_end - in.task_begin) * NI * NI;
     if (in.dtn < 0 || std::isnan(in.dtn)) return fail(AMR_E_DT, "invalid dt produced");
   }
   return admesh_all(active_, nullptr);

@@ -157,3 +157,67 @@ double criteria_grad(const double *W, int n, int ng) {
 }
 
 }  // namespace amr
+
+// ------------------------------------------------------------- seeded problems
+namespace amr {
+
+// MT19937-64 (Matsumoto & Nishimura; Nishimura 2000), written out so the draw
+// does not depend on the standard library's distributions.
+SeededDraw::SeededDraw(unsigned long long seed) {
+  mt_[0] = seed;
+  for (int i = 1; i < 312; i++)
+    mt_[i] = 6364136223846793005ULL * (mt_[i - 1] ^ (mt_[i - 1] >> 62)) + static_cast<unsigned long long>(i);
+  idx_ = 312;
+}
+
+unsigned long long SeededDraw::raw() {
+  constexpr unsigned long long kUpper = 0xFFFFFFFF80000000ULL, kLower = 0x7FFFFFFFULL;
+  constexpr unsigned long long kMatrix = 0xB5026F5AA96619E9ULL;
+  if (idx_ >= 312) {
+    for (int i = 0; i < 312; i++) {
+      const unsigned long long x = (mt_[i] & kUpper) | (mt_[(i + 1) % 312] & kLower);
+      unsigned long long xa = x >> 1;
+      if (x & 1ULL) xa ^= kMatrix;
+      mt_[i] = mt_[(i + 156) % 312] ^ xa;
+    }
+    idx_ = 0;
+  }
+  unsigned long long y = mt_[idx_++];
+  y ^= (y >> 29) & 0x5555555555555555ULL;
+  y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
+  y ^= (y << 37) & 0xFFF7EEE000000000ULL;
+  y ^= y >> 43;
+  return y;
+}
+
+double SeededDraw::uniform() { return static_cast<double>(raw() >> 11) * (1.0 / 9007199254740992.0); }
+
+double SeededDraw::normal() {
+  if (have_spare_) { have_spare_ = false; return spare_; }
+  double u1 = uniform();
+  const double u2 = uniform();
+  if (u1 <= 0.0) u1 = 1.0 / 9007199254740992.0;
+  const double r = std::sqrt(-2.0 * std::log(u1));
+  spare_ = r * std::sin(2.0 * kPi * u2);
+  have_spare_ = true;
+  return r * std::cos(2.0 * kPi * u2);
+}
+
+void blast_draw(unsigned long long seed, int index, double P[6], int &maxlevs) {
+  SeededDraw g(seed + static_cast<unsigned long long>(index));
+  const double s4p = std::sqrt(4.0 * kPi);
+  P[0] = 0.05 + 0.10 * g.uniform();
+  P[1] = 5.0 + 45.0 * g.uniform();
+  P[2] = (0.5 + 1.5 * g.uniform()) / s4p;
+  P[3] = 0.5 * kPi * g.uniform();
+  P[4] = 0.5;
+  P[5] = 0.5;
+  maxlevs = 3 + static_cast<int>(g.raw() >> 62);
+}
+
+void kh_draw(unsigned long long seed, double a[16]) {
+  SeededDraw g(seed);
+  for (int k = 0; k < 16; k++) a[k] = 1e-3 * g.normal();
+}
+
+}  // namespace amr

@@ -35,3 +35,34 @@ void prim_to_cons(const double *W, double *U, int ncell, double gamma);
 double criteria_grad(const double *W, int n, int ng);
 
 }  // namespace amr
+
+namespace amr {
+
+// Seeded problem generators.  Draws come from MT19937-64 (the engine that
+// std::mt19937_64 names, whose output sequence the C++ standard fixes) turned
+// into doubles as (x >> 11) * 2^-53, so a seed gives the same problem on
+// every platform.
+class SeededDraw {
+ public:
+  explicit SeededDraw(unsigned long long seed);
+  unsigned long long raw();
+  double uniform();            // [0, 1)
+  double normal();             // N(0, 1), Box-Muller (Box & Muller 1958)
+ private:
+  unsigned long long mt_[312];
+  int idx_;
+  bool have_spare_ = false;
+  double spare_ = 0.0;
+};
+
+// Cylindrical blast instance `index` of the batch seeded by `seed`: generator
+// seed = seed + index; draws in this order r0 ~ U[0.05, 0.15],
+// p_in ~ U[5, 50], |B| ~ U[0.5, 2] / sqrt(4 pi), theta ~ U[0, pi/2],
+// maxlevs ~ U{3..6}.  ic_param = {r0, p_in, |B|, theta, 0.5, 0.5}.
+void blast_draw(unsigned long long seed, int index, double ic_param[6], int &maxlevs);
+
+// Kelvin-Helmholtz perturbation amplitudes a_1..a_16 ~ N(0, sigma^2) with
+// sigma = 1e-3, from the generator seeded with `seed`.
+void kh_draw(unsigned long long seed, double a[16]);
+
+}  // namespace amr

@@ -144,22 +144,6 @@ def advance_to(sim, t_stop, chunk=50):
         sim.run(chunk)
 
 
-def uniform_density(sim, level):
-    """Leaf densities painted onto the uniform grid of `level` (piecewise constant)."""
-    lp, ic, lf = sim.tree()
-    U = sim.download("U")
-    ng = 2
-    n = 16 * 2 * 2 ** level
-    out = np.zeros((n, n))
-    for b in np.nonzero(lf)[0]:
-        lev = lp[b, 0]
-        r = 2 ** (level - lev)
-        rho = U[b, 0, ng:-ng, ng:-ng].T   # [i][j]
-        x0, y0 = ic[b, 0] * r, ic[b, 1] * r
-        out[x0:x0 + 16 * r, y0:y0 + 16 * r] = np.kron(rho, np.ones((r, r)))
-    return out
-
-
 def run_ours(args):
     import torch
 
@@ -237,7 +221,7 @@ def run_ours(args):
         advance_to(sim, 1e9, chunk=500)
         inf = sim.info()
         results[prec]["t_end"] = inf["t"]
-        results[prec]["rho"] = uniform_density(sim, WORKLOAD["maxlevs"] - 1) if rank == 0 else None
+        results[prec]["rho"] = sim.uniform(0) if rank == 0 else None
         sim.close()
     return results, world, rank
 

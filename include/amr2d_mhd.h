@@ -80,7 +80,10 @@ typedef struct amr_config {
   double t_end;           /* <= 0: the IC's own value */
   double ic_param[24];    /* extension ICs (blast: r0, p_in, |B|, theta, xc, yc; KH: a_1..a_16) */
   int32_t precision;      /* amr_precision */
-  int32_t reserved[7];
+  int32_t reserved0;
+  double dt_fixed;        /* extension: > 0 = every step uses this dt (no CFL
+                             reduction, no lag); 0 = main.cpp:322-347 */
+  int32_t reserved[4];
 } amr_config;
 
 typedef struct amr_info {
@@ -106,6 +109,16 @@ typedef struct amr_handle amr_handle;
  * (main.cpp:156-177: "nx ny nvar / lenx leny / CFL / IC limiter fluxMth"). */
 void amr_config_default(amr_config *cfg);
 int amr_config_from_input(const char *path, amr_config *cfg);
+/* Seeded extension problems (no counterpart in the reference, which has
+ * neither IC).  amr_config_blast: cylindrical blast instance `index` of the
+ * batch `seed` (MT19937-64 seeded with seed + index; r0 ~ U[0.05,0.15],
+ * p_in ~ U[5,50], |B| ~ U[0.5,2]/sqrt(4 pi), theta ~ U[0,pi/2], maxlevs ~
+ * U{3..6}; gamma 1.4, MUSCL-MC + HLLE, CFL 0.2, outflow, 2 x 2 roots,
+ * t_end 0.1).  amr_config_kh: frozen 256^2 periodic Kelvin-Helmholtz layer
+ * (16 x 16 roots, maxlevs 1, MC + RUSA, gamma 5/3, dt_fixed 2e-4,
+ * a_1..a_16 ~ N(0, (1e-3)^2) from MT19937-64 seeded with `seed`). */
+int amr_config_blast(uint64_t seed, int32_t index, amr_config *cfg);
+int amr_config_kh(uint64_t seed, amr_config *cfg);
 int amr_abi_version(void);
 const char *amr_status_string(int status);
 

@@ -1661,6 +1661,7 @@ int oracle_init(oracle *o) {
   for (int nb = 0; nb < o->lastActive; nb++) if (o->leafs[nb]) prim2cons(o, nb);
   o->dt = 0.0;   /* dom.dt is read before its first assignment in the reference */
   o->dtn = 0.0;
+  if (o->c.dt_fixed > 0) o->dt = o->dtn = o->c.dt_fixed;
   o->t = 0.0;
   o->count = 0;
   if (o->c.maxlevs > 1 && admesh(o)) return -1;
@@ -1720,11 +1721,15 @@ int oracle_step(oracle *o) {
   for (int l = 0; l < nL; l++) lambda = SMIN(lambda, lam_b[l]);
   free(lam_b);
   free(leaf);
-  o->t = o->t + o->dtn;
-  o->dt = o->dtn;
   o->count = o->count + 1;
-  o->dtn = o->c.cfl * lambda;
-  if (o->dtn < 0 || isnan(o->dtn)) return fail(o, "invalid dt");
+  if (o->c.dt_fixed > 0) {
+    o->t = o->t + o->c.dt_fixed;
+  } else {
+    o->t = o->t + o->dtn;
+    o->dt = o->dtn;
+    o->dtn = o->c.cfl * lambda;
+    if (o->dtn < 0 || isnan(o->dtn)) return fail(o, "invalid dt");
+  }
   if (o->c.maxlevs > 1 && !o->no_remesh && admesh(o)) return -1;
   return 0;
 }

@@ -48,6 +48,7 @@ typedef struct oracle_cfg {
   double tend_override;  /* <= 0: the IC's own value */
   double ic_param[24];   /* extension ICs: blast / KH parameters */
   int nthreads;          /* OpenMP threads over blocks (0 = default) */
+  double dt_fixed;       /* extension: > 0 = every step uses this dt */
 } oracle_cfg;
 
 /* what oracle_get copies */
