@@ -1,0 +1,462 @@
+// Discrete adjoint of one fixed-mesh time step: MUSCL reconstruction with the
+// MC / minmod limiter, the Rusanov flux, the residual and RK2 combine, CT2D and
+// the ghost fills.  Every kernel is the transpose of the forward kernel of the
+// same name (stage_split.cuh, aux_kernels.cuh) at the forward state it is
+// given; FP64 only.  An adjoint array holds d(loss)/d(value) of the forward
+// array of the same layout ([slot][var][N][N]).
+#pragma once
+
+#include "amr_common.h"
+#include "aux_kernels.cuh"
+#include "physics.cuh"
+#include "stage.cuh"
+
+namespace amr {
+
+// ------------------------------------------------------------ ghost fills
+// A fill writes dst <- f(pre-fill sources).  Its transpose moves the adjoint
+// of every written cell to the cells it was read from: first take (read and
+// zero) the adjoint of every destination, then add it to the sources.
+struct GhostAdjLaunch {
+  const GhostOp *ops;
+  const GhostSnap *snaps;
+  int nops;
+  GhostSeg seg[kMaxSeg];   // adjoint arrays (double), nv and kind of the forward field
+  int nseg;
+  double *take;            // [nseg][nops][8]
+};
+
+template <int N>
+__global__ void k_ghost_adj_take(GhostAdjLaunch g) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nops * g.nseg) return;
+  const int q = t / g.nops, r = t % g.nops;
+  const GhostOp op = g.ops[r];
+  if (op.type == GOP_NOP) return;
+  const GhostSeg &s = g.seg[q];
+  double *a = static_cast<double *>(s.field) + static_cast<size_t>(op.dst_slot) * s.nv * (N * N) + op.dst_pos;
+  double *out = g.take + (static_cast<size_t>(q) * g.nops + r) * 8;
+  for (int k = 0; k < s.nv; k++) {
+    out[k] = a[k * N * N];
+    a[k * N * N] = 0.0;
+  }
+}
+
+// weights of the 2x2 patch (i,j) (i,j+1) (i+1,j) (i+1,j+1) in fine_value()
+__device__ __forceinline__ void fine_weights(int kind, int k, double w[4]) {
+  if (kind == 0) { w[0] = w[1] = w[2] = w[3] = 0.25; return; }
+  w[0] = w[1] = w[2] = w[3] = 0.0;
+  if (kind == 1) { w[0] = 0.5; if (k == 0) w[1] = 0.5; else w[2] = 0.5; return; }
+  w[0] = 1.0;
+}
+
+template <int N>
+__global__ void k_ghost_adj_give(GhostAdjLaunch g) {
+  constexpr int NN = N * N;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nops * g.nseg) return;
+  const int q = t / g.nops, r = t % g.nops;
+  const GhostOp op = g.ops[r];
+  if (op.type == GOP_NOP) return;
+  const GhostSeg &s = g.seg[q];
+  double *fld = static_cast<double *>(s.field);
+  const double *in = g.take + (static_cast<size_t>(q) * g.nops + r) * 8;
+  for (int k = 0; k < s.nv; k++) {
+    const double v = in[k];
+    if (v == 0.0) continue;
+    if (op.type == GOP_COPY) {
+      atomicAdd(fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos, v);
+    } else if (op.type == GOP_SNAP) {
+      const GhostSnap sn = g.snaps[op.src_slot];
+      atomicAdd(fld + (static_cast<size_t>(sn.slot) * s.nv + k) * NN + sn.pos, v);
+    } else {
+      double w[4];
+      fine_weights(s.kind, k, w);
+      for (int p = 0; p < 4; p++) {
+        if (w[p] == 0.0) continue;
+        size_t at;
+        if (op.type == GOP_FINE) {
+          const int off = p == 0 ? 0 : (p == 1 ? N : (p == 2 ? 1 : N + 1));
+          at = (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos + off;
+        } else {  // GOP_SFINE: snapshot rows src_slot .. src_slot + 3
+          const GhostSnap sn = g.snaps[op.src_slot + p];
+          at = (static_cast<size_t>(sn.slot) * s.nv + k) * NN + sn.pos;
+        }
+        atomicAdd(fld + at, w[p] * v);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- CT2D
+struct CtAdjArgs {
+  const LeafTask *tasks;
+  const InstParams *inst;
+  int step;
+  // forward values
+  const double *Bnew;      // face field after its fill (input of the cell correction)
+  const double *qpre;      // cell state before the correction
+  // adjoints
+  double *aq;              // cell state (in place: post -> pre correction)
+  double *aBnew;           // face field written by the face update
+  double *aBsrc;           // CT2D's Bi argument
+  double *aE;              // EMF
+  double *aF, *aG;         // fluxes after their fill
+};
+
+// CT2D.cpp:99-120 transposed: q4 += (|b_avg|^2 - q5^2 - q6^2)/2, q5 = bx, q6 = by
+template <int NG>
+__global__ void k_ct_cell_adj(CtAdjArgs a) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  const LeafTask t = a.tasks[blockIdx.x];
+  const double *B = a.Bnew + static_cast<size_t>(t.slot) * 2 * NN;
+  const double *qp = a.qpre + static_cast<size_t>(t.slot) * 8 * NN;
+  double *aq = a.aq + static_cast<size_t>(t.slot) * 8 * NN;
+  double *aB = a.aBnew + static_cast<size_t>(t.slot) * 2 * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    const int ip = i < N - 1 ? i + 1 : i, ii = ip - 1;
+    const int jp = j < N - 1 ? j + 1 : j, jj = jp - 1;
+    const double bx = 0.5 * (B[j * N + ip] + B[j * N + ii]);
+    const double by = 0.5 * (B[NN + jp * N + i] + B[NN + jj * N + i]);
+    const double a4 = aq[4 * NN + c];
+    const double lbx = aq[5 * NN + c] + a4 * bx;
+    const double lby = aq[6 * NN + c] + a4 * by;
+    aq[5 * NN + c] = -a4 * qp[5 * NN + c];
+    aq[6 * NN + c] = -a4 * qp[6 * NN + c];
+    atomicAdd(aB + j * N + ip, 0.5 * lbx);
+    atomicAdd(aB + j * N + ii, 0.5 * lbx);
+    atomicAdd(aB + NN + jp * N + i, 0.5 * lby);
+    atomicAdd(aB + NN + jj * N + i, 0.5 * lby);
+  }
+}
+
+// CT2D.cpp:78-92 transposed.  Bx' = s Bsrc (+ s Bold) - s dt/dy (E[i][jp] - E[i][j]),
+// By' = ... + s dt/dx (E[ip][j] - E[i][j]), s = 1 (stage 1) or 1/2 (stage 2).
+// Adds the EMF adjoint (gathered) and s * aBnew to aBsrc; the caller then
+// scales (stage 2) or clears (stage 1) aBnew.
+template <int NG>
+__global__ void k_ct_face_adj(CtAdjArgs a) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  const LeafTask t = a.tasks[blockIdx.x];
+  const double dt = a.inst[t.inst].dt;
+  const double s = a.step == 1 ? 1.0 : 0.5;
+  const double cx = s * dt * (1. / t.dy), cy = s * dt * (1. / t.dx);
+  const double *aBx = a.aBnew + static_cast<size_t>(t.slot) * 2 * NN, *aBy = aBx + NN;
+  double *aS = a.aBsrc + static_cast<size_t>(t.slot) * 2 * NN;
+  double *aE = a.aE + static_cast<size_t>(t.slot) * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    double e = 0.0;
+    if (j < N - 1) e += cx * aBx[c];
+    if (j >= 1 && j - 1 < N - 1) e -= cx * aBx[c - N];
+    if (i < N - 1) e -= cy * aBy[c];
+    if (i >= 1 && i - 1 < N - 1) e += cy * aBy[c - 1];
+    aE[c] += e;
+    aS[c] += s * aBx[c];
+    aS[NN + c] += s * aBy[c];
+  }
+}
+
+// CT2D.cpp:16-26 transposed: E[i][j] = (gg5[i-1][j] + gg5[i][j] - ff6[i][j-1]
+// - ff6[i][j]) / 4 for i, j >= 1
+template <int NG>
+__global__ void k_ct_emf_adj(CtAdjArgs a) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  const LeafTask t = a.tasks[blockIdx.x];
+  const double *aE = a.aE + static_cast<size_t>(t.slot) * NN;
+  double *aF6 = a.aF + static_cast<size_t>(t.slot) * 8 * NN + 6 * NN;
+  double *aG5 = a.aG + static_cast<size_t>(t.slot) * 8 * NN + 5 * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    double g = 0.0, f = 0.0;
+    if (i >= 1 && j >= 1) { g += aE[c]; f += aE[c]; }
+    if (i + 1 < N && j >= 1) g += aE[c + 1];
+    if (j + 1 < N && i >= 1) f += aE[c + N];
+    aG5[c] += 0.25 * g;
+    aF6[c] -= 0.25 * f;
+  }
+}
+
+// ------------------------------------------------------------- RK stage
+struct StageAdjArgs {
+  const LeafTask *tasks;
+  const InstParams *inst;
+  int step;
+  int ntasks;
+  int limiter;
+  const double *W;     // primitive state of the stage (all cells)
+  const double *B;     // face field the stage read
+  double *aOut;        // adjoint of the stage output (Us or U)
+  double *aIn;         // adjoint of the stage input (U or Us)
+  double *aPrev;       // stage 2: adjoint of the old U (in place); else null
+  double *aF, *aG;     // flux adjoints (pre-fill)
+  double *aB;          // adjoint of B (normal face components)
+  double *aL[2], *aR[2];  // face-state adjoints: [x|y] left / right states [slot][8][NN]
+};
+
+// the residual (main.cpp:147-157) transposed onto the fluxes: face p of a
+// row receives inv_dx * (ares(p-1) - ares(p)), ares = -s dt aOut on [LO, HI]^2
+template <int NG>
+__global__ void k_resid_adj_faces(StageAdjArgs a) {
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
+  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<size_t>(a.ntasks) * 8 * NN) return;
+  const int t = static_cast<int>(e / (8 * NN)), r = static_cast<int>(e % (8 * NN));
+  const int c = r % NN, i = c % N, j = c / N;
+  const LeafTask task = a.tasks[t];
+  const size_t idx = static_cast<size_t>(task.slot) * 8 * NN + r;
+  const double s = a.step == 1 ? 1.0 : 0.5;
+  const double dt = a.inst[task.inst].dt;
+  auto ares = [&](int ii, int jj) -> double {
+    if (ii < LO || ii > HI || jj < LO || jj > HI) return 0.0;
+    return -s * dt * a.aOut[idx + (jj - j) * N + (ii - i)];
+  };
+  const double fx = task.inv_dx != 0.0 ? task.inv_dx : 1.0 / task.dx;
+  const double fy = task.inv_dy != 0.0 ? task.inv_dy : 1.0 / task.dy;
+  a.aF[idx] += (ares(i - 1, j) - ares(i, j)) * fx;
+  a.aG[idx] += (ares(i, j - 1) - ares(i, j)) * fy;
+}
+
+// the RK combine (main.cpp:260-270 / 292-302) transposed onto the states
+template <int NG>
+__global__ void k_resid_adj_cells(StageAdjArgs a) {
+  constexpr int NN = Geo<NG>::NN;
+  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<size_t>(a.ntasks) * 8 * NN) return;
+  const int t = static_cast<int>(e / (8 * NN)), r = static_cast<int>(e % (8 * NN));
+  const size_t idx = static_cast<size_t>(a.tasks[t].slot) * 8 * NN + r;
+  const double o = a.aOut[idx];
+  if (a.step == 1) {          // Us = U - dt res
+    a.aIn[idx] += o;
+    a.aOut[idx] = 0.0;
+  } else {                    // U' = (U + Us - dt res) / 2
+    a.aIn[idx] += 0.5 * o;
+    a.aOut[idx] = 0.5 * o;    // the old U is the array U' overwrote
+  }
+}
+
+// MC / minmod limiter and its derivative in r (slopelimiter.cpp:14-27),
+// following the branch the forward takes
+__device__ __forceinline__ double limiter_d(int lim, double r, double &d) {
+  if (lim == LIM_MC) {
+    const double a = 2.0 * r, b = 0.5 * (1.0 + r);
+    const double c = mmin(a, b), dc = a < b ? 2.0 : 0.5;
+    const double e = mmin(c, 2.0), de = c < 2.0 ? dc : 0.0;
+    const double ph = mmax(0.0, e);
+    d = 0.0 > e ? 0.0 : de;
+    return ph;
+  }
+  // minmod
+  const double e = mmin(1.0, r), de = 1.0 < r ? 0.0 : 1.0;
+  d = 0.0 > e ? 0.0 : de;
+  return mmax(0.0, e);
+}
+
+// d(left, right)/d(W[m-1], W[m], W[m+1], W[m+2]) of the face m+1/2
+// (celledges.cpp:38-43, muscl_face in physics.cuh)
+__device__ __forceinline__ void muscl_face_jac(int lim, double wm, double w0, double w1, double w2,
+                                               double jl[3], double jr[3]) {
+  const double E = 1.0E-15;
+  const double dA = w0 - wm, dB = w1 - w0, dC = w2 - w1;
+  double dphi;
+  double r = limiter_ratio<double>(lim, dB, dA + E);
+  double phi = limiter_d(lim, r, dphi);
+  // left = w0 + phi dA / 2
+  double q = 0.5 * dA * dphi;
+  double ldA = 0.5 * phi - q * dB / ((dA + E) * (dA + E));
+  double ldB = q / (dA + E);
+  jl[0] = -ldA;               // W[m-1]
+  jl[1] = 1.0 + ldA - ldB;    // W[m]
+  jl[2] = ldB;                // W[m+1]
+  // right = w1 - phi' dC / 2
+  r = limiter_ratio<double>(lim, dB, dC + E);
+  phi = limiter_d(lim, r, dphi);
+  q = 0.5 * dC * dphi;
+  const double rdC = -(0.5 * phi - q * dB / ((dC + E) * (dC + E)));
+  const double rdB = -q / (dC + E);
+  jr[0] = -rdB;               // W[m]
+  jr[1] = 1.0 + rdB - rdC;    // W[m+1]
+  jr[2] = rdC;                // W[m+2]
+}
+
+// Reverse of side_state + fast_speed (riemannS.cpp:59-108, misc.cpp:71-79)
+// for the normal direction x: adds d/dw of lF.F + lq.q + lcf.cf to lw.
+__device__ __forceinline__ void side_adj(const double *w, double g, const double *lF, const double *lq,
+                                         double lcf, double *lw) {
+  const double rho = w[0], u = w[1], v = w[2], z = w[3], p = w[4], bx = w[5], by = w[6], bz = w[7];
+  const double b2 = bx * bx + by * by + bz * bz;
+  const double e = p / (g - 1.0) + 0.5 * rho * (u * u + v * v + z * z) + 0.5 * b2;
+  const double pt = p + 0.5 * b2;
+  const double le = lq[4] + lF[4] * u;     // adjoint of e
+  const double lpt = lF[1] + lF[4] * u;    // adjoint of pt
+  double lr = lq[0] + lq[1] * u + lq[2] * v + lq[3] * z + lF[0] * u + lF[1] * u * u + lF[2] * u * v +
+              lF[3] * u * z + le * 0.5 * (u * u + v * v + z * z);
+  double lu = rho * (lq[1] + lF[0]) + 2.0 * rho * u * lF[1] + rho * v * lF[2] + rho * z * lF[3] +
+              lF[4] * (e + pt - bx * bx) + lF[6] * by + lF[7] * bz + le * rho * u;
+  double lv = rho * lq[2] + rho * u * lF[2] - lF[4] * bx * by - lF[6] * bx + le * rho * v;
+  double lz = rho * lq[3] + rho * u * lF[3] - lF[4] * bx * bz - lF[7] * bx + le * rho * z;
+  double lp = le / (g - 1.0) + lpt;
+  double lbx = lq[5] + (le + lpt) * bx - 2.0 * bx * lF[1] - by * lF[2] - bz * lF[3] -
+               (2.0 * u * bx + v * by + z * bz) * lF[4] - v * lF[6] - z * lF[7];
+  double lby = lq[6] + (le + lpt) * by - bx * lF[2] - bx * v * lF[4] + u * lF[6];
+  double lbz = lq[7] + (le + lpt) * bz - bx * lF[3] - bx * z * lF[4] + u * lF[7];
+  if (lcf != 0.0) {
+    const double A = g * p / rho, C = b2 / rho, T = (by * by + bz * bz) / rho;
+    const double D = sqrt((C - A) * (C - A) + 4.0 * A * T);
+    const double cf = sqrt(0.5 * (C + A + D));
+    const double k = lcf / (4.0 * cf);
+    double lA = k, lC = k, lT = 0.0;
+    if (D > 0.0) {
+      lA += k * (2.0 * T - (C - A)) / D;
+      lC += k * (C - A) / D;
+      lT = k * 2.0 * A / D;
+    }
+    lr += -(A * lA + C * lC + T * lT) / rho;
+    lp += g * lA / rho;
+    lbx += 2.0 * bx * lC / rho;
+    lby += 2.0 * by * (lC + lT) / rho;
+    lbz += 2.0 * bz * (lC + lT) / rho;
+  }
+  lw[0] += lr; lw[1] += lu; lw[2] += lv; lw[3] += lz;
+  lw[4] += lp; lw[5] += lbx; lw[6] += lby; lw[7] += lbz;
+}
+
+// riemannS.cpp:58-116 (Rusanov) transposed for one face in the x frame
+__device__ __forceinline__ void rusa_adj(const double *wL, const double *wR, double g, const double *lf,
+                                         double *lwL, double *lwR) {
+  Side<double> L, R;
+  side_state<double>(wL, g, L);
+  side_state<double>(wR, g, R);
+  const double a = L.cf + fabs(wL[1]), b = R.cf + fabs(wR[1]);
+  const double im = smax(a, b);
+  double lF[8], lqL[8], lqR[8], lim = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    lF[k] = 0.5 * lf[k];
+    lqL[k] = 0.5 * im * lf[k];
+    lqR[k] = -0.5 * im * lf[k];
+    lim -= 0.5 * lf[k] * (R.q[k] - L.q[k]);
+  }
+  const double la = a < b ? 0.0 : lim, lb = a < b ? lim : 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) { lwL[k] = 0.0; lwR[k] = 0.0; }
+  lwL[1] += la * sgn(wL[1]);
+  lwR[1] += lb * sgn(wR[1]);
+  side_adj(wL, g, lF, lqL, la, lwL);
+  side_adj(wR, g, lF, lqR, lb, lwR);
+}
+
+// MUSCL2D.cpp:24-116 + riemannS transposed for one face: the flux adjoints
+// become adjoints of the two reconstructed states (stored per face) and of
+// the normal face field (added to aB)
+template <int NG>
+__global__ void __launch_bounds__(128) k_faces_adj(StageAdjArgs a) {
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN, LO = G::LO, NF = G::NF, PER = 2 * NF * NF;
+  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<size_t>(a.ntasks) * PER) return;
+  const int t = static_cast<int>(e / PER), f = static_cast<int>(e % PER);
+  const LeafTask task = a.tasks[t];
+  const double gamma = a.inst[task.inst].gamma;
+  const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
+  const double *W = a.W + base;
+  const bool yf = f >= NF * NF;
+  const int gi = yf ? f - NF * NF : f;
+  const int r = gi / NF, c = gi % NF;
+  const int s = yf ? N : 1;
+  const int cL = (LO + r) * N + (LO + c);
+  const int kn = yf ? 6 : 5;
+  const int fpos = cL + s;
+  const double bn = a.B[static_cast<size_t>(task.slot) * 2 * NN + (yf ? NN : 0) + fpos];
+  double wl[8], wr[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    if (k == kn) { wl[k] = wr[k] = bn; continue; }
+    const double *w = W + k * NN + cL;
+    const double wm = w[-s], w0 = w[0], w1 = w[s], w2 = w[2 * s];
+    muscl_face<double>(a.limiter, w0, w1, w0 - wm, w1 - w0, w2 - w1, 0.0, wl[k], wr[k]);
+  }
+  const double *af = (yf ? a.aG : a.aF) + base + fpos;
+  double lf[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) lf[k] = af[k * NN];
+  double lwl[8], lwr[8];
+  if (!yf) {
+    rusa_adj(wl, wr, gamma, lf, lwl, lwr);
+  } else {  // riemannS.cpp:12-23 / 47-55: swap (u, v) and (Bx, By)
+    double l2[8], r2[8], f2[8], a2[8], b2[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) { l2[k] = wl[k]; r2[k] = wr[k]; f2[k] = lf[k]; }
+    l2[1] = wl[2]; l2[2] = wl[1]; r2[1] = wr[2]; r2[2] = wr[1];
+    l2[5] = wl[6]; l2[6] = wl[5]; r2[5] = wr[6]; r2[6] = wr[5];
+    f2[1] = lf[2]; f2[2] = lf[1]; f2[5] = lf[6]; f2[6] = lf[5];
+    rusa_adj(l2, r2, gamma, f2, a2, b2);
+#pragma unroll
+    for (int k = 0; k < 8; k++) { lwl[k] = a2[k]; lwr[k] = b2[k]; }
+    lwl[1] = a2[2]; lwl[2] = a2[1]; lwr[1] = b2[2]; lwr[2] = b2[1];
+    lwl[5] = a2[6]; lwl[6] = a2[5]; lwr[5] = b2[6]; lwr[6] = b2[5];
+  }
+  // the normal component of both states is the face field (MUSCL2D.cpp:48-51)
+  a.aB[static_cast<size_t>(task.slot) * 2 * NN + (yf ? NN : 0) + fpos] += lwl[kn] + lwr[kn];
+  double *oL = a.aL[yf ? 1 : 0] + base + fpos, *oR = a.aR[yf ? 1 : 0] + base + fpos;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    oL[k * NN] = k == kn ? 0.0 : lwl[k];
+    oR[k * NN] = k == kn ? 0.0 : lwr[k];
+  }
+}
+
+// Gathers, per cell, the adjoint of its primitive state from the face-state
+// adjoints of the (up to 12) faces whose reconstruction read it, then applies
+// the transpose of U2W (meshblock.cpp:119-145) and adds the result to aIn.
+// Face m+1/2 of a row (left cell m, m in [LO, HI]) reads W[m-1 .. m+2].
+template <int NG>
+__global__ void __launch_bounds__(256) k_muscl_prim_adj(StageAdjArgs a) {
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
+  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<size_t>(a.ntasks) * NN) return;
+  const int t = static_cast<int>(e / NN), c = static_cast<int>(e % NN);
+  const int i = c % N, j = c / N;
+  const LeafTask task = a.tasks[t];
+  const double gamma = a.inst[task.inst].gamma;
+  const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
+  const double *W = a.W + base;
+  double lw[8];
+#pragma unroll 1
+  for (int k = 0; k < 8; k++) {
+    double acc = 0.0;
+    for (int d = 0; d < 2; d++) {       // x faces, then y faces
+      if ((d == 0 && k == 5) || (d == 1 && k == 6)) continue;
+      const int pos = d == 0 ? i : j, row = d == 0 ? j : i, s = d == 0 ? 1 : N;
+      if (row < LO || row > HI) continue;
+      const double *aL = a.aL[d] + base + k * NN, *aR = a.aR[d] + base + k * NN;
+      for (int m = pos - 2; m <= pos + 1; m++) {
+        if (m < LO || m > HI) continue;
+        const int cm = c + (m - pos) * s;   // cell m of this row
+        const double *w = W + k * NN + cm;
+        double jl[3], jr[3];
+        muscl_face_jac(a.limiter, w[-s], w[0], w[s], w[2 * s], jl, jr);
+        const double la = aL[cm + s], ra = aR[cm + s];   // stored at the face position (cell m+1)
+        const int o = pos - m;                            // this cell is W[m + o], o in -1..2
+        if (o >= -1 && o <= 1) acc += jl[o + 1] * la;
+        if (o >= 0 && o <= 2) acc += jr[o] * ra;
+      }
+    }
+    lw[k] = acc;
+  }
+  // U2W transposed
+  const double rho = W[c], u = W[NN + c], v = W[2 * NN + c], z = W[3 * NN + c];
+  const double gm = gamma - 1.0;
+  double *ai = a.aIn + base + c;
+  ai[0] += lw[0] - (lw[1] * u + lw[2] * v + lw[3] * z) / rho + lw[4] * gm * 0.5 * (u * u + v * v + z * z);
+  ai[NN] += lw[1] / rho - lw[4] * gm * u;
+  ai[2 * NN] += lw[2] / rho - lw[4] * gm * v;
+  ai[3 * NN] += lw[3] / rho - lw[4] * gm * z;
+  ai[4 * NN] += lw[4] * gm;
+  for (int k = 5; k < 8; k++) ai[k * NN] += lw[k] - lw[4] * gm * W[k * NN + c];
+}
+
+}  // namespace amr

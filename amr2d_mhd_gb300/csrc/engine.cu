@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <initializer_list>
@@ -258,6 +259,46 @@ int Engine::assign_slots(Instance &in) {
 }
 
 // ------------------------------------------------------------- programs
+namespace {
+// Runs body(worker, item) for items 0..n-1 on up to `threads` host threads
+// (dynamic assignment); returns the first exception's message, if any.
+template <typename F>
+std::string parallel_items(size_t n, size_t threads, F body) {
+  std::atomic<size_t> next{0};
+  std::mutex mu;
+  std::string err;
+  auto work = [&](size_t w) {
+    for (;;) {
+      const size_t q = next.fetch_add(1);
+      if (q >= n) break;
+      try {
+        body(w, q);
+      } catch (const std::exception &ex) {
+        std::lock_guard<std::mutex> g(mu);
+        if (err.empty()) err = ex.what();
+      }
+    }
+  };
+  if (threads > n) threads = n;
+  if (threads <= 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (size_t w = 1; w < threads; w++) th.emplace_back(work, w);
+    work(0);
+    for (auto &t : th) t.join();
+  }
+  return err;
+}
+
+size_t host_threads(size_t work_blocks) {
+  if (work_blocks < 2048) return 1;  // thread start-up would cost more than the work
+  const unsigned hw = std::thread::hardware_concurrency();
+  const size_t n = hw ? hw : 1;
+  return n > 32 ? 32 : n;
+}
+}  // namespace
+
 // Recompiles the ghost fill of every active instance whose tree changed since
 // its last compile, spread over host threads (one compiler each).
 int Engine::compile_programs() {
@@ -269,41 +310,17 @@ int Engine::compile_programs() {
       blocks += static_cast<size_t>(inst_[a].tree.lastActive);
     }
   if (todo.empty()) return AMR_OK;
-  unsigned hw = std::thread::hardware_concurrency();
-  size_t nth = hw ? hw : 1;
-  if (nth > 32) nth = 32;
-  if (nth > todo.size()) nth = todo.size();
-  if (blocks < 2048) nth = 1;  // thread start-up would cost more than the compile
+  const size_t nth = host_threads(blocks);
   while (gcs_.size() < nth) gcs_.push_back(new GhostCompiler(n_, ng_));
-  std::atomic<size_t> next{0};
-  std::mutex mu;
-  std::string err;
-  auto work = [&](size_t w) {
-    std::vector<Bound> bounds;
-    for (;;) {
-      const size_t q = next.fetch_add(1);
-      if (q >= todo.size()) break;
-      Instance &in = inst_[todo[q]];
-      try {
-        in.tree.locate_bounds(bounds);
-        in.prog.clear();
-        gcs_[w]->compile(in.tree, bounds, in.slot.data(), in.prog);
-        in.prog_version = in.tree.version;
-        in.prog_dirty = true;
-      } catch (const std::exception &ex) {
-        std::lock_guard<std::mutex> g(mu);
-        if (err.empty()) err = ex.what();
-      }
-    }
-  };
-  if (nth == 1) {
-    work(0);
-  } else {
-    std::vector<std::thread> th;
-    for (size_t w = 1; w < nth; w++) th.emplace_back(work, w);
-    work(0);
-    for (auto &t : th) t.join();
-  }
+  std::vector<std::vector<Bound>> bounds(nth);
+  const std::string err = parallel_items(todo.size(), nth, [&](size_t w, size_t q) {
+    Instance &in = inst_[todo[q]];
+    in.tree.locate_bounds(bounds[w]);
+    in.prog.clear();
+    gcs_[w]->compile(in.tree, bounds[w], in.slot.data(), in.prog);
+    in.prog_version = in.tree.version;
+    in.prog_dirty = true;
+  });
   if (!err.empty()) return fail(AMR_E_STATE, err);
   return AMR_OK;
 }
@@ -393,40 +410,57 @@ int Engine::layout_programs(bool relayout) {
   GhostSnap *hs = h_snaps_.as<GhostSnap>();
   const GhostOp nop{0, 0, 0, 0, GOP_NOP, {0, 0, 0}};
   const GhostSnap nosnap{-1, 0};
-  int64_t bytes = 0;
-  auto put = [&](int64_t off, int64_t cnt, bool ops) -> int {
-    if (cnt <= 0) return AMR_OK;
-    const size_t sz = ops ? sizeof(GhostOp) : sizeof(GhostSnap);
-    char *dst = static_cast<char *>(ops ? d_ops_.p : d_snaps_.p) + sz * off;
-    const char *src = (ops ? reinterpret_cast<const char *>(ho) : reinterpret_cast<const char *>(hs)) + sz * off;
-    CK(cudaMemcpyAsync(dst, src, sz * cnt, cudaMemcpyHostToDevice, stream_), "h2d");
-    bytes += static_cast<int64_t>(sz * cnt);
-    return AMR_OK;
-  };
-  for (const auto &h : op_holes) {
+  // ranges to upload: holes (filled with no-ops) and the dirty programs
+  std::vector<std::pair<int64_t, int64_t>> up_ops(op_holes), up_snaps(snap_holes);
+  for (const auto &h : op_holes)
     for (int64_t q = 0; q < h.second; q++) ho[h.first + q] = nop;
-    if (int rc = put(h.first, h.second, true)) return rc;
-  }
-  for (const auto &h : snap_holes) {
+  for (const auto &h : snap_holes)
     for (int64_t q = 0; q < h.second; q++) hs[h.first + q] = nosnap;
-    if (int rc = put(h.first, h.second, false)) return rc;
-  }
-  for (int a : active_) {
-    Instance &in = inst_[a];
-    if (!in.prog_dirty) continue;
+  std::vector<int> dirty;
+  size_t blocks = 0;
+  for (int a : active_)
+    if (inst_[a].prog_dirty) {
+      dirty.push_back(a);
+      blocks += static_cast<size_t>(inst_[a].tree.lastActive);
+      up_ops.emplace_back(inst_[a].ops_off, inst_[a].ops_cap);
+      up_snaps.emplace_back(inst_[a].snaps_off, inst_[a].snaps_cap);
+    }
+  parallel_items(dirty.size(), host_threads(blocks), [&](size_t, size_t q) {
+    Instance &in = inst_[dirty[q]];
     const int64_t no = static_cast<int64_t>(in.prog.ops.size()), ns = static_cast<int64_t>(in.prog.snaps.size());
     GhostOp *d = ho + in.ops_off;
-    for (int64_t q = 0; q < no; q++) {
-      d[q] = in.prog.ops[q];
-      if (d[q].type == GOP_SNAP || d[q].type == GOP_SFINE) d[q].src_slot += static_cast<int32_t>(in.snaps_off);
+    for (int64_t k = 0; k < no; k++) {
+      d[k] = in.prog.ops[k];
+      if (d[k].type == GOP_SNAP || d[k].type == GOP_SFINE) d[k].src_slot += static_cast<int32_t>(in.snaps_off);
     }
-    for (int64_t q = no; q < in.ops_cap; q++) d[q] = nop;
+    for (int64_t k = no; k < in.ops_cap; k++) d[k] = nop;
     if (ns) std::memcpy(hs + in.snaps_off, in.prog.snaps.data(), sizeof(GhostSnap) * ns);
-    for (int64_t q = ns; q < in.snaps_cap; q++) hs[in.snaps_off + q] = nosnap;
-    if (int rc = put(in.ops_off, in.ops_cap, true)) return rc;
-    if (int rc = put(in.snaps_off, in.snaps_cap, false)) return rc;
+    for (int64_t k = ns; k < in.snaps_cap; k++) hs[in.snaps_off + k] = nosnap;
     in.prog_dirty = false;
-  }
+  });
+  // one copy per run of adjacent ranges
+  int64_t bytes = 0;
+  auto upload = [&](std::vector<std::pair<int64_t, int64_t>> &r, bool ops) -> int {
+    std::sort(r.begin(), r.end());
+    const size_t sz = ops ? sizeof(GhostOp) : sizeof(GhostSnap);
+    char *dbase = static_cast<char *>(ops ? d_ops_.p : d_snaps_.p);
+    const char *hbase = ops ? reinterpret_cast<const char *>(ho) : reinterpret_cast<const char *>(hs);
+    for (size_t q = 0; q < r.size();) {
+      const int64_t off = r[q].first;
+      int64_t end = off + r[q].second;
+      size_t k = q + 1;
+      while (k < r.size() && r[k].first <= end) { end = std::max(end, r[k].first + r[k].second); k++; }
+      if (end > off) {
+        CK(cudaMemcpyAsync(dbase + sz * off, hbase + sz * off, sz * (end - off), cudaMemcpyHostToDevice, stream_),
+           "h2d");
+        bytes += static_cast<int64_t>(sz * (end - off));
+      }
+      q = k;
+    }
+    return AMR_OK;
+  };
+  if (int rc = upload(up_ops, true)) return rc;
+  if (int rc = upload(up_snaps, false)) return rc;
   prof_.h2d_bytes += bytes;
   return AMR_OK;
 }

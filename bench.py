@@ -223,7 +223,62 @@ def run_ours(args):
         results[prec]["t_end"] = inf["t"]
         results[prec]["rho"] = sim.uniform(0) if rank == 0 else None
         sim.close()
+    if not args.no_batch:
+        results["batch"] = run_batch(stream, args.batch_steps, args.batch_advance)
     return results, world, rank
+
+
+BATCH_SEED = 2026
+BATCH_N = 512
+
+
+def run_batch(stream, steps, advance):
+    """The seeded blast batch (512 instances, maxlevs 3..6, MUSCL-MC + HLLE + CT,
+    CFL 0.2): `advance` untimed batch steps, then `steps` timed ones, each one
+    time step of every unfinished instance, in FP64 and FP32.  Accuracy: four
+    instances (at most 4 levels) run to t = 0.1 in both precisions."""
+    import torch
+
+    import amr2d_mhd_gb300 as amr
+    out = {}
+    for prec in ("fp64", "fp32"):
+        sim = amr.Simulation([amr.blast_config(BATCH_SEED, i, prec) for i in range(BATCH_N)])
+        sim.set_stream(stream.cuda_stream)
+        sim.init()
+        sim.run(advance)
+        sim.profile(True)
+        c0 = sum(sim.info(q)["cell_updates"] for q in range(BATCH_N))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        c1 = sum(sim.info(q)["cell_updates"] for q in range(BATCH_N))
+        p = sim.profile()
+        out[prec] = dict(value=(c1 - c0) / (ms * 1e-3), ms_per_step=ms / steps,
+                         leaves=sum(sim.info(q)["n_leaves"] for q in range(BATCH_N)),
+                         host_ms_per_step=(p["host_compile_ms"] + p["host_admesh_ms"]) / steps,
+                         gpu_launches=int(p["launches"]))
+        sim.close()
+    l1 = []
+    sims = {}
+    for prec in ("fp64", "fp32"):
+        cf = []
+        for i in range(4):
+            c = amr.blast_config(BATCH_SEED, i, prec)
+            c.maxlevs = min(c.maxlevs, 4)
+            cf.append(c)
+        sims[prec] = amr.Simulation(cf).init()
+        sims[prec].run()
+    for i in range(4):
+        a, b = sims["fp32"].uniform(0, instance=i), sims["fp64"].uniform(0, instance=i)
+        l1.append(float(np.abs(a - b).sum() / np.abs(b).sum()))
+    for v in sims.values():
+        v.close()
+    out["l1_rel_density_fp32_vs_fp64_max"] = max(l1)
+    return out
 
 
 def cpu_baseline(steps, threads):
@@ -285,6 +340,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=40, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the blast-batch measurement")
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-advance", type=int, default=120)
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: the rotor from its initial condition for this many steps, then exit")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="precision of --ncu-case")
@@ -349,6 +407,14 @@ def main():
         "fp64_pipe": fp64,
         "fp32": {"value": value32, "speedup_vs_fp64": value32 / value, "l1_rel_density_vs_fp64_at_t_end": l1,
                  "t_end_fp32": r32["t_end"], "t_end_fp64": r64["t_end"], "ms_per_step": r32["ms"] / args.steps},
+        "batch": None if "batch" not in res else {
+            "workload": "%d seeded cylindrical blasts (seed %d, amr_config_blast): [0,1]^2, gamma 1.4, 4 roots, "
+                        "maxlevs U{3..6}, MUSCL-MC + HLLE + CT, CFL 0.2, outflow; %d untimed batch steps, then "
+                        "%d timed" % (BATCH_N, BATCH_SEED, args.batch_advance, args.batch_steps),
+            "fp64": res["batch"]["fp64"], "fp32": res["batch"]["fp32"],
+            "fp32_vs_plain_fp64_rotor": res["batch"]["fp32"]["value"] / value,
+            "l1_rel_density_fp32_vs_fp64_max": res["batch"]["l1_rel_density_fp32_vs_fp64_max"],
+            "l1_sample": "4 instances of the batch (maxlevs capped at 4) run to t = 0.1, finest uniform grid"},
         "cpu_baseline": cpu,
         "clocks": {"sm_mhz": clk.get("sm_mhz"), "sm_max_mhz": clk.get("sm_max_mhz"), "reasons": clk.get("reasons", [])},
         "gpu_launches": int(prof["launches"]),
