@@ -29,7 +29,8 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "a
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static"]
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_adjoint_enable",
+           "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
 
 
 class AmrError(RuntimeError):
@@ -107,6 +108,11 @@ def load(build_if_missing: bool = True):
         "amr_profile_enable": (ctypes.c_int, [vp, i32]),
         "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
         "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
+        "amr_adjoint_enable": (ctypes.c_int, [vp, i32]),
+        "amr_adjoint_seed": (ctypes.c_int, [vp, i32, i32, dp, i64]),
+        "amr_adjoint_step": (ctypes.c_int, [vp]),
+        "amr_adjoint_read": (ctypes.c_int, [vp, i32, i32, dp, i64]),
+        "amr_adjoint_recorded": (ctypes.c_int, [vp, ctypes.POINTER(i32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -286,6 +292,30 @@ class Simulation:
             x0, y0 = ic[b, 0] * r, ic[b, 1] * r
             out[x0:x0 + c.nx * r, y0:y0 + c.ny * r] = np.kron(v, np.ones((r, r)))
         return out
+
+    # discrete adjoint of the frozen-mesh step
+    def adjoint_enable(self, on=True):
+        self._ck(load().amr_adjoint_enable(self.h, int(on)))
+
+    def adjoint_seed(self, field, lam, instance=0):
+        a = np.ascontiguousarray(lam, np.float64)
+        self._ck(load().amr_adjoint_seed(self.h, instance, FIELDS[field], a.ctypes.data, a.size))
+
+    def adjoint_step(self):
+        self._ck(load().amr_adjoint_step(self.h))
+
+    def adjoint_read(self, field, instance=0):
+        inf = self.info(instance)
+        nv = 2 if field == "Bi" else 8
+        n = inf["nx_tot"]
+        a = np.empty((inf["last_active"], nv, n, n), np.float64)
+        self._ck(load().amr_adjoint_read(self.h, instance, FIELDS[field], a.ctypes.data, a.size))
+        return a
+
+    def adjoint_recorded(self):
+        n = ctypes.c_int32()
+        self._ck(load().amr_adjoint_recorded(self.h, ctypes.byref(n)))
+        return n.value
 
     def state(self, instance=0):
         """Dict in the form the oracle's state() returns."""

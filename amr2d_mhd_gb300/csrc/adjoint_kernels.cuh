@@ -184,7 +184,6 @@ struct StageAdjArgs {
   const InstParams *inst;
   int step;
   int ntasks;
-  int limiter;
   const double *W;     // primitive state of the stage (all cells)
   const double *B;     // face field the stage read
   double *aOut;        // adjoint of the stage output (Us or U)
@@ -360,6 +359,7 @@ __global__ void __launch_bounds__(128) k_faces_adj(StageAdjArgs a) {
   const int t = static_cast<int>(e / PER), f = static_cast<int>(e % PER);
   const LeafTask task = a.tasks[t];
   const double gamma = a.inst[task.inst].gamma;
+  const int lim = a.inst[task.inst].limiter;
   const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
   const double *W = a.W + base;
   const bool yf = f >= NF * NF;
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(128) k_faces_adj(StageAdjArgs a) {
     if (k == kn) { wl[k] = wr[k] = bn; continue; }
     const double *w = W + k * NN + cL;
     const double wm = w[-s], w0 = w[0], w1 = w[s], w2 = w[2 * s];
-    muscl_face<double>(a.limiter, w0, w1, w0 - wm, w1 - w0, w2 - w1, 0.0, wl[k], wr[k]);
+    muscl_face<double>(lim, w0, w1, w0 - wm, w1 - w0, w2 - w1, 0.0, wl[k], wr[k]);
   }
   const double *af = (yf ? a.aG : a.aF) + base + fpos;
   double lf[8];
@@ -422,6 +422,7 @@ __global__ void __launch_bounds__(256) k_muscl_prim_adj(StageAdjArgs a) {
   const int i = c % N, j = c / N;
   const LeafTask task = a.tasks[t];
   const double gamma = a.inst[task.inst].gamma;
+  const int lim = a.inst[task.inst].limiter;
   const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
   const double *W = a.W + base;
   double lw[8];
@@ -438,7 +439,7 @@ __global__ void __launch_bounds__(256) k_muscl_prim_adj(StageAdjArgs a) {
         const int cm = c + (m - pos) * s;   // cell m of this row
         const double *w = W + k * NN + cm;
         double jl[3], jr[3];
-        muscl_face_jac(a.limiter, w[-s], w[0], w[s], w[2 * s], jl, jr);
+        muscl_face_jac(lim, w[-s], w[0], w[s], w[2 * s], jl, jr);
         const double la = aL[cm + s], ra = aR[cm + s];   // stored at the face position (cell m+1)
         const int o = pos - m;                            // this cell is W[m + o], o in -1..2
         if (o >= -1 && o <= 1) acc += jl[o + 1] * la;

@@ -193,4 +193,22 @@ int amr_profile_read(amr_handle *h, amr_profile *o) {
   return guarded(h, [&](amr::Engine &e) { return e.profile_read(o); });
 }
 
+int amr_adjoint_enable(amr_handle *h, int32_t on) {
+  return guarded(h, [&](amr::Engine &e) { return e.adjoint_enable(on != 0); });
+}
+int amr_adjoint_seed(amr_handle *h, int32_t inst, int32_t field, const double *lam, int64_t count) {
+  return guarded(h, [&](amr::Engine &e) { return e.adjoint_seed(inst, field, lam, count); });
+}
+int amr_adjoint_step(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.adjoint_step(); }); }
+int amr_adjoint_read(amr_handle *h, int32_t inst, int32_t field, double *lam, int64_t count) {
+  return guarded(h, [&](amr::Engine &e) { return e.adjoint_read(inst, field, lam, count); });
+}
+int amr_adjoint_recorded(amr_handle *h, int32_t *steps) {
+  if (!steps) return AMR_E_ARG;
+  return guarded(h, [&](amr::Engine &e) {
+    *steps = e.adjoint_recorded();
+    return AMR_OK;
+  });
+}
+
 }  // extern "C"

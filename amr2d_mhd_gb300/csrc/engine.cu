@@ -79,6 +79,10 @@ Engine::~Engine() {
     b->release();
   d_ops_.release();
   d_snaps_.release();
+  for (DevBuf *b : {&a_U_, &a_Us_, &a_B_, &a_Bs_, &a_E_, &a_F_, &a_G_, &a_L_[0], &a_L_[1], &a_R_[0], &a_R_[1],
+                    &a_take_, &t_W1_, &t_B1_, &t_BisF_, &t_UsPre_, &t_BnewF_, &t_UPre_})
+    b->release();
+  for (DevBuf &b : ckpt_) b.release();
   for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_, &h_ops_, &h_snaps_, &h_tasks_})
     b->release();
   if (own_stream_ && stream_) cudaStreamDestroy(stream_);
@@ -201,11 +205,13 @@ void *Engine::field_ptr(int f) const {
     case AMR_FIELD_BI: return Bi_;
     case AMR_FIELD_BIS: return Bis_;
     case AMR_FIELD_EMF: return EMF_;
+    case kFieldAdjU: return a_U_.p;
+    case kFieldAdjB: return a_B_.p;
     default: return nullptr;
   }
 }
 int Engine::field_nv(int f) const {
-  if (f == AMR_FIELD_BI || f == AMR_FIELD_BIS) return 2;
+  if (f == AMR_FIELD_BI || f == AMR_FIELD_BIS || f == kFieldAdjB) return 2;
   if (f == AMR_FIELD_EMF) return 1;
   return 8;
 }

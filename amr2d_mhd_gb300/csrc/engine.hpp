@@ -36,6 +36,9 @@ struct HostBuf {
   template <typename T> T *as() const { return static_cast<T *>(p); }
 };
 
+// engine-internal field ids of the adjoint arrays (transfers only)
+constexpr int kFieldAdjU = 100, kFieldAdjB = 101;
+
 struct Instance {
   amr_config cfg{};
   Tree tree;
@@ -82,6 +85,13 @@ class Engine {
 
   int profile_enable(bool on);
   int profile_read(amr_profile *out);
+
+  // discrete adjoint of the frozen-mesh step (adjoint.cu)
+  int adjoint_enable(bool on);
+  int adjoint_seed(int inst, int field, const double *lam, int64_t count);
+  int adjoint_read(int inst, int field, double *lam, int64_t count);
+  int adjoint_step();
+  int adjoint_recorded() const { return static_cast<int>(ckpt_meta_.size()); }
 
   std::string last_error;
 
@@ -157,6 +167,25 @@ class Engine {
   int ev_used_ = 0;
   int64_t stage_cells_pending_ = 0;
   void prof_collect();
+
+  // adjoint: checkpoints of (U, Bi) at the start of every recorded step, the
+  // adjoint arrays and the tape of the step being reversed
+  struct InstMeta { double t, dt, dtn; int64_t count, cell_updates; };
+  struct Checkpoint { std::vector<InstMeta> meta; std::vector<int> active; };
+  struct AdjSeg { FillKind kind; double *a; int nv; };
+  bool adj_on_ = false;
+  std::vector<Checkpoint> ckpt_meta_;
+  std::vector<DevBuf> ckpt_;               // one buffer per recorded step
+  size_t ckpt_slots_ = 0;                  // slots each checkpoint holds
+  DevBuf a_U_, a_Us_, a_B_, a_Bs_, a_E_, a_F_, a_G_, a_L_[2], a_R_[2], a_take_;
+  DevBuf t_W1_, t_B1_, t_BisF_, t_UsPre_, t_BnewF_, t_UPre_;
+  int adjoint_supported();
+  int adjoint_alloc();
+  int adjoint_record();                    // called by step() before the step
+  int adjoint_recompute();
+  int adjoint_sequence();
+  int ghost_adj(std::initializer_list<AdjSeg> what);
+  int ct2d_taped(int step);
 };
 
 }  // namespace amr

@@ -171,6 +171,8 @@ int Engine::step() {
   }
   if (active_.empty()) return AMR_OK;
   if (int rc = rebuild()) return rc;
+  if (adj_on_)
+    if (int rc = adjoint_record()) return rc;
   if (int rc = launch_step()) return rc;
   return finish_step();
 }

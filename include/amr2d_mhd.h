@@ -179,6 +179,27 @@ typedef struct amr_profile {
 int amr_profile_enable(amr_handle *h, int32_t on);
 int amr_profile_read(amr_handle *h, amr_profile *out);
 
+/* ---- discrete adjoint of the frozen-mesh step (no counterpart in the
+ * reference) ------------------------------------------------------------------
+ * Reverse mode through whole time steps, with a checkpoint of (U, Bi) per
+ * step and the step recomputed from it.  Supported: FP64, MUSCL with MC or
+ * minmod, RUSA, nghosts 2, maxlevs 1 (frozen mesh) and dt_fixed > 0, else
+ * AMR_E_UNSUPPORTED.
+ *   amr_adjoint_enable(h, 1): clears the adjoint and the checkpoints; every
+ *     later amr_step records one checkpoint (on = 0 drops them).
+ *   amr_adjoint_seed: sets the adjoint (d loss / d field) of the current
+ *     state, field AMR_FIELD_U or AMR_FIELD_BI, in amr_download's layout.
+ *   amr_adjoint_step: reverses the last recorded step; the adjoint becomes
+ *     that of the state before the step, and the state, t and the step count
+ *     return to the checkpoint.  AMR_E_STATE when nothing is left to reverse.
+ *   amr_adjoint_read: the current adjoint of U or BI (ghost entries are 0).
+ *   amr_adjoint_recorded: steps that can still be reversed. */
+int amr_adjoint_enable(amr_handle *h, int32_t on);
+int amr_adjoint_seed(amr_handle *h, int32_t inst, int32_t field, const double *lam, int64_t count);
+int amr_adjoint_step(amr_handle *h);
+int amr_adjoint_read(amr_handle *h, int32_t inst, int32_t field, double *lam, int64_t count);
+int amr_adjoint_recorded(amr_handle *h, int32_t *steps);
+
 /* ---- allocation-free CFL reduction (no counterpart in the reference) ------
  * For callers that may not allocate device memory (inside a captured CUDA
  * graph, in allocator-free real-time loops, or in frameworks that own every

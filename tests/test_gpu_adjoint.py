@@ -1,0 +1,156 @@
+"""The discrete adjoint of the frozen-mesh step (amr_adjoint_*), wrapped in a
+torch.autograd.Function here in the test harness only: one step against
+torch.autograd through the FP64 restatement (kh_reference.py), and the
+gradient of the Kelvin-Helmholtz loss with respect to the 16 perturbation
+amplitudes against central finite differences (h = 1e-6) and against the
+FP64 autograd reference over the same 200 steps."""
+import numpy as np
+import pytest
+import torch
+
+import kh_reference as K
+
+DT, GAMMA, N = 2e-4, 5.0 / 3.0, 256
+
+
+def kh_sim(gpu, seed=5):
+    c = gpu.kh_config(seed)
+    c.t_end = 1e9   # repeated forward runs in one handle
+    return gpu.Simulation(c).init(), c
+
+
+def block_index(icoord, ng=2, nb=16, n=N):
+    """Global (ix, iy) of every block cell, ghosts wrapped periodically: [blocks, N, N] ([j][i])."""
+    idx = np.arange(nb + 2 * ng) - ng
+    gi = np.stack([np.broadcast_to(((x0 + idx) % n)[None, :], (nb + 2 * ng,) * 2) for x0, _ in icoord])
+    gj = np.stack([np.broadcast_to(((y0 + idx) % n)[:, None], (nb + 2 * ng,) * 2) for _, y0 in icoord])
+    return torch.from_numpy(gi.copy()), torch.from_numpy(gj.copy())
+
+
+def interior_only(a, ng=2):
+    a = np.array(a, copy=True)
+    a[..., :ng, :] = 0
+    a[..., -ng:, :] = 0
+    a[..., :, :ng] = 0
+    a[..., :, -ng:] = 0
+    return a
+
+
+class KHLoss(torch.autograd.Function):
+    """loss(U0) = total density in [0.4, 0.6]^2 after `steps` steps of the
+    library's FP64 path; the backward pass is the library's adjoint."""
+
+    @staticmethod
+    def forward(ctx, U0, sim, B0, steps, mask):
+        sim.upload("U", U0.detach().cpu().numpy())
+        sim.upload("Bi", B0)
+        sim.adjoint_enable(True)
+        sim.run(steps)
+        U = sim.download("U")
+        ctx.sim, ctx.steps, ctx.mask, ctx.shape = sim, steps, mask, U.shape
+        return torch.tensor(float((U[:, 0] * mask).sum()), dtype=torch.float64)
+
+    @staticmethod
+    def backward(ctx, g):
+        sim = ctx.sim
+        lam = np.zeros(ctx.shape)
+        lam[:, 0] = ctx.mask * float(g)
+        sim.adjoint_seed("U", lam)
+        assert sim.adjoint_recorded() == ctx.steps
+        for _ in range(ctx.steps):
+            sim.adjoint_step()
+        gU = sim.adjoint_read("U")
+        return torch.from_numpy(gU), None, None, None, None
+
+
+def blocks_of(U, gi, gj):
+    """Global [8, n, n] -> block layout [blocks, 8, N, N], differentiable."""
+    return U[:, gi, gj].permute(1, 0, 2, 3)
+
+
+@pytest.mark.gpu
+def test_adjoint_rejects_unsupported(gpu):
+    sim = gpu.Simulation(ic="rotor", limiter="MC", flux="HLLD", maxlevs=3).init()
+    with pytest.raises(gpu.AmrError) as e:
+        sim.adjoint_enable(True)
+    assert e.value.code == -11   # AMR_E_UNSUPPORTED
+
+
+@pytest.mark.gpu
+def test_adjoint_one_step_matches_autograd(gpu):
+    """Adjoint of one step with random seeds on U and the face field equals the
+    vector-Jacobian product of the FP64 restatement."""
+    sim, _ = kh_sim(gpu)
+    sim.run(3)
+    ic = sim.tree()[1]
+    U0 = torch.from_numpy(K.from_blocks(sim.download("U"), ic)).requires_grad_(True)
+    B0 = K.from_blocks(sim.download("Bi"), ic)
+    Bx0 = torch.from_numpy(B0[0].copy()).requires_grad_(True)
+    By0 = torch.from_numpy(B0[1].copy()).requires_grad_(True)
+    rng = np.random.default_rng(11)
+    lU, lB = rng.standard_normal((8, N, N)), rng.standard_normal((2, N, N))
+    sim.adjoint_enable(True)
+    sim.step()
+    # seeds: interior entries only (ghost cells are copies, not state)
+    sim.adjoint_seed("U", interior_only(K.to_blocks(lU, ic)))
+    sim.adjoint_seed("Bi", interior_only(K.to_blocks(lB, ic)))
+    sim.adjoint_step()
+    gU = K.from_blocks(sim.adjoint_read("U"), ic)
+    gB = K.from_blocks(sim.adjoint_read("Bi"), ic)
+    U1, Bx1, By1 = K.step(U0, Bx0, By0, DT, GAMMA, 1.0 / N)
+    L = (torch.from_numpy(lU) * U1).sum() + (torch.from_numpy(lB[0]) * Bx1).sum() + \
+        (torch.from_numpy(lB[1]) * By1).sum()
+    L.backward()
+    for k in range(8):
+        ref = U0.grad[k].numpy()
+        err = np.abs(gU[k] - ref).max() / (np.abs(ref).max() + 1e-300)
+        assert err < 1e-10, (k, err)
+    for d, ref in enumerate((Bx0.grad.numpy(), By0.grad.numpy())):
+        err = np.abs(gB[d] - ref).max() / np.abs(ref).max()
+        assert err < 1e-10, (d, err)
+    # the state went back to the checkpoint
+    assert sim.info()["steps"] == 3 and sim.adjoint_recorded() == 0
+
+
+@pytest.mark.gpu
+def test_kh_gradient_fd_and_reference(gpu):
+    """d(loss)/d(a_k) of the 200-step KH problem: adjoint vs central finite
+    differences (h = 1e-6, agreement 1e-5) and vs the FP64 autograd reference."""
+    steps = 200
+    sim, c = kh_sim(gpu)
+    ic = sim.tree()[1]
+    B0 = sim.download("Bi")
+    gi, gj = block_index(ic)
+    mask = interior_only(K.to_blocks(K.box_mask().numpy()[None], ic)[:, 0])
+    a0 = torch.tensor(list(c.ic_param[:16]), dtype=torch.float64)
+
+    def loss_of(a):
+        U, _, _ = K.kh_ic(a)
+        return KHLoss.apply(blocks_of(U, gi, gj), sim, B0, steps, mask)
+
+    a = a0.clone().requires_grad_(True)
+    L = loss_of(a)
+    L.backward()
+    g_adj = a.grad.numpy().copy()
+    assert np.all(np.isfinite(g_adj)) and np.abs(g_adj).max() > 0
+    # central differences
+    h = 1e-6
+    g_fd = np.zeros(16)
+    with torch.no_grad():
+        for k in range(16):
+            e = torch.zeros(16, dtype=torch.float64)
+            e[k] = h
+            g_fd[k] = (float(loss_of(a0 + e)) - float(loss_of(a0 - e))) / (2 * h)
+    scale = np.abs(g_fd).max()
+    assert np.abs(g_adj - g_fd).max() <= 1e-5 * scale, (g_adj, g_fd)
+    # FP64 reference gradient: autograd through the restatement
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    ar = a0.clone().to(dev).requires_grad_(True)
+    U, Bx, By = K.kh_ic(ar)
+    for _ in range(steps):
+        U, Bx, By = K.step(U, Bx, By, DT, GAMMA, 1.0 / N)
+    Lr = (U[0] * K.box_mask(device=dev)).sum()
+    Lr.backward()
+    g_ref = ar.grad.cpu().numpy()
+    assert abs(float(Lr) - float(L)) <= 1e-12 * abs(float(L))
+    assert np.abs(g_adj - g_ref).max() <= 1e-8 * np.abs(g_ref).max(), (g_adj, g_ref)
