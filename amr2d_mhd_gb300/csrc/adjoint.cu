@@ -44,8 +44,8 @@ int Engine::adjoint_supported() {
 int Engine::adjoint_alloc() {
   const size_t cell = sizeof(double) * 8 * nn_ * cap_slots_, face = sizeof(double) * 2 * nn_ * cap_slots_;
   const size_t edge = sizeof(double) * nn_ * cap_slots_;
-  for (DevBuf *b : {&a_U_, &a_Us_, &a_F_, &a_G_, &a_L_[0], &a_L_[1], &a_R_[0], &a_R_[1], &t_W1_, &t_UsPre_,
-                    &t_UPre_}) {
+  for (DevBuf *b : {&a_U_, &a_Us_, &a_F_, &a_G_, &a_C_[0], &a_C_[1], &a_C_[2], &a_C_[3], &a_C_[4], &a_C_[5],
+                    &a_C_[6], &a_C_[7], &t_W1_, &t_UsPre_, &t_UPre_}) {
     CK(b->ensure(cell), "adjoint alloc");
     CK(cudaMemsetAsync(b->p, 0, cell, stream_), "memset");
   }
@@ -66,6 +66,7 @@ int Engine::adjoint_enable(bool on) {
     CK(cudaStreamSynchronize(stream_), "sync");
   }
   adj_on_ = on;
+  adj_gen_ = 0;  // the adjoint arrays may have moved: capture again
   ckpt_meta_.clear();
   for (DevBuf &b : ckpt_) b.release();
   ckpt_.clear();
@@ -177,8 +178,7 @@ int Engine::ghost_adj(std::initializer_list<AdjSeg> what) {
     s.f32 = 0;
   }
   g.nseg = q;
-  CK(a_take_.ensure(sizeof(double) * 8 * kMaxSeg * static_cast<size_t>(nops_)), "alloc");
-  g.take = a_take_.as<double>();
+  g.take = a_take_.as<double>();  // sized by adjoint_step
   const size_t n = static_cast<size_t>(g.nops) * g.nseg;
   k_ghost_adj_take<G2::N><<<blocks_for(n, 256), 256, 0, stream_>>>(g);
   k_ghost_adj_give<G2::N><<<blocks_for(n, 256), 256, 0, stream_>>>(g);
@@ -227,10 +227,10 @@ int Engine::adjoint_sequence() {
     s.aF = aF;
     s.aG = aG;
     s.aB = step == 1 ? aB : aBs;
-    for (int d = 0; d < 2; d++) { s.aL[d] = a_L_[d].as<double>(); s.aR[d] = a_R_[d].as<double>(); }
+    for (int d = 0; d < 2; d++)
+      for (int q = 0; q < 4; q++) s.C[d][q] = a_C_[4 * d + q].as<double>();
     return s;
   };
-  const size_t ncell8 = static_cast<size_t>(nt) * 8 * G2::NN;
   const size_t nface = static_cast<size_t>(nt) * 2 * G2::NF * G2::NF;
   const size_t ncell = static_cast<size_t>(nt) * G2::NN;
   int rc;
@@ -255,17 +255,20 @@ int Engine::adjoint_sequence() {
       if ((rc = ghost_adj({{FILL_FC, aB, 2}, {FILL_FC, aF, 8}, {FILL_FC, aG, 8}}))) return rc;
     }
     const StageAdjArgs s = st_args(step);
-    k_resid_adj_faces<kNG><<<blocks_for(ncell8, 256), 256, 0, stream_>>>(s);
-    k_resid_adj_cells<kNG><<<blocks_for(ncell8, 256), 256, 0, stream_>>>(s);
     k_faces_adj<kNG><<<blocks_for(nface, 128), 128, 0, stream_>>>(s);
-    k_muscl_prim_adj<kNG><<<blocks_for(ncell, 256), 256, 0, stream_>>>(s);
+    k_cells_adj<kNG><<<blocks_for(ncell, 256), 256, 0, stream_>>>(s);
     CK(cudaGetLastError(), "adjoint kernels");
-    prof_.launches += 8;
+    prof_.launches += 6;
     CK(cudaMemsetAsync(aF, 0, cell, stream_), "memset");
     CK(cudaMemsetAsync(aG, 0, cell, stream_), "memset");
   }
   // the first fills of the step (U and Bi)
   return ghost_adj({{FILL_CC, aU, 8}, {FILL_FC, aB, 2}});
+}
+
+int Engine::adjoint_enqueue() {
+  if (int rc = adjoint_recompute()) return rc;
+  return adjoint_sequence();
 }
 
 // One step back: restore the last checkpoint, recompute that step with its
@@ -286,10 +289,33 @@ int Engine::adjoint_step() {
     inst_[q].dtn = c.meta[q].dtn;
   }
   if (int rc = upload_params()) return rc;
+  CK(a_take_.ensure(sizeof(double) * 8 * kMaxSeg * static_cast<size_t>(nops_ > 0 ? nops_ : 1)), "alloc");
   CK(cudaMemcpyAsync(U_, d.p, u, cudaMemcpyDeviceToDevice, stream_), "restore");
   CK(cudaMemcpyAsync(Bi_, static_cast<char *>(d.p) + u, b, cudaMemcpyDeviceToDevice, stream_), "restore");
-  if (int rc = adjoint_recompute()) return rc;
-  if (int rc = adjoint_sequence()) return rc;
+  if (!graph_on_ || prof_on_) {
+    if (int rc = adjoint_enqueue()) return rc;
+  } else {
+    if (!adj_exec_ || adj_gen_ != gen_) {  // capture once per tree and pool
+      if (adj_exec_) { cudaGraphExecDestroy(adj_exec_); adj_exec_ = nullptr; }
+      cudaStream_t user = stream_;
+      stream_ = cap_stream_;
+      cudaError_t e = cudaStreamBeginCapture(cap_stream_, cudaStreamCaptureModeRelaxed);
+      if (e != cudaSuccess) { stream_ = user; return cuda_fail(e, "graph capture"); }
+      capturing_ = true;
+      int rc = adjoint_enqueue();
+      capturing_ = false;
+      cudaGraph_t g = nullptr;
+      e = cudaStreamEndCapture(cap_stream_, &g);
+      stream_ = user;
+      if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+      if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+      e = cudaGraphInstantiate(&adj_exec_, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { adj_exec_ = nullptr; return cuda_fail(e, "graph instantiate"); }
+      adj_gen_ = gen_;
+    }
+    CK(cudaGraphLaunch(adj_exec_, stream_), "graph launch");
+  }
   CK(cudaMemcpyAsync(U_, d.p, u, cudaMemcpyDeviceToDevice, stream_), "restore");
   CK(cudaMemcpyAsync(Bi_, static_cast<char *>(d.p) + u, b, cudaMemcpyDeviceToDevice, stream_), "restore");
   if (int rc = check_device_error()) return rc;

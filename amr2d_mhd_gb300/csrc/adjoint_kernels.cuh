@@ -188,96 +188,63 @@ struct StageAdjArgs {
   const double *B;     // face field the stage read
   double *aOut;        // adjoint of the stage output (Us or U)
   double *aIn;         // adjoint of the stage input (U or Us)
-  double *aPrev;       // stage 2: adjoint of the old U (in place); else null
-  double *aF, *aG;     // flux adjoints (pre-fill)
+  const double *aF, *aG;  // flux adjoints after the transposed fill (pre-fill fluxes)
   double *aB;          // adjoint of B (normal face components)
-  double *aL[2], *aR[2];  // face-state adjoints: [x|y] left / right states [slot][8][NN]
+  // per face and variable, the adjoint reaching the primitive state of the
+  // stencil cells m-1, m, m+1, m+2 of the face m+1/2: C[dir][q], [slot][8][NN],
+  // stored at the face position (cell m+1)
+  double *C[2][4];
 };
 
-// the residual (main.cpp:147-157) transposed onto the fluxes: face p of a
-// row receives inv_dx * (ares(p-1) - ares(p)), ares = -s dt aOut on [LO, HI]^2
-template <int NG>
-__global__ void k_resid_adj_faces(StageAdjArgs a) {
-  using G = Geo<NG>;
-  constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
-  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= static_cast<size_t>(a.ntasks) * 8 * NN) return;
-  const int t = static_cast<int>(e / (8 * NN)), r = static_cast<int>(e % (8 * NN));
-  const int c = r % NN, i = c % N, j = c / N;
-  const LeafTask task = a.tasks[t];
-  const size_t idx = static_cast<size_t>(task.slot) * 8 * NN + r;
-  const double s = a.step == 1 ? 1.0 : 0.5;
-  const double dt = a.inst[task.inst].dt;
-  auto ares = [&](int ii, int jj) -> double {
-    if (ii < LO || ii > HI || jj < LO || jj > HI) return 0.0;
-    return -s * dt * a.aOut[idx + (jj - j) * N + (ii - i)];
-  };
-  const double fx = task.inv_dx != 0.0 ? task.inv_dx : 1.0 / task.dx;
-  const double fy = task.inv_dy != 0.0 ? task.inv_dy : 1.0 / task.dy;
-  a.aF[idx] += (ares(i - 1, j) - ares(i, j)) * fx;
-  a.aG[idx] += (ares(i, j - 1) - ares(i, j)) * fy;
-}
-
-// the RK combine (main.cpp:260-270 / 292-302) transposed onto the states
-template <int NG>
-__global__ void k_resid_adj_cells(StageAdjArgs a) {
-  constexpr int NN = Geo<NG>::NN;
-  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= static_cast<size_t>(a.ntasks) * 8 * NN) return;
-  const int t = static_cast<int>(e / (8 * NN)), r = static_cast<int>(e % (8 * NN));
-  const size_t idx = static_cast<size_t>(a.tasks[t].slot) * 8 * NN + r;
-  const double o = a.aOut[idx];
-  if (a.step == 1) {          // Us = U - dt res
-    a.aIn[idx] += o;
-    a.aOut[idx] = 0.0;
-  } else {                    // U' = (U + Us - dt res) / 2
-    a.aIn[idx] += 0.5 * o;
-    a.aOut[idx] = 0.5 * o;    // the old U is the array U' overwrote
-  }
-}
-
-// MC / minmod limiter and its derivative in r (slopelimiter.cpp:14-27),
+// MC / minmod limiter value and its derivative in r (slopelimiter.cpp:14-27),
 // following the branch the forward takes
 __device__ __forceinline__ double limiter_d(int lim, double r, double &d) {
   if (lim == LIM_MC) {
     const double a = 2.0 * r, b = 0.5 * (1.0 + r);
     const double c = mmin(a, b), dc = a < b ? 2.0 : 0.5;
     const double e = mmin(c, 2.0), de = c < 2.0 ? dc : 0.0;
-    const double ph = mmax(0.0, e);
     d = 0.0 > e ? 0.0 : de;
-    return ph;
+    return mmax(0.0, e);
   }
-  // minmod
-  const double e = mmin(1.0, r), de = 1.0 < r ? 0.0 : 1.0;
+  const double e = mmin(1.0, r), de = 1.0 < r ? 0.0 : 1.0;  // minmod
   d = 0.0 > e ? 0.0 : de;
   return mmax(0.0, e);
 }
 
-// d(left, right)/d(W[m-1], W[m], W[m+1], W[m+2]) of the face m+1/2
-// (celledges.cpp:38-43, muscl_face in physics.cuh)
-__device__ __forceinline__ void muscl_face_jac(int lim, double wm, double w0, double w1, double w2,
-                                               double jl[3], double jr[3]) {
+// celledges.cpp:38-43 for one variable of the face m+1/2 (the states of
+// muscl_face, same operations) and their derivatives with respect to
+// W[m-1], W[m], W[m+1], W[m+2]: left = l0 W[m-1] + l1 W[m] + l2 W[m+1] to
+// first order, right = r0 W[m] + r1 W[m+1] + r2 W[m+2]
+struct FaceJac { double left, right, l0, l1, l2, r0, r1, r2; };
+
+__device__ __forceinline__ FaceJac muscl_face_jac(int lim, double wm, double w0, double w1, double w2) {
   const double E = 1.0E-15;
   const double dA = w0 - wm, dB = w1 - w0, dC = w2 - w1;
-  double dphi;
-  double r = limiter_ratio<double>(lim, dB, dA + E);
-  double phi = limiter_d(lim, r, dphi);
-  // left = w0 + phi dA / 2
-  double q = 0.5 * dA * dphi;
-  double ldA = 0.5 * phi - q * dB / ((dA + E) * (dA + E));
-  double ldB = q / (dA + E);
-  jl[0] = -ldA;               // W[m-1]
-  jl[1] = 1.0 + ldA - ldB;    // W[m]
-  jl[2] = ldB;                // W[m+1]
-  // right = w1 - phi' dC / 2
-  r = limiter_ratio<double>(lim, dB, dC + E);
-  phi = limiter_d(lim, r, dphi);
-  q = 0.5 * dC * dphi;
-  const double rdC = -(0.5 * phi - q * dB / ((dC + E) * (dC + E)));
-  const double rdB = -q / (dC + E);
-  jr[0] = -rdB;               // W[m]
-  jr[1] = 1.0 + rdB - rdC;    // W[m+1]
-  jr[2] = rdC;                // W[m+2]
+  FaceJac J;
+  double d;
+  double phi = limiter_d(lim, limiter_ratio<double>(lim, dB, dA + E), d);
+  J.left = w0 + 0.5 * phi * dA;
+  double ldA = 0.5 * phi, ldB = 0.0;
+  if (d != 0.0) {  // d/d(dA), d/d(dB) of phi(dB / (dA + E)) dA / 2
+    const double inv = 1.0 / (dA + E), q = 0.5 * dA * d;
+    ldA -= q * dB * inv * inv;
+    ldB = q * inv;
+  }
+  J.l0 = -ldA;
+  J.l1 = 1.0 + ldA - ldB;
+  J.l2 = ldB;
+  phi = limiter_d(lim, limiter_ratio<double>(lim, dB, dC + E), d);
+  J.right = w1 - 0.5 * phi * dC;
+  double rdC = -0.5 * phi, rdB = 0.0;
+  if (d != 0.0) {
+    const double inv = 1.0 / (dC + E), q = 0.5 * dC * d;
+    rdC += q * dB * inv * inv;
+    rdB = -q * inv;
+  }
+  J.r0 = -rdB;
+  J.r1 = 1.0 + rdB - rdC;
+  J.r2 = rdC;
+  return J;
 }
 
 // Reverse of side_state + fast_speed (riemannS.cpp:59-108, misc.cpp:71-79)
@@ -347,44 +314,60 @@ __device__ __forceinline__ void rusa_adj(const double *wL, const double *wR, dou
   side_adj(wR, g, lF, lqR, lb, lwR);
 }
 
-// MUSCL2D.cpp:24-116 + riemannS transposed for one face: the flux adjoints
-// become adjoints of the two reconstructed states (stored per face) and of
-// the normal face field (added to aB)
+// MUSCL2D.cpp:24-116 + riemannS + the residual (main.cpp:147-157)
+// transposed for one face: the flux adjoint (from CT2D through the fill, plus
+// the residual of the face's two cells) becomes the adjoint of the two
+// reconstructed states, of the normal face field (added to aB) and, through
+// the MUSCL Jacobian, of the primitive state of the four stencil cells (C).
 template <int NG>
 __global__ void __launch_bounds__(128) k_faces_adj(StageAdjArgs a) {
   using G = Geo<NG>;
-  constexpr int N = G::N, NN = G::NN, LO = G::LO, NF = G::NF, PER = 2 * NF * NF;
+  constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI, NF = G::NF, PER = 2 * NF * NF;
   const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= static_cast<size_t>(a.ntasks) * PER) return;
   const int t = static_cast<int>(e / PER), f = static_cast<int>(e % PER);
   const LeafTask task = a.tasks[t];
-  const double gamma = a.inst[task.inst].gamma;
-  const int lim = a.inst[task.inst].limiter;
+  const InstParams ip = a.inst[task.inst];
+  const int lim = ip.limiter;
   const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
   const double *W = a.W + base;
   const bool yf = f >= NF * NF;
   const int gi = yf ? f - NF * NF : f;
   const int r = gi / NF, c = gi % NF;
   const int s = yf ? N : 1;
-  const int cL = (LO + r) * N + (LO + c);
+  const int cL = (LO + r) * N + (LO + c);   // cell m of the face m+1/2
   const int kn = yf ? 6 : 5;
   const int fpos = cL + s;
   const double bn = a.B[static_cast<size_t>(task.slot) * 2 * NN + (yf ? NN : 0) + fpos];
   double wl[8], wr[8];
+  FaceJac J[8];
 #pragma unroll
   for (int k = 0; k < 8; k++) {
     if (k == kn) { wl[k] = wr[k] = bn; continue; }
     const double *w = W + k * NN + cL;
-    const double wm = w[-s], w0 = w[0], w1 = w[s], w2 = w[2 * s];
-    muscl_face<double>(lim, w0, w1, w0 - wm, w1 - w0, w2 - w1, 0.0, wl[k], wr[k]);
+    J[k] = muscl_face_jac(lim, w[-s], w[0], w[s], w[2 * s]);
+    wl[k] = J[k].left;
+    wr[k] = J[k].right;
   }
+  // flux adjoint: CT2D part after the fill, plus the residual of cells m
+  // (+1/h) and m+1 (-1/h) when they lie in [LO, HI]
+  const double sdt = (a.step == 1 ? 1.0 : 0.5) * ip.dt;
+  const double h = yf ? (task.inv_dy != 0.0 ? task.inv_dy : 1.0 / task.dy)
+                      : (task.inv_dx != 0.0 ? task.inv_dx : 1.0 / task.dx);
+  const int m = LO + (yf ? r : c);          // cell index along the face normal
+  const bool hi_in = m + 1 <= HI;
   const double *af = (yf ? a.aG : a.aF) + base + fpos;
+  const double *ao = a.aOut + base + cL;
   double lf[8];
 #pragma unroll
-  for (int k = 0; k < 8; k++) lf[k] = af[k * NN];
+  for (int k = 0; k < 8; k++) {
+    const double r0 = -sdt * ao[k * NN];
+    const double r1 = hi_in ? -sdt * ao[k * NN + s] : 0.0;
+    lf[k] = af[k * NN] + (r0 - r1) * h;
+  }
   double lwl[8], lwr[8];
   if (!yf) {
-    rusa_adj(wl, wr, gamma, lf, lwl, lwr);
+    rusa_adj(wl, wr, ip.gamma, lf, lwl, lwr);
   } else {  // riemannS.cpp:12-23 / 47-55: swap (u, v) and (Bx, By)
     double l2[8], r2[8], f2[8], a2[8], b2[8];
 #pragma unroll
@@ -392,7 +375,7 @@ __global__ void __launch_bounds__(128) k_faces_adj(StageAdjArgs a) {
     l2[1] = wl[2]; l2[2] = wl[1]; r2[1] = wr[2]; r2[2] = wr[1];
     l2[5] = wl[6]; l2[6] = wl[5]; r2[5] = wr[6]; r2[6] = wr[5];
     f2[1] = lf[2]; f2[2] = lf[1]; f2[5] = lf[6]; f2[6] = lf[5];
-    rusa_adj(l2, r2, gamma, f2, a2, b2);
+    rusa_adj(l2, r2, ip.gamma, f2, a2, b2);
 #pragma unroll
     for (int k = 0; k < 8; k++) { lwl[k] = a2[k]; lwr[k] = b2[k]; }
     lwl[1] = a2[2]; lwl[2] = a2[1]; lwr[1] = b2[2]; lwr[2] = b2[1];
@@ -400,20 +383,27 @@ __global__ void __launch_bounds__(128) k_faces_adj(StageAdjArgs a) {
   }
   // the normal component of both states is the face field (MUSCL2D.cpp:48-51)
   a.aB[static_cast<size_t>(task.slot) * 2 * NN + (yf ? NN : 0) + fpos] += lwl[kn] + lwr[kn];
-  double *oL = a.aL[yf ? 1 : 0] + base + fpos, *oR = a.aR[yf ? 1 : 0] + base + fpos;
+  const int d = yf ? 1 : 0;
+  double *c0 = a.C[d][0] + base + fpos, *c1 = a.C[d][1] + base + fpos;
+  double *c2 = a.C[d][2] + base + fpos, *c3 = a.C[d][3] + base + fpos;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    oL[k * NN] = k == kn ? 0.0 : lwl[k];
-    oR[k * NN] = k == kn ? 0.0 : lwr[k];
+    if (k == kn) continue;
+    const double L = lwl[k], R = lwr[k];
+    c0[k * NN] = J[k].l0 * L;                  // cell m-1
+    c1[k * NN] = J[k].l1 * L + J[k].r0 * R;    // cell m
+    c2[k * NN] = J[k].l2 * L + J[k].r1 * R;    // cell m+1
+    c3[k * NN] = J[k].r2 * R;                  // cell m+2
   }
 }
 
-// Gathers, per cell, the adjoint of its primitive state from the face-state
-// adjoints of the (up to 12) faces whose reconstruction read it, then applies
-// the transpose of U2W (meshblock.cpp:119-145) and adds the result to aIn.
-// Face m+1/2 of a row (left cell m, m in [LO, HI]) reads W[m-1 .. m+2].
+// Per cell: the primitive-state adjoint gathered from the (up to 8) faces
+// whose reconstruction read the cell, the transpose of U2W
+// (meshblock.cpp:119-145) added to aIn, and the RK combine
+// (main.cpp:260-270 / 292-302) transposed (aIn += s aOut; aOut -> the old
+// state's adjoint).  Face m+1/2 (m in [LO, HI]) gives cell m-1+q its C[q].
 template <int NG>
-__global__ void __launch_bounds__(256) k_muscl_prim_adj(StageAdjArgs a) {
+__global__ void __launch_bounds__(256) k_cells_adj(StageAdjArgs a) {
   using G = Geo<NG>;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
   const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -422,42 +412,45 @@ __global__ void __launch_bounds__(256) k_muscl_prim_adj(StageAdjArgs a) {
   const int i = c % N, j = c / N;
   const LeafTask task = a.tasks[t];
   const double gamma = a.inst[task.inst].gamma;
-  const int lim = a.inst[task.inst].limiter;
   const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
-  const double *W = a.W + base;
+  const bool xrow = j >= LO && j <= HI, ycol = i >= LO && i <= HI;
+  // faces m = pos + 1 - q: valid when LO <= m <= HI
+  bool vx[4], vy[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    vx[q] = xrow && i + 1 - q >= LO && i + 1 - q <= HI;
+    vy[q] = ycol && j + 1 - q >= LO && j + 1 - q <= HI;
+  }
   double lw[8];
-#pragma unroll 1
+#pragma unroll
   for (int k = 0; k < 8; k++) {
     double acc = 0.0;
-    for (int d = 0; d < 2; d++) {       // x faces, then y faces
-      if ((d == 0 && k == 5) || (d == 1 && k == 6)) continue;
-      const int pos = d == 0 ? i : j, row = d == 0 ? j : i, s = d == 0 ? 1 : N;
-      if (row < LO || row > HI) continue;
-      const double *aL = a.aL[d] + base + k * NN, *aR = a.aR[d] + base + k * NN;
-      for (int m = pos - 2; m <= pos + 1; m++) {
-        if (m < LO || m > HI) continue;
-        const int cm = c + (m - pos) * s;   // cell m of this row
-        const double *w = W + k * NN + cm;
-        double jl[3], jr[3];
-        muscl_face_jac(lim, w[-s], w[0], w[s], w[2 * s], jl, jr);
-        const double la = aL[cm + s], ra = aR[cm + s];   // stored at the face position (cell m+1)
-        const int o = pos - m;                            // this cell is W[m + o], o in -1..2
-        if (o >= -1 && o <= 1) acc += jl[o + 1] * la;
-        if (o >= 0 && o <= 2) acc += jr[o] * ra;
-      }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (k != 5 && vx[q]) acc += a.C[0][q][base + k * NN + c + 2 - q];
+      if (k != 6 && vy[q]) acc += a.C[1][q][base + k * NN + c + (2 - q) * N];
     }
     lw[k] = acc;
   }
-  // U2W transposed
+  const double *W = a.W + base;
   const double rho = W[c], u = W[NN + c], v = W[2 * NN + c], z = W[3 * NN + c];
   const double gm = gamma - 1.0;
-  double *ai = a.aIn + base + c;
-  ai[0] += lw[0] - (lw[1] * u + lw[2] * v + lw[3] * z) / rho + lw[4] * gm * 0.5 * (u * u + v * v + z * z);
-  ai[NN] += lw[1] / rho - lw[4] * gm * u;
-  ai[2 * NN] += lw[2] / rho - lw[4] * gm * v;
-  ai[3 * NN] += lw[3] / rho - lw[4] * gm * z;
-  ai[4 * NN] += lw[4] * gm;
-  for (int k = 5; k < 8; k++) ai[k * NN] += lw[k] - lw[4] * gm * W[k * NN + c];
+  double g[8];
+  g[0] = lw[0] - (lw[1] * u + lw[2] * v + lw[3] * z) / rho + lw[4] * gm * 0.5 * (u * u + v * v + z * z);
+  g[1] = lw[1] / rho - lw[4] * gm * u;
+  g[2] = lw[2] / rho - lw[4] * gm * v;
+  g[3] = lw[3] / rho - lw[4] * gm * z;
+  g[4] = lw[4] * gm;
+#pragma unroll
+  for (int k = 5; k < 8; k++) g[k] = lw[k] - lw[4] * gm * W[k * NN + c];
+  const double sk = a.step == 1 ? 1.0 : 0.5;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const size_t idx = base + k * NN + c;
+    const double o = a.aOut[idx];
+    a.aIn[idx] += sk * o + g[k];
+    a.aOut[idx] = a.step == 1 ? 0.0 : 0.5 * o;
+  }
 }
 
 }  // namespace amr

@@ -79,14 +79,16 @@ Engine::~Engine() {
     b->release();
   d_ops_.release();
   d_snaps_.release();
-  for (DevBuf *b : {&a_U_, &a_Us_, &a_B_, &a_Bs_, &a_E_, &a_F_, &a_G_, &a_L_[0], &a_L_[1], &a_R_[0], &a_R_[1],
-                    &a_take_, &t_W1_, &t_B1_, &t_BisF_, &t_UsPre_, &t_BnewF_, &t_UPre_})
+  for (DevBuf *b : {&a_U_, &a_Us_, &a_B_, &a_Bs_, &a_E_, &a_F_, &a_G_, &a_take_, &t_W1_, &t_B1_, &t_BisF_,
+                    &t_UsPre_, &t_BnewF_, &t_UPre_})
     b->release();
+  for (DevBuf &b : a_C_) b.release();
   for (DevBuf &b : ckpt_) b.release();
   for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_, &h_ops_, &h_snaps_, &h_tasks_})
     b->release();
   if (own_stream_ && stream_) cudaStreamDestroy(stream_);
   if (exec_) cudaGraphExecDestroy(exec_);
+  if (adj_exec_) cudaGraphExecDestroy(adj_exec_);
   if (cap_stream_) cudaStreamDestroy(cap_stream_);
   for (cudaEvent_t e : ev_) cudaEventDestroy(e);
   for (GhostCompiler *g : gcs_) delete g;

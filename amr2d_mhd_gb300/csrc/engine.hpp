@@ -177,7 +177,7 @@ class Engine {
   std::vector<Checkpoint> ckpt_meta_;
   std::vector<DevBuf> ckpt_;               // one buffer per recorded step
   size_t ckpt_slots_ = 0;                  // slots each checkpoint holds
-  DevBuf a_U_, a_Us_, a_B_, a_Bs_, a_E_, a_F_, a_G_, a_L_[2], a_R_[2], a_take_;
+  DevBuf a_U_, a_Us_, a_B_, a_Bs_, a_E_, a_F_, a_G_, a_C_[8], a_take_;
   DevBuf t_W1_, t_B1_, t_BisF_, t_UsPre_, t_BnewF_, t_UPre_;
   int adjoint_supported();
   int adjoint_alloc();
@@ -186,6 +186,9 @@ class Engine {
   int adjoint_sequence();
   int ghost_adj(std::initializer_list<AdjSeg> what);
   int ct2d_taped(int step);
+  int adjoint_enqueue();                   // recompute + transposed step on stream_
+  cudaGraphExec_t adj_exec_ = nullptr;     // the same, captured (re-captured when gen_ moves)
+  uint64_t adj_gen_ = 0;
 };
 
 }  // namespace amr
