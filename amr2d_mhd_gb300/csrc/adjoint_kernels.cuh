@@ -222,24 +222,26 @@ __device__ __forceinline__ FaceJac muscl_face_jac(int lim, double wm, double w0,
   const double dA = w0 - wm, dB = w1 - w0, dC = w2 - w1;
   FaceJac J;
   double d;
+  // left = w0 + phi(dB / (dA + E)) dA / 2
   double phi = limiter_d(lim, limiter_ratio<double>(lim, dB, dA + E), d);
   J.left = w0 + 0.5 * phi * dA;
   double ldA = 0.5 * phi, ldB = 0.0;
-  if (d != 0.0) {  // d/d(dA), d/d(dB) of phi(dB / (dA + E)) dA / 2
-    const double inv = 1.0 / (dA + E), q = 0.5 * dA * d;
-    ldA -= q * dB * inv * inv;
-    ldB = q * inv;
+  if (d != 0.0) {
+    const double inv = 1.0 / (dA + E), q = 0.5 * dA * d * inv;
+    ldA -= q * dB * inv;
+    ldB = q;
   }
   J.l0 = -ldA;
   J.l1 = 1.0 + ldA - ldB;
   J.l2 = ldB;
+  // right = w1 - phi(dB / (dC + E)) dC / 2
   phi = limiter_d(lim, limiter_ratio<double>(lim, dB, dC + E), d);
   J.right = w1 - 0.5 * phi * dC;
   double rdC = -0.5 * phi, rdB = 0.0;
   if (d != 0.0) {
-    const double inv = 1.0 / (dC + E), q = 0.5 * dC * d;
-    rdC += q * dB * inv * inv;
-    rdB = -q * inv;
+    const double inv = 1.0 / (dC + E), q = 0.5 * dC * d * inv;
+    rdC += q * dB * inv;
+    rdB = -q;
   }
   J.r0 = -rdB;
   J.r1 = 1.0 + rdB - rdC;
@@ -247,54 +249,76 @@ __device__ __forceinline__ FaceJac muscl_face_jac(int lim, double wm, double w0,
   return J;
 }
 
-// Reverse of side_state + fast_speed (riemannS.cpp:59-108, misc.cpp:71-79)
-// for the normal direction x: adds d/dw of lF.F + lq.q + lcf.cf to lw.
-__device__ __forceinline__ void side_adj(const double *w, double g, const double *lF, const double *lq,
-                                         double lcf, double *lw) {
+// One side of a Rusanov face in the x frame (riemannS.cpp:59-108,
+// misc.cpp:71-79): the conserved state and the intermediates of the fast
+// speed, each evaluated once for the transposed flux.
+struct SideAD {
+  double q[8];
+  double irho, e, pt, A, C, T, D, cf;
+};
+
+__device__ __forceinline__ void side_fwd(const double *w, double g, double ig1, SideAD &S) {
   const double rho = w[0], u = w[1], v = w[2], z = w[3], p = w[4], bx = w[5], by = w[6], bz = w[7];
-  const double b2 = bx * bx + by * by + bz * bz;
-  const double e = p / (g - 1.0) + 0.5 * rho * (u * u + v * v + z * z) + 0.5 * b2;
-  const double pt = p + 0.5 * b2;
+  const double b2 = bx * bx + by * by + bz * bz, t2 = by * by + bz * bz;
+  S.irho = 1.0 / rho;
+  S.e = p * ig1 + 0.5 * rho * (u * u + v * v + z * z) + 0.5 * b2;
+  S.pt = p + 0.5 * b2;
+  S.q[0] = rho; S.q[1] = rho * u; S.q[2] = rho * v; S.q[3] = rho * z;
+  S.q[4] = S.e; S.q[5] = bx; S.q[6] = by; S.q[7] = bz;
+  S.A = g * p * S.irho;
+  S.C = b2 * S.irho;
+  S.T = t2 * S.irho;
+  S.D = sqrt((S.C - S.A) * (S.C - S.A) + 4.0 * S.A * S.T);
+  S.cf = sqrt(0.5 * (S.C + S.A + S.D));
+}
+
+// adds d/dw of lF.F + lq.q + lcf.cf of one side to lw
+__device__ __forceinline__ void side_adj(const double *w, double g, double ig1, const SideAD &S, const double *lF,
+                                         const double *lq, double lcf, double *lw) {
+  const double rho = w[0], u = w[1], v = w[2], z = w[3], bx = w[5], by = w[6], bz = w[7];
   const double le = lq[4] + lF[4] * u;     // adjoint of e
   const double lpt = lF[1] + lF[4] * u;    // adjoint of pt
+  const double v2 = u * u + v * v + z * z;
   double lr = lq[0] + lq[1] * u + lq[2] * v + lq[3] * z + lF[0] * u + lF[1] * u * u + lF[2] * u * v +
-              lF[3] * u * z + le * 0.5 * (u * u + v * v + z * z);
+              lF[3] * u * z + le * 0.5 * v2;
   double lu = rho * (lq[1] + lF[0]) + 2.0 * rho * u * lF[1] + rho * v * lF[2] + rho * z * lF[3] +
-              lF[4] * (e + pt - bx * bx) + lF[6] * by + lF[7] * bz + le * rho * u;
+              lF[4] * (S.e + S.pt - bx * bx) + lF[6] * by + lF[7] * bz + le * rho * u;
   double lv = rho * lq[2] + rho * u * lF[2] - lF[4] * bx * by - lF[6] * bx + le * rho * v;
   double lz = rho * lq[3] + rho * u * lF[3] - lF[4] * bx * bz - lF[7] * bx + le * rho * z;
-  double lp = le / (g - 1.0) + lpt;
-  double lbx = lq[5] + (le + lpt) * bx - 2.0 * bx * lF[1] - by * lF[2] - bz * lF[3] -
+  double lp = le * ig1 + lpt;
+  const double lb = le + lpt;
+  double lbx = lq[5] + lb * bx - 2.0 * bx * lF[1] - by * lF[2] - bz * lF[3] -
                (2.0 * u * bx + v * by + z * bz) * lF[4] - v * lF[6] - z * lF[7];
-  double lby = lq[6] + (le + lpt) * by - bx * lF[2] - bx * v * lF[4] + u * lF[6];
-  double lbz = lq[7] + (le + lpt) * bz - bx * lF[3] - bx * z * lF[4] + u * lF[7];
-  if (lcf != 0.0) {
-    const double A = g * p / rho, C = b2 / rho, T = (by * by + bz * bz) / rho;
-    const double D = sqrt((C - A) * (C - A) + 4.0 * A * T);
-    const double cf = sqrt(0.5 * (C + A + D));
-    const double k = lcf / (4.0 * cf);
+  double lby = lq[6] + lb * by - bx * lF[2] - bx * v * lF[4] + u * lF[6];
+  double lbz = lq[7] + lb * bz - bx * lF[3] - bx * z * lF[4] + u * lF[7];
+  if (lcf != 0.0) {  // cf^2 = (C + A + D) / 2, D^2 = (C - A)^2 + 4 A T
+    const double k = lcf / (4.0 * S.cf);
     double lA = k, lC = k, lT = 0.0;
-    if (D > 0.0) {
-      lA += k * (2.0 * T - (C - A)) / D;
-      lC += k * (C - A) / D;
-      lT = k * 2.0 * A / D;
+    if (S.D > 0.0) {
+      const double kD = k / S.D;
+      lA += kD * (2.0 * S.T - (S.C - S.A));
+      lC += kD * (S.C - S.A);
+      lT = kD * 2.0 * S.A;
     }
-    lr += -(A * lA + C * lC + T * lT) / rho;
-    lp += g * lA / rho;
-    lbx += 2.0 * bx * lC / rho;
-    lby += 2.0 * by * (lC + lT) / rho;
-    lbz += 2.0 * bz * (lC + lT) / rho;
+    lr -= (S.A * lA + S.C * lC + S.T * lT) * S.irho;
+    lp += g * lA * S.irho;
+    const double c2 = 2.0 * lC * S.irho, ct = 2.0 * (lC + lT) * S.irho;
+    lbx += bx * c2;
+    lby += by * ct;
+    lbz += bz * ct;
   }
   lw[0] += lr; lw[1] += lu; lw[2] += lv; lw[3] += lz;
   lw[4] += lp; lw[5] += lbx; lw[6] += lby; lw[7] += lbz;
 }
 
-// riemannS.cpp:58-116 (Rusanov) transposed for one face in the x frame
+// riemannS.cpp:58-116 (Rusanov) transposed for one face in the x frame:
+// f = (FL + FR)/2 - max(cfL + |uL|, cfR + |uR|) (qR - qL)/2
 __device__ __forceinline__ void rusa_adj(const double *wL, const double *wR, double g, const double *lf,
                                          double *lwL, double *lwR) {
-  Side<double> L, R;
-  side_state<double>(wL, g, L);
-  side_state<double>(wR, g, R);
+  const double ig1 = 1.0 / (g - 1.0);
+  SideAD L, R;
+  side_fwd(wL, g, ig1, L);
+  side_fwd(wR, g, ig1, R);
   const double a = L.cf + fabs(wL[1]), b = R.cf + fabs(wR[1]);
   const double im = smax(a, b);
   double lF[8], lqL[8], lqR[8], lim = 0.0;
@@ -310,8 +334,8 @@ __device__ __forceinline__ void rusa_adj(const double *wL, const double *wR, dou
   for (int k = 0; k < 8; k++) { lwL[k] = 0.0; lwR[k] = 0.0; }
   lwL[1] += la * sgn(wL[1]);
   lwR[1] += lb * sgn(wR[1]);
-  side_adj(wL, g, lF, lqL, la, lwL);
-  side_adj(wR, g, lF, lqR, lb, lwR);
+  side_adj(wL, g, ig1, L, lF, lqL, la, lwL);
+  side_adj(wR, g, ig1, R, lF, lqR, lb, lwR);
 }
 
 // MUSCL2D.cpp:24-116 + riemannS + the residual (main.cpp:147-157)
