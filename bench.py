@@ -225,6 +225,8 @@ def run_ours(args):
         sim.close()
     if not args.no_batch:
         results["batch"] = run_batch(stream, args.batch_steps, args.batch_advance)
+    if not args.no_adjoint:
+        results["adjoint"] = run_adjoint(stream)
     return results, world, rank
 
 
@@ -279,6 +281,114 @@ def run_batch(stream, steps, advance):
         v.close()
     out["l1_rel_density_fp32_vs_fp64_max"] = max(l1)
     return out
+
+
+KH_SEED = 42
+
+
+def kh_u0(a, icoord, gamma=5.0 / 3.0, n=256, ng=2, nb=16):
+    """Block-layout conserved state of the KH problem with amplitudes a (the
+    IC of amr_config_kh, evaluated here so it can be perturbed)."""
+    N = nb + 2 * ng
+    idx = np.arange(N) - ng
+    U = np.zeros((len(icoord), 8, N, N))
+    k = np.arange(1, 17)
+    for b, (x0, y0) in enumerate(icoord):
+        x = (((x0 + idx) % n) + 0.5) / n
+        y = (((y0 + idx) % n) + 0.5) / n
+        Y, X = np.meshgrid(y, x, indexing="ij")   # [j][i]
+        inside = np.abs(Y - 0.5) <= 0.25
+        rho = np.where(inside, 2.0, 1.0)
+        u = np.where(inside, 0.5, -0.5)
+        env = np.exp(-(Y - 0.25) ** 2 / 0.01) + np.exp(-(Y - 0.75) ** 2 / 0.01)
+        v = np.tensordot(a, np.sin(2.0 * np.pi * k[:, None, None] * X[None]), axes=1) * env
+        bx = 0.1 / np.sqrt(4.0 * np.pi)
+        U[b, 0], U[b, 1], U[b, 2] = rho, rho * u, rho * v
+        U[b, 4] = 2.5 / (gamma - 1) + 0.5 * rho * (u * u + v * v) + 0.5 * bx * bx
+        U[b, 5] = bx
+    return U
+
+
+def run_adjoint(stream, steps=200):
+    """Gradient of the KH loss (total density in [0.4,0.6]^2 after `steps`
+    steps of dt 2e-4 on the frozen 256^2 periodic mesh) w.r.t. the 16
+    perturbation amplitudes: adjoint cost against a forward step, and the
+    gradient against central differences (h = 1e-7)."""
+    import torch
+
+    import amr2d_mhd_gb300 as amr
+    c = amr.kh_config(KH_SEED)
+    c.t_end = 1e9
+    a0 = np.array(c.ic_param[:16])
+    sim = amr.Simulation(c)
+    sim.set_stream(stream.cuda_stream)
+    sim.init()
+    ic = sim.tree()[1]
+    B0 = sim.download("Bi")
+    ng, nb = 2, 16
+    mask = np.zeros((len(ic), 20, 20))
+    cc = (np.arange(20) - ng + 0.5)
+    for b, (x0, y0) in enumerate(ic):
+        x = (x0 + cc) / 256.0
+        y = (y0 + cc) / 256.0
+        inx, iny = (x >= 0.4) & (x <= 0.6), (y >= 0.4) & (y <= 0.6)
+        m = np.outer(iny, inx).astype(float) / 256.0 ** 2
+        m[:ng, :] = 0; m[-ng:, :] = 0; m[:, :ng] = 0; m[:, -ng:] = 0
+        mask[b] = m
+
+    def forward(a, record=False):
+        sim.upload("U", kh_u0(a, ic))
+        sim.upload("Bi", B0)
+        sim.adjoint_enable(record)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.run(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        U = sim.download("U")
+        return float((U[:, 0] * mask).sum()), e0.elapsed_time(e1)
+
+    forward(a0)                                   # warm-up (graph capture)
+    _, fwd_ms = forward(a0)
+    L, rec_ms = forward(a0, record=True)
+    lam = np.zeros((len(ic), 8, 20, 20))
+    lam[:, 0] = mask
+    sim.adjoint_seed("U", lam)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        sim.adjoint_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    adj_ms = e0.elapsed_time(e1)
+    gU = sim.adjoint_read("U")
+    # chain rule through the IC: U2 = rho v, U4 = ... + rho v^2 / 2
+    k = np.arange(1, 17)
+    g = np.zeros(16)
+    for b, (x0, y0) in enumerate(ic):
+        x = (((x0 + np.arange(20) - ng) % 256) + 0.5) / 256
+        y = (((y0 + np.arange(20) - ng) % 256) + 0.5) / 256
+        Y, X = np.meshgrid(y, x, indexing="ij")
+        inside = np.abs(Y - 0.5) <= 0.25
+        rho = np.where(inside, 2.0, 1.0)
+        env = np.exp(-(Y - 0.25) ** 2 / 0.01) + np.exp(-(Y - 0.75) ** 2 / 0.01)
+        basis = np.sin(2.0 * np.pi * k[:, None, None] * X[None]) * env    # dv/da_k
+        v = np.tensordot(a0, basis, axes=1)
+        w = gU[b, 2] * rho + gU[b, 4] * rho * v
+        g += (basis * w[None]).sum(axis=(1, 2))
+    h = 1e-7
+    fd = np.zeros(16)
+    for q in range(16):
+        e = np.zeros(16)
+        e[q] = h
+        fd[q] = (forward(a0 + e)[0] - forward(a0 - e)[0]) / (2 * h)
+    sim.close()
+    return dict(forward_ms_per_step=fwd_ms / steps, recording_ms_per_step=rec_ms / steps,
+                adjoint_ms_per_step=adj_ms / steps, cost_ratio=adj_ms / fwd_ms, loss=L,
+                grad_max_abs=float(np.abs(g).max()),
+                fd_max_rel_diff=float(np.abs(g - fd).max() / np.abs(fd).max()))
 
 
 def cpu_baseline(steps, threads):
@@ -341,6 +451,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=40, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the blast-batch measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--batch-advance", type=int, default=120)
     ap.add_argument("--ncu-case", type=int, default=0,
@@ -415,6 +526,12 @@ def main():
             "fp32_vs_plain_fp64_rotor": res["batch"]["fp32"]["value"] / value,
             "l1_rel_density_fp32_vs_fp64_max": res["batch"]["l1_rel_density_fp32_vs_fp64_max"],
             "l1_sample": "4 instances of the batch (maxlevs capped at 4) run to t = 0.1, finest uniform grid"},
+        "adjoint": None if "adjoint" not in res else dict(
+            workload="Kelvin-Helmholtz, frozen 256^2 periodic mesh (256 blocks), gamma 5/3, MUSCL-MC + RUSA + CT, "
+                     "RK2, 200 steps of dt 2e-4, loss = total density in [0.4,0.6]^2, gradient w.r.t. the 16 "
+                     "amplitudes (seed %d); cost ratio = adjoint incl. recompute / plain forward, per step; "
+                     "fd = central differences h = 1e-7 (first-order error from MC kinks)" % KH_SEED,
+            **res["adjoint"]),
         "cpu_baseline": cpu,
         "clocks": {"sm_mhz": clk.get("sm_mhz"), "sm_max_mhz": clk.get("sm_max_mhz"), "reasons": clk.get("reasons", [])},
         "gpu_launches": int(prof["launches"]),

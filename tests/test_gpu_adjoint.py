@@ -148,7 +148,7 @@ def test_kh_gradient_fd_and_reference(gpu):
     Lr.backward()
     g_ref = ar.grad.cpu().numpy()
     del U, Bx, By, Lr
-    assert abs(float(loss_of(a0.clone())) - float(L)) == 0.0   # the forward is deterministic
+    assert float(loss_of(a0.clone()).detach()) == float(L.detach())   # the forward is deterministic
     assert np.abs(g_adj - g_ref).max() <= 1e-9 * np.abs(g_ref).max(), (g_adj, g_ref)
     # central differences at decreasing h
     errs = []
