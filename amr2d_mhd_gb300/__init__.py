@@ -166,6 +166,15 @@ def kh_config(seed, precision="fp64") -> Config:
     return c
 
 
+def ot_config(maxlevs=7, precision="fp64", cfl=0.4) -> Config:
+    """Orszag-Tang vortex on [0, 2 pi]^2, periodic, 4 x 4 roots of 16 x 16,
+    WENO5 + HLLD with 4 ghost layers, gamma 5/3, t_end pi (extension)."""
+    import math
+    return make_config(ic="OT", limiter="WENO5", flux="HLLD", cfl=cfl, maxlevs=maxlevs, nghosts=4, nroots=(4, 4),
+                       periodic=True, geometry=1, gamma=5.0 / 3.0, t_end=math.pi, precision=precision,
+                       lenx=2 * math.pi, leny=2 * math.pi)
+
+
 class Simulation:
     """One handle: an AMR problem (or a batch of them) resident on the GPU.
 

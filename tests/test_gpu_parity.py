@@ -27,6 +27,11 @@ CASES = [
     dict(ic="BWx", limiter="WENO3", flux="RUSA", cfl=0.4, maxlevs=3, steps=20),
     dict(ic="BWx", limiter="WENO5", flux="HLLD", cfl=0.4, maxlevs=3, nghosts=4, steps=20),
     dict(ic="rotor", limiter="WENO5", flux="RUSA", cfl=0.4, maxlevs=3, nghosts=4, steps=20),
+    # Orszag-Tang on [0, 2 pi]^2, periodic, 4 x 4 roots, clean geometry (extension)
+    dict(ic="OT", limiter="WENO5", flux="HLLD", cfl=0.4, maxlevs=3, nghosts=4, nroots=(4, 4), periodic=True,
+         geom_ref=False, lenx=2 * 3.141592653589793, leny=2 * 3.141592653589793, steps=30),
+    dict(ic="OT", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4, nroots=(4, 4), periodic=True,
+         geom_ref=False, lenx=2 * 3.141592653589793, leny=2 * 3.141592653589793, steps=30),
 ]
 
 
