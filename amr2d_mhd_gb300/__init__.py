@@ -29,7 +29,8 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "a
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_adjoint_enable",
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_save4py",
+           "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
            "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
 
 
@@ -108,6 +109,9 @@ def load(build_if_missing: bool = True):
         "amr_profile_enable": (ctypes.c_int, [vp, i32]),
         "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
         "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
+        "amr_save4py": (ctypes.c_int, [vp, i32, i32, ctypes.c_char_p, i32, ctypes.c_char_p, ctypes.c_size_t]),
+        "amr_checkpoint_save": (ctypes.c_int, [vp, ctypes.c_char_p]),
+        "amr_checkpoint_load": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "amr_adjoint_enable": (ctypes.c_int, [vp, i32]),
         "amr_adjoint_seed": (ctypes.c_int, [vp, i32, i32, dp, i64]),
         "amr_adjoint_step": (ctypes.c_int, [vp]),
@@ -301,6 +305,20 @@ class Simulation:
             x0, y0 = ic[b, 0] * r, ic[b, 1] * r
             out[x0:x0 + c.nx * r, y0:y0 + c.ny * r] = np.kron(v, np.ones((r, r)))
         return out
+
+    def save4py(self, directory, id=0, digits=0, instance=0):
+        """savedata.cpp's text output of one instance; returns the file name."""
+        buf = ctypes.create_string_buffer(4096)
+        self._ck(load().amr_save4py(self.h, instance, id, os.fsencode(directory), digits, buf, 4096))
+        return buf.value.decode()
+
+    def checkpoint_save(self, path):
+        self._ck(load().amr_checkpoint_save(self.h, os.fsencode(path)))
+
+    def checkpoint_load(self, path):
+        """Restore a checkpoint instead of init() (same configurations)."""
+        self._ck(load().amr_checkpoint_load(self.h, os.fsencode(path)))
+        return self
 
     # discrete adjoint of the frozen-mesh step
     def adjoint_enable(self, on=True):

@@ -193,6 +193,17 @@ int amr_profile_read(amr_handle *h, amr_profile *o) {
   return guarded(h, [&](amr::Engine &e) { return e.profile_read(o); });
 }
 
+int amr_save4py(amr_handle *h, int32_t inst, int32_t id, const char *dir, int32_t digits, char *name_out,
+                size_t name_len) {
+  return guarded(h, [&](amr::Engine &e) { return e.save4py(inst, id, dir, digits, name_out, name_len); });
+}
+int amr_checkpoint_save(amr_handle *h, const char *path) {
+  return guarded(h, [&](amr::Engine &e) { return e.checkpoint_save(path); });
+}
+int amr_checkpoint_load(amr_handle *h, const char *path) {
+  return guarded(h, [&](amr::Engine &e) { return e.checkpoint_load(path); });
+}
+
 int amr_adjoint_enable(amr_handle *h, int32_t on) {
   return guarded(h, [&](amr::Engine &e) { return e.adjoint_enable(on != 0); });
 }

@@ -86,6 +86,11 @@ class Engine {
   int profile_enable(bool on);
   int profile_read(amr_profile *out);
 
+  // checkpoint / restart and the savedata.cpp writer (checkpoint.cu)
+  int checkpoint_save(const char *path);
+  int checkpoint_load(const char *path);
+  int save4py(int inst, int id, const char *dir, int digits, char *name_out, size_t name_len);
+
   // discrete adjoint of the frozen-mesh step (adjoint.cu)
   int adjoint_enable(bool on);
   int adjoint_seed(int inst, int field, const double *lam, int64_t count);

@@ -517,7 +517,10 @@ def main():
                      "bytes_per_launch": alg_bytes, "launch_ms": stage_ms_avg},
         "fp64_pipe": fp64,
         "fp32": {"value": value32, "speedup_vs_fp64": value32 / value, "l1_rel_density_vs_fp64_at_t_end": l1,
-                 "t_end_fp32": r32["t_end"], "t_end_fp64": r64["t_end"], "ms_per_step": r32["ms"] / args.steps},
+                 "t_end_fp32": r32["t_end"], "t_end_fp64": r64["t_end"], "ms_per_step": r32["ms"] / args.steps,
+                 "host_ms_per_step": (r32["prof"]["host_compile_ms"] + r32["prof"]["host_admesh_ms"]) / args.steps,
+                 "wait_ms_per_step": r32["prof"]["wait_ms"] / args.steps},
+        "host_ms_per_step": (prof["host_compile_ms"] + prof["host_admesh_ms"]) / args.steps,
         "batch": None if "batch" not in res else {
             "workload": "%d seeded cylindrical blasts (seed %d, amr_config_blast): [0,1]^2, gamma 1.4, 4 roots, "
                         "maxlevs U{3..6}, MUSCL-MC + HLLE + CT, CFL 0.2, outflow; %d untimed batch steps, then "

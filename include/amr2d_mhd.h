@@ -179,6 +179,22 @@ typedef struct amr_profile {
 int amr_profile_enable(amr_handle *h, int32_t on);
 int amr_profile_read(amr_handle *h, amr_profile *out);
 
+/* ---- output and restart --------------------------------------------------
+ * amr_save4py writes instance `inst` in the format of save4py
+ * (savedata.cpp:7-46) to <dir>/<IC><id, 3 digits>t_<t>.dat: per leaf block a
+ * "#" header line, then x, y, dx/2, dy/2, rho, u, v, w, p, Bx, By, Bz of
+ * every interior cell in columns of width 16.  digits = 0 keeps the
+ * reference's 6 significant digits; > 0 sets the precision (17 = exact).
+ * The file name is copied to name_out (may be NULL).
+ * amr_checkpoint_save / _load (extension): the whole handle (configurations,
+ * counters, quadtrees, every field) in one binary file; load into a handle
+ * created with the same configurations, in place of amr_init; the run then
+ * continues bit for bit. */
+int amr_save4py(amr_handle *h, int32_t inst, int32_t id, const char *dir, int32_t digits, char *name_out,
+                size_t name_len);
+int amr_checkpoint_save(amr_handle *h, const char *path);
+int amr_checkpoint_load(amr_handle *h, const char *path);
+
 /* ---- discrete adjoint of the frozen-mesh step (no counterpart in the
  * reference) ------------------------------------------------------------------
  * Reverse mode through whole time steps, with a checkpoint of (U, Bi) per

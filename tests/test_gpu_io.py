@@ -1,0 +1,92 @@
+"""Output and restart on the GPU: the savedata.cpp text writer against the
+oracle's state printed the same way, and checkpoint / restart continuing a
+run bit for bit (FP64 and FP32, single and batched handles)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as P
+from parity_util import to_gpu_cfg
+
+
+def cxx_default(v):
+    """A double through std::ostream's default formatting (6 significant digits, %g)."""
+    s = "%g" % v
+    return s
+
+
+@pytest.mark.gpu
+def test_save4py_matches_oracle_text(gpu, tmp_path):
+    kw = dict(ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=3)
+    sim = gpu.Simulation(**to_gpu_cfg(kw)).init()
+    o = P.Oracle(**kw).init()
+    sim.run(12)
+    o.run(12)
+    name = sim.save4py(str(tmp_path), id=7)
+    assert os.path.basename(name).startswith("BWx007t_")
+    got = open(name).read().splitlines()
+    W, lp, ic, lf = o.get("W"), o.get("lp"), o.get("icoord"), o.get("leafs")
+    inf = o.info()
+    dx0, dy0 = inf["dx0"], inf["dy0"]
+    exp = []
+    hdr = "#" + "x".rjust(15) + "".join(s.rjust(16) for s in
+                                        ("y", "xdelta", "ydelta", "density", "U", "v", "w", "pressure", "Bx", "By", "Bz"))
+    for nb in range(inf["lastActive"]):
+        if not lf[nb]:
+            continue
+        exp.append(hdr)
+        lev = lp[nb][0]
+        dx, dy = dx0 / 2 ** lev, dy0 / 2 ** lev
+        for j in range(2, 18):
+            y = ((j + ic[nb][1] - 2) + 0.5) * dy - dy0
+            for i in range(2, 18):
+                x = ((i + ic[nb][0] - 2) + 0.5) * dx - dx0
+                vals = [x, y, dx / 2.0, dy / 2.0] + [W[nb, k, j, i] for k in range(8)]
+                exp.append("".join(cxx_default(v).rjust(16) for v in vals))
+    assert got == exp
+    # full precision round-trips the state
+    name17 = sim.save4py(str(tmp_path), id=8, digits=17)
+    rows = np.array([list(map(float, r.split())) for r in open(name17) if not r.startswith("#")])
+    leafW = np.concatenate([W[nb, :, 2:18, 2:18].reshape(8, -1).T for nb in range(inf["lastActive"]) if lf[nb]])
+    assert np.array_equal(rows[:, 4:], leafW)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_checkpoint_restart_bitwise(gpu, tmp_path, precision):
+    cfg = to_gpu_cfg(dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4, precision=precision))
+    a = gpu.Simulation(**cfg).init()
+    a.run(25)
+    path = str(tmp_path / "ck.bin")
+    a.checkpoint_save(path)
+    a.run(20)
+    b = gpu.Simulation(**cfg).checkpoint_load(path)
+    assert b.info()["steps"] == 25
+    b.run(20)
+    sa, sb = a.state(), b.state()
+    assert sa["t"] == sb["t"] and sa["step"] == sb["step"]
+    for k in ("lp", "icoord", "leafs", "U", "Bi"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.mark.gpu
+def test_checkpoint_batch_and_errors(gpu, tmp_path):
+    cfgs = [gpu.blast_config(3, i) for i in range(3)]
+    for c in cfgs:
+        c.maxlevs = min(c.maxlevs, 4)
+    a = gpu.Simulation(cfgs).init()
+    a.run(15)
+    path = str(tmp_path / "ck.bin")
+    a.checkpoint_save(path)
+    a.run(10)
+    b = gpu.Simulation(cfgs).checkpoint_load(path)
+    b.run(10)
+    for i in range(3):
+        assert np.array_equal(a.download("U", i), b.download("U", i))
+    # a different configuration or an initialised handle is refused
+    other = gpu.Simulation([gpu.blast_config(4, i) for i in range(3)])
+    with pytest.raises(gpu.AmrError):
+        other.checkpoint_load(path)
+    with pytest.raises(gpu.AmrError):
+        a.checkpoint_load(path)
