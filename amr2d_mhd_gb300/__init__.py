@@ -29,7 +29,7 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "a
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_save4py",
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_autotune", "amr_save4py",
            "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
            "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
 
@@ -109,6 +109,7 @@ def load(build_if_missing: bool = True):
         "amr_profile_enable": (ctypes.c_int, [vp, i32]),
         "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
         "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
+        "amr_autotune": (ctypes.c_int, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "amr_save4py": (ctypes.c_int, [vp, i32, i32, ctypes.c_char_p, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "amr_checkpoint_save": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "amr_checkpoint_load": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -305,6 +306,13 @@ class Simulation:
             x0, y0 = ic[b, 0] * r, ic[b, 1] * r
             out[x0:x0 + c.nx * r, y0:y0 + c.ny * r] = np.kron(v, np.ones((r, r)))
         return out
+
+    def autotune(self, reps=5):
+        """Pick the fastest launch schedule on the current state; returns the
+        report (one line per candidate, the chosen one marked '*')."""
+        buf = ctypes.create_string_buffer(8192)
+        self._ck(load().amr_autotune(self.h, reps, buf, 8192))
+        return buf.value.decode()
 
     def save4py(self, directory, id=0, digits=0, instance=0):
         """savedata.cpp's text output of one instance; returns the file name."""

@@ -50,15 +50,20 @@ cudaError_t launch_faces(const Method &m, const SplitArgs &a, cudaStream_t s) {
   }
 }
 
+namespace {
+int cell_threads(const Method &m) { return m.cell_block == 128 || m.cell_block == 512 ? m.cell_block : 256; }
+}  // namespace
+
 cudaError_t launch_prim(const Method &m, const SplitArgs &a, cudaStream_t s) {
   const int nn = m.ng == 2 ? Geo<2>::NN : Geo<4>::NN;
   const size_t n = static_cast<size_t>(a.ntasks) * nn;
   if (n == 0) return cudaSuccess;
-  const unsigned g = static_cast<unsigned>((n + 255) / 256);
-  if (m.ng == 2 && !m.f32) k_prim<2, double><<<g, 256, 0, s>>>(a);
-  else if (m.ng == 2) k_prim<2, float><<<g, 256, 0, s>>>(a);
-  else if (!m.f32) k_prim<4, double><<<g, 256, 0, s>>>(a);
-  else k_prim<4, float><<<g, 256, 0, s>>>(a);
+  const int b = cell_threads(m);
+  const unsigned g = static_cast<unsigned>((n + b - 1) / b);
+  if (m.ng == 2 && !m.f32) k_prim<2, double><<<g, b, 0, s>>>(a);
+  else if (m.ng == 2) k_prim<2, float><<<g, b, 0, s>>>(a);
+  else if (!m.f32) k_prim<4, double><<<g, b, 0, s>>>(a);
+  else k_prim<4, float><<<g, b, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -66,16 +71,18 @@ cudaError_t launch_resid(const Method &m, const SplitArgs &a, cudaStream_t s) {
   const int nn = m.ng == 2 ? Geo<2>::NN : Geo<4>::NN;
   const size_t n = static_cast<size_t>(a.ntasks) * 8 * nn;
   if (n == 0) return cudaSuccess;
-  const unsigned g = static_cast<unsigned>((n + 255) / 256);
-  if (m.ng == 2 && !m.f32) k_resid<2, double><<<g, 256, 0, s>>>(a);
-  else if (m.ng == 2) k_resid<2, float><<<g, 256, 0, s>>>(a);
-  else if (!m.f32) k_resid<4, double><<<g, 256, 0, s>>>(a);
-  else k_resid<4, float><<<g, 256, 0, s>>>(a);
+  const int b = cell_threads(m);
+  const unsigned g = static_cast<unsigned>((n + b - 1) / b);
+  if (m.ng == 2 && !m.f32) k_resid<2, double><<<g, b, 0, s>>>(a);
+  else if (m.ng == 2) k_resid<2, float><<<g, b, 0, s>>>(a);
+  else if (!m.f32) k_resid<4, double><<<g, b, 0, s>>>(a);
+  else k_resid<4, float><<<g, b, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ghost(int ng, const GhostLaunch &g, cudaStream_t s) {
-  constexpr int B = 256;
+cudaError_t launch_ghost(const Method &m, const GhostLaunch &g, cudaStream_t s) {
+  const int B = m.ghost_block == 128 || m.ghost_block == 512 ? m.ghost_block : 256;
+  const int ng = m.ng;
   const int ns = g.nsnaps * g.nseg, no = g.nops * g.nseg;
   if (ns > 0) {
     if (ng == 2) k_ghost_snap<Geo<2>::N><<<(ns + B - 1) / B, B, 0, s>>>(g);

@@ -193,6 +193,10 @@ int amr_profile_read(amr_handle *h, amr_profile *o) {
   return guarded(h, [&](amr::Engine &e) { return e.profile_read(o); });
 }
 
+int amr_autotune(amr_handle *h, int32_t reps, char *report, size_t len) {
+  return guarded(h, [&](amr::Engine &e) { return e.autotune(reps, report, len); });
+}
+
 int amr_save4py(amr_handle *h, int32_t inst, int32_t id, const char *dir, int32_t digits, char *name_out,
                 size_t name_len) {
   return guarded(h, [&](amr::Engine &e) { return e.save4py(inst, id, dir, digits, name_out, name_len); });

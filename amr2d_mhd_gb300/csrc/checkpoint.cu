@@ -133,7 +133,9 @@ int Engine::save4py(int q, int id, const char *dir, int digits, char *name_out, 
   std::ofstream out(name);
   if (!out) return fail(AMR_E_ARG, "cannot write " + name);
   if (digits > 0) out << std::setprecision(digits);
-  const int w = 16, ng = ng_, lo = ng, hi = ng + NI - 1;
+  // the reference's width of 16 holds 6 significant digits; wider columns
+  // keep more digits separated
+  const int w = digits > 9 ? digits + 9 : 16, ng = ng_, lo = ng, hi = ng + NI - 1;
   const double sx = in.cfg.geometry == 0 ? in.dx[0] : 0.0, sy = in.cfg.geometry == 0 ? in.dy[0] : 0.0;
   for (int nb = 0; nb < t.lastActive; nb++) {
     if (!t.leafs[nb]) continue;

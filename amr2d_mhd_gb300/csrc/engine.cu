@@ -2,6 +2,7 @@
 #include "engine.hpp"
 
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
@@ -551,7 +552,7 @@ int Engine::fill(std::initializer_list<std::pair<FillKind, int>> what) {
   }
   g.nseg = q;
   g.snapbuf = d_snap_.as<double>();
-  CK(launch_ghost(ng_, g, stream_), "ghost fill");
+  CK(launch_ghost(m_, g, stream_), "ghost fill");
   prof_.launches += (g.nsnaps > 0) + (g.nops > 0);
   return AMR_OK;
 }
@@ -614,6 +615,78 @@ int Engine::stage(int step) {
   }
   prof_.stage_launches += 1;
   stage_cells_pending_ += static_cast<int64_t>(n) * NI * NI;
+  return AMR_OK;
+}
+
+int Engine::autotune(int reps, char *report, size_t len) {
+  if (!initialised_) return fail(AMR_E_STATE, "amr_init has not been called");
+  if (poisoned_) return fail(AMR_E_STATE, "engine stopped by an earlier error: " + last_error);
+  if (reps < 1) reps = 1;
+  active_.clear();
+  for (size_t q = 0; q < inst_.size(); q++)
+    if (!inst_[q].done) active_.push_back(static_cast<int>(q));
+  if (active_.empty()) return fail(AMR_E_STATE, "no active instance to tune on");
+  if (int rc = rebuild()) return rc;
+  if (int rc = upload_params()) return rc;
+  const bool prof = prof_on_;
+  prof_on_ = false;
+  struct Cand { bool split; int fb, cb, gb; float ms; };
+  std::vector<Cand> cands;
+  for (int gb : {128, 256, 512}) {
+    cands.push_back({false, 128, 256, gb, 0.f});
+    for (int fb : {64, 128})
+      for (int cb : {256, 512}) cands.push_back({true, fb, cb, gb, 0.f});
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  auto probe = [&]() -> int {
+    if (int rc = fill({{FILL_CC, AMR_FIELD_U}, {FILL_FC, AMR_FIELD_BI}})) return rc;
+    if (int rc = stage(1)) return rc;
+    return fill({{FILL_FC, AMR_FIELD_BI}, {FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}});
+  };
+  int rc = AMR_OK;
+  const Method keep = m_;
+  const bool keep_split = split_;
+  for (Cand &c : cands) {
+    split_ = c.split;
+    m_.faces_block = c.fb;
+    m_.cell_block = c.cb;
+    m_.ghost_block = c.gb;
+    if ((rc = probe())) break;  // warm-up
+    cudaEventRecord(e0, stream_);
+    for (int r = 0; r < reps && !rc; r++) rc = probe();
+    cudaEventRecord(e1, stream_);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "autotune"); break; }
+    cudaEventElapsedTime(&c.ms, e0, e1);
+    c.ms /= static_cast<float>(reps);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  prof_on_ = prof;
+  stage_cells_pending_ = 0;
+  if (rc) { m_ = keep; split_ = keep_split; return rc; }
+  if (int r2 = check_device_error()) return r2;
+  const Cand *best = &cands[0];
+  for (const Cand &c : cands)
+    if (c.ms < best->ms) best = &c;
+  split_ = best->split;
+  m_.faces_block = best->fb;
+  m_.cell_block = best->cb;
+  m_.ghost_block = best->gb;
+  gen_++;  // the captured step uses the chosen launches
+  if (report && len) {
+    std::string s;
+    char line[160];
+    for (const Cand &c : cands) {
+      std::snprintf(line, sizeof line, "%s%s faces %d cells %d ghosts %d: %.4f ms\n", &c == best ? "* " : "  ",
+                    c.split ? "split" : "fused", c.fb, c.cb, c.gb, c.ms);
+      s += line;
+    }
+    std::strncpy(report, s.c_str(), len - 1);
+    report[len - 1] = '\0';
+  }
   return AMR_OK;
 }
 

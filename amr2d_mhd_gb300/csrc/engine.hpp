@@ -86,6 +86,12 @@ class Engine {
   int profile_enable(bool on);
   int profile_read(amr_profile *out);
 
+  // Times candidate launch schedules (fused or split stage, threads per CTA
+  // of the face, cell and ghost kernels) on the current state with an
+  // idempotent probe (ghost fill of U and Bi + stage 1 + the fill after it),
+  // keeps the fastest and describes the trials in `report`.
+  int autotune(int reps, char *report, size_t len);
+
   // checkpoint / restart and the savedata.cpp writer (checkpoint.cu)
   int checkpoint_save(const char *path);
   int checkpoint_load(const char *path);

@@ -19,6 +19,11 @@ struct Method {
   int recon;   // Recon
   int flux;    // Flux
   int f32;     // FP32 bulk storage / arithmetic
+  // launch schedule (picked by Engine::autotune): threads per CTA of the
+  // face-flux kernel (64 or 128), of the per-cell kernels and of the ghost fills
+  int faces_block = 128;
+  int cell_block = 256;
+  int ghost_block = 256;
 };
 
 // true if the (ng, recon, flux, precision) combination is compiled
@@ -45,7 +50,7 @@ cudaError_t launch_faces(const Method &m, const SplitArgs &a, cudaStream_t s);
 cudaError_t launch_resid(const Method &m, const SplitArgs &a, cudaStream_t s);
 
 // ghost fill: snapshot pass (if any snapshots) then the gather pass
-cudaError_t launch_ghost(int ng, const GhostLaunch &g, cudaStream_t s);
+cudaError_t launch_ghost(const Method &m, const GhostLaunch &g, cudaStream_t s);
 cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);

@@ -39,21 +39,23 @@ cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, c
 #endif
 
 template <int NG, int RECON, int FLUX, typename S>
-cudaError_t launch_faces_t(const SplitArgs &a, cudaStream_t s) {
+cudaError_t launch_faces_t(const SplitArgs &a, int block, cudaStream_t s) {
   constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
   const size_t n = static_cast<size_t>(a.ntasks) * PER;
   if (n == 0) return cudaSuccess;
-  k_faces<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(a);
+  if (block != 64) block = 128;  // the kernel is bounded at 128 threads per CTA
+  k_faces<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>((n + block - 1) / block), block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int FLUX, typename S>
 cudaError_t launch_faces_flux(const Method &m, const SplitArgs &a, cudaStream_t s) {
-  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, s);
-  if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, s);
-  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, s);
-  if (m.ng == 4 && m.recon == REC_WENO3) return launch_faces_t<4, REC_WENO3, FLUX, S>(a, s);
-  if (m.ng == 4 && m.recon == REC_WENO5) return launch_faces_t<4, REC_WENO5, FLUX, S>(a, s);
+  const int b = m.faces_block;
+  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, b, s);
+  if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, b, s);
+  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, b, s);
+  if (m.ng == 4 && m.recon == REC_WENO3) return launch_faces_t<4, REC_WENO3, FLUX, S>(a, b, s);
+  if (m.ng == 4 && m.recon == REC_WENO5) return launch_faces_t<4, REC_WENO5, FLUX, S>(a, b, s);
   return cudaErrorInvalidValue;
 }
 

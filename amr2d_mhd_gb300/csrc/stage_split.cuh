@@ -26,7 +26,7 @@ struct SplitArgs {
 
 // U2W / Us2W (meshblock.cpp:119-179) for every cell of every leaf
 template <int NG, typename S>
-__global__ void __launch_bounds__(256) k_prim(SplitArgs a) {
+__global__ void __launch_bounds__(512) k_prim(SplitArgs a) {
   using G = Geo<NG>;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
   const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(128, MINB) k_faces(SplitArgs a) {
 // residual on [LO, HI]^2 (zero elsewhere) and the RK stage on every cell
 // (main.cpp:260-270 / 292-302)
 template <int NG, typename S>
-__global__ void __launch_bounds__(256) k_resid(SplitArgs a) {
+__global__ void __launch_bounds__(512) k_resid(SplitArgs a) {
   using G = Geo<NG>;
   using T = S;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;

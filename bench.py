@@ -170,6 +170,7 @@ def run_ours(args):
     for prec in ("fp64", "fp32"):
         sim = make(prec)
         advance_to(sim, T0)
+        tune = sim.autotune() if not args.no_tune else ""
         sim.run(W)
         clocks = ClockSampler(local) if prec == "fp64" else None
         if clocks:
@@ -196,7 +197,8 @@ def run_ours(args):
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
             ms, cells = float(mx[0]), float(t[1])
         results[prec] = dict(ms=ms, cells=cells, prof=prof, clocks=clk, leaves=i1["n_leaves"],
-                             steps=i1["steps"] - i0["steps"])
+                             steps=i1["steps"] - i0["steps"],
+                             schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"))
         if prec == "fp64":
             # e2e through the C ABI with the state in host memory
             U = sim.download("U")
@@ -248,6 +250,7 @@ def run_batch(stream, steps, advance):
         sim.set_stream(stream.cuda_stream)
         sim.init()
         sim.run(advance)
+        tune = sim.autotune(2)
         sim.profile(True)
         c0 = sum(sim.info(q)["cell_updates"] for q in range(BATCH_N))
         torch.cuda.synchronize()
@@ -262,7 +265,8 @@ def run_batch(stream, steps, advance):
         out[prec] = dict(value=(c1 - c0) / (ms * 1e-3), ms_per_step=ms / steps,
                          leaves=sum(sim.info(q)["n_leaves"] for q in range(BATCH_N)),
                          host_ms_per_step=(p["host_compile_ms"] + p["host_admesh_ms"]) / steps,
-                         gpu_launches=int(p["launches"]))
+                         gpu_launches=int(p["launches"]),
+                         schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"))
         sim.close()
     l1 = []
     sims = {}
@@ -452,6 +456,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the blast-batch measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch schedule")
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--batch-advance", type=int, default=120)
     ap.add_argument("--ncu-case", type=int, default=0,
@@ -516,7 +521,9 @@ def main():
                      "peak_source": peak_kind, "traffic": traffic, "kernel": "k_faces<2,MUSCL,HLLD,double>",
                      "bytes_per_launch": alg_bytes, "launch_ms": stage_ms_avg},
         "fp64_pipe": fp64,
+        "schedule": r64["schedule"],
         "fp32": {"value": value32, "speedup_vs_fp64": value32 / value, "l1_rel_density_vs_fp64_at_t_end": l1,
+                 "schedule": r32["schedule"],
                  "t_end_fp32": r32["t_end"], "t_end_fp64": r64["t_end"], "ms_per_step": r32["ms"] / args.steps,
                  "host_ms_per_step": (r32["prof"]["host_compile_ms"] + r32["prof"]["host_admesh_ms"]) / args.steps,
                  "wait_ms_per_step": r32["prof"]["wait_ms"] / args.steps},

@@ -179,12 +179,21 @@ typedef struct amr_profile {
 int amr_profile_enable(amr_handle *h, int32_t on);
 int amr_profile_read(amr_handle *h, amr_profile *out);
 
+/* Autotuner (no counterpart in the reference): times the candidate launch
+ * schedules (fused or split RK stage; threads per CTA of the face-flux, cell
+ * and ghost-fill kernels) on the handle's current state, `reps` probes each
+ * (ghost fill + stage 1, which leaves U and Bi unchanged), and keeps the
+ * fastest for later steps.  `report` (may be NULL) receives one line per
+ * candidate, the chosen one marked with '*'. */
+int amr_autotune(amr_handle *h, int32_t reps, char *report, size_t len);
+
 /* ---- output and restart --------------------------------------------------
  * amr_save4py writes instance `inst` in the format of save4py
  * (savedata.cpp:7-46) to <dir>/<IC><id, 3 digits>t_<t>.dat: per leaf block a
  * "#" header line, then x, y, dx/2, dy/2, rho, u, v, w, p, Bx, By, Bz of
  * every interior cell in columns of width 16.  digits = 0 keeps the
- * reference's 6 significant digits; > 0 sets the precision (17 = exact).
+ * reference's 6 significant digits; > 0 sets the precision (17 = exact;
+ * above 9 digits the columns widen to digits + 9 characters).
  * The file name is copied to name_out (may be NULL).
  * amr_checkpoint_save / _load (extension): the whole handle (configurations,
  * counters, quadtrees, every field) in one binary file; load into a handle
