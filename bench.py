@@ -226,10 +226,45 @@ def run_ours(args):
         results[prec]["rho"] = sim.uniform(0) if rank == 0 else None
         sim.close()
     if not args.no_batch:
+        results["rotor_batch"] = run_rotor_batch(stream, args.batch_steps)
         results["batch"] = run_batch(stream, args.batch_steps, args.batch_advance)
     if not args.no_adjoint:
         results["adjoint"] = run_adjoint(stream)
     return results, world, rank
+
+
+ROTOR_BATCH = 64
+
+
+def run_rotor_batch(stream, steps):
+    """ROTOR_BATCH copies of the bench rotor in one handle (independent
+    instances, each bit-identical to a single run), advanced untimed to T0,
+    then `steps` timed batch steps, FP64 and FP32."""
+    import torch
+
+    import amr2d_mhd_gb300 as amr
+    out = {}
+    for prec in ("fp64", "fp32"):
+        sim = amr.Simulation([amr.make_config(precision=prec, **WORKLOAD) for _ in range(ROTOR_BATCH)])
+        sim.set_stream(stream.cuda_stream)
+        sim.init()
+        while sim.info(0)["t"] < T0:
+            sim.run(50)
+        tune = sim.autotune(2)
+        sim.run(3)
+        c0 = sum(sim.info(q)["cell_updates"] for q in range(ROTOR_BATCH))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        c1 = sum(sim.info(q)["cell_updates"] for q in range(ROTOR_BATCH))
+        out[prec] = dict(value=(c1 - c0) / (ms * 1e-3), ms_per_step=ms / steps,
+                         schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"))
+        sim.close()
+    return out
 
 
 BATCH_SEED = 2026
@@ -528,6 +563,13 @@ def main():
                  "host_ms_per_step": (r32["prof"]["host_compile_ms"] + r32["prof"]["host_admesh_ms"]) / args.steps,
                  "wait_ms_per_step": r32["prof"]["wait_ms"] / args.steps},
         "host_ms_per_step": (prof["host_compile_ms"] + prof["host_admesh_ms"]) / args.steps,
+        "rotor_batch": None if "rotor_batch" not in res else {
+            "workload": "%d copies of the bench rotor in one handle (one launch per kernel over all their leaf "
+                        "blocks), from t=%.2f; each copy is bit-identical to a single run, so the FP32 density "
+                        "error is the fp32 entry's" % (ROTOR_BATCH, T0),
+            "fp64": res["rotor_batch"]["fp64"], "fp32": res["rotor_batch"]["fp32"],
+            "fp32_batched_vs_plain_fp64": res["rotor_batch"]["fp32"]["value"] / value,
+            "l1_rel_density_vs_fp64_at_t_end": l1},
         "batch": None if "batch" not in res else {
             "workload": "%d seeded cylindrical blasts (seed %d, amr_config_blast): [0,1]^2, gamma 1.4, 4 roots, "
                         "maxlevs U{3..6}, MUSCL-MC + HLLE + CT, CFL 0.2, outflow; %d untimed batch steps, then "
