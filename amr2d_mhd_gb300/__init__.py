@@ -171,13 +171,17 @@ def kh_config(seed, precision="fp64") -> Config:
     return c
 
 
-def ot_config(maxlevs=7, precision="fp64", cfl=0.4) -> Config:
+def ot_config(maxlevs=7, precision="fp64", cfl=0.4, limiter="WENO5", dt_fixed=0.0) -> Config:
     """Orszag-Tang vortex on [0, 2 pi]^2, periodic, 4 x 4 roots of 16 x 16,
-    WENO5 + HLLD with 4 ghost layers, gamma 5/3, t_end pi (extension)."""
+    WENO5 (4 ghost layers) or a MUSCL limiter (2) + HLLD, gamma 5/3, t_end pi
+    (extension); dt_fixed > 0 replaces the CFL step (a common time grid for
+    comparing precisions)."""
     import math
-    return make_config(ic="OT", limiter="WENO5", flux="HLLD", cfl=cfl, maxlevs=maxlevs, nghosts=4, nroots=(4, 4),
-                       periodic=True, geometry=1, gamma=5.0 / 3.0, t_end=math.pi, precision=precision,
-                       lenx=2 * math.pi, leny=2 * math.pi)
+    c = make_config(ic="OT", limiter=limiter, flux="HLLD", cfl=cfl, maxlevs=maxlevs,
+                    nghosts=4 if limiter == "WENO5" else 2, nroots=(4, 4), periodic=True, geometry=1,
+                    gamma=5.0 / 3.0, t_end=math.pi, precision=precision, lenx=2 * math.pi, leny=2 * math.pi)
+    c.dt_fixed = dt_fixed
+    return c
 
 
 class Simulation:

@@ -18,7 +18,10 @@ template <typename T> __device__ __forceinline__ T smax(T a, T b) { return a < b
 template <typename T> __device__ __forceinline__ T sgn(T v) { return v > T(0) ? T(1) : (v < T(0) ? T(-1) : T(0)); }
 template <typename T> __device__ __forceinline__ T eps_of();
 template <> __device__ __forceinline__ double eps_of<double>() { return 1.0E-15; }
-template <> __device__ __forceinline__ float eps_of<float>() { return 1.0E-6f; }  // defs.hpp:20
+// The FP32 bulk path keeps the FP64 scheme's epsilon (representable in
+// float): defs.hpp:20 would switch to 1e-6 in a float build, which changes
+// the WENO weights and limiter ratios, i.e. the scheme, not just the rounding.
+template <> __device__ __forceinline__ float eps_of<float>() { return 1.0E-15f; }
 
 // slopelimiter.cpp:6-54
 template <typename T>
