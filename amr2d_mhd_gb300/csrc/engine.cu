@@ -630,12 +630,13 @@ int Engine::autotune(int reps, char *report, size_t len) {
   if (int rc = upload_params()) return rc;
   const bool prof = prof_on_;
   prof_on_ = false;
-  struct Cand { bool split; int fb, cb, gb; float ms; };
+  struct Cand { bool split; int fb, cb, gb, pers; float ms; };
   std::vector<Cand> cands;
   for (int gb : {128, 256, 512}) {
-    cands.push_back({false, 128, 256, gb, 0.f});
-    for (int fb : {64, 128})
-      for (int cb : {256, 512}) cands.push_back({true, fb, cb, gb, 0.f});
+    cands.push_back({false, 128, 256, gb, 0, 0.f});
+    for (int pers : {0, 1})
+      for (int fb : {64, 128})
+        for (int cb : {256, 512}) cands.push_back({true, fb, cb, gb, pers, 0.f});
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   CK(cudaEventCreate(&e0), "event");
@@ -653,6 +654,7 @@ int Engine::autotune(int reps, char *report, size_t len) {
     m_.faces_block = c.fb;
     m_.cell_block = c.cb;
     m_.ghost_block = c.gb;
+    m_.persistent = c.pers;
     if ((rc = probe())) break;  // warm-up
     cudaEventRecord(e0, stream_);
     for (int r = 0; r < reps && !rc; r++) rc = probe();
@@ -675,13 +677,14 @@ int Engine::autotune(int reps, char *report, size_t len) {
   m_.faces_block = best->fb;
   m_.cell_block = best->cb;
   m_.ghost_block = best->gb;
+  m_.persistent = best->pers;
   gen_++;  // the captured step uses the chosen launches
   if (report && len) {
     std::string s;
     char line[160];
     for (const Cand &c : cands) {
-      std::snprintf(line, sizeof line, "%s%s faces %d cells %d ghosts %d: %.4f ms\n", &c == best ? "* " : "  ",
-                    c.split ? "split" : "fused", c.fb, c.cb, c.gb, c.ms);
+      std::snprintf(line, sizeof line, "%s%s faces %d%s cells %d ghosts %d: %.4f ms\n", &c == best ? "* " : "  ",
+                    c.split ? "split" : "fused", c.fb, c.pers ? " persistent" : "", c.cb, c.gb, c.ms);
       s += line;
     }
     std::strncpy(report, s.c_str(), len - 1);

@@ -24,6 +24,7 @@ struct Method {
   int faces_block = 128;
   int cell_block = 256;
   int ghost_block = 256;
+  int persistent = 0;   // face fluxes by a grid of resident CTAs looping over the face list
 };
 
 // true if the (ng, recon, flux, precision) combination is compiled

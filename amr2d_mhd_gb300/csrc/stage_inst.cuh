@@ -39,23 +39,46 @@ cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, c
 #endif
 
 template <int NG, int RECON, int FLUX, typename S>
-cudaError_t launch_faces_t(const SplitArgs &a, int block, cudaStream_t s) {
+cudaError_t launch_faces_t(const SplitArgs &a, int block, bool persistent, cudaStream_t s) {
   constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
   const size_t n = static_cast<size_t>(a.ntasks) * PER;
   if (n == 0) return cudaSuccess;
   if (block != 64) block = 128;  // the kernel is bounded at 128 threads per CTA
-  k_faces<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>((n + block - 1) / block), block, 0, s>>>(a);
+  size_t grid = (n + block - 1) / block;
+  if (persistent) {
+    // resident CTAs per SM for each block size, looked up once
+    static int per_sm[2] = {0, 0}, sms = 0;
+    int &ps = per_sm[block == 64 ? 0 : 1];
+    if (!sms) {
+      int dev = 0;
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+    }
+    if (!ps) {
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &ps, k_faces_persist<NG, RECON, FLUX, S, AMR_FACES_MINB>, block, 0);
+      if (e != cudaSuccess) return e;
+      if (ps < 1) ps = 1;
+    }
+    const size_t cap = static_cast<size_t>(sms) * ps;
+    if (grid > cap) grid = cap;
+    k_faces_persist<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>(grid), block, 0, s>>>(a);
+  } else {
+    k_faces<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>(grid), block, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
 template <int FLUX, typename S>
 cudaError_t launch_faces_flux(const Method &m, const SplitArgs &a, cudaStream_t s) {
   const int b = m.faces_block;
-  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, b, s);
-  if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, b, s);
-  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, b, s);
-  if (m.ng == 4 && m.recon == REC_WENO3) return launch_faces_t<4, REC_WENO3, FLUX, S>(a, b, s);
-  if (m.ng == 4 && m.recon == REC_WENO5) return launch_faces_t<4, REC_WENO5, FLUX, S>(a, b, s);
+  const bool p = m.persistent != 0;
+  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, b, p, s);
+  if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, b, p, s);
+  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, b, p, s);
+  if (m.ng == 4 && m.recon == REC_WENO3) return launch_faces_t<4, REC_WENO3, FLUX, S>(a, b, p, s);
+  if (m.ng == 4 && m.recon == REC_WENO5) return launch_faces_t<4, REC_WENO5, FLUX, S>(a, b, p, s);
   return cudaErrorInvalidValue;
 }
 

@@ -53,13 +53,11 @@ __global__ void __launch_bounds__(512) k_prim(SplitArgs a) {
 
 // MUSCL2D.cpp:24-116 for one face of one leaf: x faces (i+1/2, j) for i, j in
 // [LO, HI], then y faces (i, j+1/2)
-template <int NG, int RECON, int FLUX, typename S, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_faces(SplitArgs a) {
+template <int NG, int RECON, int FLUX, typename S>
+__device__ __forceinline__ void face_flux(const SplitArgs &a, size_t e) {
   using G = Geo<NG>;
   using T = S;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, NF = G::NF, PER = 2 * NF * NF;
-  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= static_cast<size_t>(a.ntasks) * PER) return;
   const int t = static_cast<int>(e / PER), f = static_cast<int>(e % PER);
   const LeafTask task = a.tasks[t];
   const InstParams ip = a.inst[task.inst];
@@ -119,6 +117,25 @@ __global__ void __launch_bounds__(128, MINB) k_faces(SplitArgs a) {
     out[k * NN] = fl[k];
   }
   if (bad) dev_fail(a.err, DERR_NAN, task.slot, fpos % N, fpos / N, 0.0);
+}
+
+template <int NG, int RECON, int FLUX, typename S, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_faces(SplitArgs a) {
+  constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
+  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<size_t>(a.ntasks) * PER) return;
+  face_flux<NG, RECON, FLUX, S>(a, e);
+}
+
+// persistent variant: a grid sized to the CTAs the SMs hold at once walks
+// the whole face list of the step (all leaf blocks of all instances)
+template <int NG, int RECON, int FLUX, typename S, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_faces_persist(SplitArgs a) {
+  constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
+  const size_t n = static_cast<size_t>(a.ntasks) * PER;
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  for (size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n; e += stride)
+    face_flux<NG, RECON, FLUX, S>(a, e);
 }
 
 // residual on [LO, HI]^2 (zero elsewhere) and the RK stage on every cell
