@@ -17,7 +17,7 @@ enum Recon { REC_MUSCL = 0, REC_WENO3 = 1, REC_WENO5 = 2 };
 enum Flux { FLX_RUSA = 0, FLX_HLLE, FLX_HLLC, FLX_HLLD, FLX_ROE };
 
 // device error word: first failure wins (code, block, i, j)
-enum DevErr { DERR_NONE = 0, DERR_PRESSURE = 1, DERR_NAN = 2, DERR_HLLC = 3, DERR_REFINE_NAN = 4 };
+enum DevErr { DERR_NONE = 0, DERR_PRESSURE = 1, DERR_NAN = 2, DERR_HLLC = 3, DERR_REFINE_NAN = 4, DERR_TIMEOUT = 5 };
 struct DevError {
   int code;
   int blk;

@@ -67,6 +67,7 @@ int map_dev_error(int code) {
   switch (code) {
     case DERR_PRESSURE: return AMR_E_PRESSURE;
     case DERR_HLLC: return AMR_E_HLLC;
+    case DERR_TIMEOUT: return AMR_E_TIMEOUT;
     default: return AMR_E_NAN;
   }
 }

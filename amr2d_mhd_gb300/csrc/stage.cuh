@@ -85,6 +85,40 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
   w[7] = u[7];
 }
 
+// ------------------------------------------------------------ bulk staging
+// One thread issues a bulk copy (TMA, cp.async.bulk) of `bytes` contiguous
+// bytes from global to shared memory, completing on an mbarrier; every
+// thread then waits for the phase with a bounded spin.  Both addresses and
+// the size are multiples of 16 bytes (checked by the caller's layout).
+constexpr long kBulkSpinLimit = 1L << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void bulk_stage_issue(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  const uint32_t b = smem_u32(bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(b)
+               : "memory");
+}
+
+// true once the phase completed; false after the spin limit
+__device__ __forceinline__ bool bulk_stage_wait(uint64_t *bar, uint32_t phase) {
+  const uint32_t b = smem_u32(bar);
+  for (long it = 0; it < kBulkSpinLimit; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(b), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 template <int NG, int RECON, int FLUX, typename S>
 __global__ void __launch_bounds__(256) k_stage(StageArgs a) {
   using G = Geo<NG>;
@@ -105,11 +139,26 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs a) {
   const double *By = Bx + NN;
   const int tid = threadIdx.x, nthr = blockDim.x;
 
-  // 1. primitive variables of every cell (U2W / Us2W), with the traps
+  // 0. the block's conserved state (8 planes, contiguous) into sW by TMA
+  __shared__ __align__(8) uint64_t bar;
+  static_assert((8 * NN * sizeof(S)) % 16 == 0, "bulk copies move multiples of 16 bytes");
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) bulk_stage_issue(sW, Q, static_cast<uint32_t>(8 * NN * sizeof(S)), &bar);
+  if (!bulk_stage_wait(&bar, 0)) {
+    if (tid == 0) dev_fail(a.err, DERR_TIMEOUT, task.slot, 0, 0, 0.0);
+    bulk_stage_wait(&bar, 0);  // let the copy land before the CTA's shared memory is released
+    return;
+  }
+
+  // 1. primitive variables of every cell (U2W / Us2W), in place, with the traps
   for (int c = tid; c < NN; c += nthr) {
     S u[8], w[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) u[k] = Q[k * NN + c];
+    for (int k = 0; k < 8; k++) u[k] = sW[k * NN + c];
     cons2prim_cell<S>(u, w, ip.gamma);
 #pragma unroll
     for (int k = 0; k < 8; k++) sW[k * NN + c] = w[k];
