@@ -537,6 +537,9 @@ def main():
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: the rotor from its initial condition for this many steps, then exit")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="precision of --ncu-case")
+    ap.add_argument("--ncu-rotor-batch", type=int, default=0,
+                    help="profiling case: the %d-rotor batch, fused stage kernel, this many steps, then exit"
+                         % ROTOR_BATCH)
     ap.add_argument("--adjoint-case", type=int, default=0,
                     help="profiling case: this many recorded and reversed steps of the KH adjoint, then exit")
     args = ap.parse_args()
@@ -552,6 +555,14 @@ def main():
         sim.adjoint_seed("U", lam)
         for _ in range(args.adjoint_case):
             sim.adjoint_step()
+        print(json.dumps(sim.info()))
+        return 0
+    if args.ncu_rotor_batch:
+        import amr2d_mhd_gb300 as amr
+        os.environ["AMR2D_STAGE_KERNEL"] = "fused"
+        sim = amr.Simulation([amr.make_config(precision=args.precision, **WORKLOAD) for _ in range(ROTOR_BATCH)])
+        sim.init()
+        sim.run(args.ncu_rotor_batch)
         print(json.dumps(sim.info()))
         return 0
     if args.ncu_case:
@@ -613,8 +624,9 @@ def main():
                      "bytes_per_launch": alg_bytes, "launch_ms": stage_ms_avg},
         "fp64_pipe": fp64,
         "schedule": r64["schedule"],
+        "host_compile_ms_per_step": prof["host_compile_ms"] / args.steps,
         "fp32": {"value": value32, "speedup_vs_fp64": value32 / value, "l1_rel_density_vs_fp64_at_t_end": l1,
-                 "schedule": r32["schedule"],
+                 "schedule": r32["schedule"], "host_compile_ms_per_step": r32["prof"]["host_compile_ms"] / args.steps,
                  "t_end_fp32": r32["t_end"], "t_end_fp64": r64["t_end"], "ms_per_step": r32["ms"] / args.steps,
                  "host_ms_per_step": (r32["prof"]["host_compile_ms"] + r32["prof"]["host_admesh_ms"]) / args.steps,
                  "wait_ms_per_step": r32["prof"]["wait_ms"] / args.steps},
