@@ -82,14 +82,18 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
   // recovered pressure below zero where the FP64 path stays positive
   if (!(p > kPressureFloor)) p = kPressureFloor;
   w[0] = u[0];
-  w[1] = u[1] * ir;
-  w[2] = u[2] * ir;
-  w[3] = u[3] * ir;
+  w[1] = static_cast<float>(mx * ird);  // correctly rounded to ~1e-14 before the cast
+  w[2] = static_cast<float>(my * ird);
+  w[3] = static_cast<float>(mz * ird);
   w[4] = static_cast<float>(p);
   w[5] = u[5];
   w[6] = u[6];
   w[7] = u[7];
 }
+
+#ifndef AMR_STAGE_F32_MINB
+#define AMR_STAGE_F32_MINB 3
+#endif
 
 // ------------------------------------------------------------ bulk staging
 // One thread issues a bulk copy (TMA, cp.async.bulk) of `bytes` contiguous
@@ -125,8 +129,13 @@ __device__ __forceinline__ bool bulk_stage_wait(uint64_t *bar, uint32_t phase) {
   return false;
 }
 
+// resident CTAs per SM the fused stage kernel is compiled for: the FP32
+// instantiation trades registers for occupancy (it is latency-bound)
+template <typename S> struct StageMinBlocks { static constexpr int value = 1; };
+template <> struct StageMinBlocks<float> { static constexpr int value = AMR_STAGE_F32_MINB; };
+
 template <int NG, int RECON, int FLUX, typename S>
-__global__ void __launch_bounds__(256) k_stage(StageArgs a) {
+__global__ void __launch_bounds__(256, StageMinBlocks<S>::value) k_stage(StageArgs a) {
   using G = Geo<NG>;
   using T = S;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI, NF = G::NF, NFX = G::NFX;
