@@ -29,7 +29,7 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "a
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_autotune", "amr_save4py",
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_autotune", "amr_save4py",
            "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
            "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
 
@@ -109,6 +109,7 @@ def load(build_if_missing: bool = True):
         "amr_profile_enable": (ctypes.c_int, [vp, i32]),
         "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
         "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
+        "amr_criteria": (ctypes.c_int, [vp, dp, i32]),
         "amr_autotune": (ctypes.c_int, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "amr_save4py": (ctypes.c_int, [vp, i32, i32, ctypes.c_char_p, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "amr_checkpoint_save": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -310,6 +311,13 @@ class Simulation:
             x0, y0 = ic[b, 0] * r, ic[b, 1] * r
             out[x0:x0 + c.nx * r, y0:y0 + c.ny * r] = np.kron(v, np.ones((r, r)))
         return out
+
+    def criteria(self):
+        """criteria.cpp per block ID of instance 0 (-1 for non-leaves)."""
+        na = self.info()["last_active"]
+        g = np.empty(na, np.float64)
+        self._ck(load().amr_criteria(self.h, g.ctypes.data, na))
+        return g
 
     def autotune(self, reps=5):
         """Pick the fastest launch schedule on the current state; returns the

@@ -193,6 +193,10 @@ int amr_profile_read(amr_handle *h, amr_profile *o) {
   return guarded(h, [&](amr::Engine &e) { return e.profile_read(o); });
 }
 
+int amr_criteria(amr_handle *h, double *grad, int32_t cap) {
+  return guarded(h, [&](amr::Engine &e) { return e.api_criteria(grad, cap); });
+}
+
 int amr_autotune(amr_handle *h, int32_t reps, char *report, size_t len) {
   return guarded(h, [&](amr::Engine &e) { return e.autotune(reps, report, len); });
 }

@@ -78,6 +78,7 @@ class Engine {
   int api_ct2d(int step);
   int api_cfl_dt(double *lambda_min);
   int api_admesh();
+  int api_criteria(double *grad, int32_t cap);
   // host <-> device state
   int get_tree(int inst, int32_t *lp, int32_t *icoord, uint8_t *leafs, int32_t cap);
   int download(int inst, int field, double *dst, int64_t count);

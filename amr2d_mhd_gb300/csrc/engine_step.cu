@@ -263,6 +263,22 @@ int Engine::api_cfl_dt(double *lambda_min) {
   return AMR_OK;
 }
 
+// criteria.cpp:6-44 on the current state: per block ID of instance 0 the
+// largest relative jump of p, rho, Bx, By over its interior cells (leaves;
+// -1 for blocks that are not leaves), from the same device reduction the
+// step uses
+int Engine::api_criteria(double *grad, int32_t cap) {
+  if (!grad) return fail(AMR_E_ARG, "null pointer");
+  double lam;
+  if (int rc = api_cfl_dt(&lam)) return rc;
+  const Instance &in = inst_[0];
+  if (cap < in.tree.lastActive) return fail(AMR_E_ARG, "buffer too small");
+  for (int b = 0; b < in.tree.lastActive; b++) grad[b] = -1.0;
+  const double *hg = h_grad_.as<double>();
+  for (int t = in.task_begin; t < in.task_end; t++) grad[task_blk_[t]] = hg[t];
+  return AMR_OK;
+}
+
 int Engine::api_admesh() {
   double lam;
   if (int rc = api_cfl_dt(&lam)) return rc;

@@ -149,7 +149,12 @@ int amr_boundary(amr_handle *h, int32_t field);              /* boundary/boundar
 int amr_muscl2d_rk(amr_handle *h, int32_t step);             /* MUSCL2D + main.cpp:257-272 / 289-308 */
 int amr_ct2d(amr_handle *h, int32_t step);                   /* CT2D.cpp:11 with its ghost fills */
 int amr_cfl_dt(amr_handle *h, double *lambda_min);           /* main.cpp:322-343 */
-int amr_admesh(amr_handle *h);                               /* admesh.cpp:17 */
+int amr_admesh(amr_handle *h);
+/* criteria.cpp:6-44 on the current state of instance 0: grad[b] = the
+ * largest relative jump of p, rho, Bx, By over the interior of leaf block b
+ * (admesh refines where it is >= 0.05), -1 for blocks that are not leaves;
+ * cap >= amr_info.last_active */
+int amr_criteria(amr_handle *h, double *grad, int32_t cap);                               /* admesh.cpp:17 */
 
 /* ---- state exchange with host buffers ----------------------------------- */
 /* Tree of one instance: lp[last_active][8], icoord[last_active][2], leafs[last_active] */

@@ -114,3 +114,25 @@ def test_fp32_density_close_to_fp64(gpu):
     ra, rb = sa["U"][lf][:, 0, 2:-2, 2:-2], sb["U"][lf][:, 0, 2:-2, 2:-2]
     err = np.abs(ra - rb).sum() / np.abs(ra).sum()
     assert err < 1e-4, err
+
+
+@pytest.mark.gpu
+def test_criteria_matches_oracle(gpu):
+    """amr_criteria (device reduction) equals criteria.cpp evaluated by the
+    oracle's helper on the same state, bit for bit."""
+    kw = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4)
+    sim = gpu.Simulation(**to_gpu_cfg(kw)).init()
+    o = P.Oracle(**kw).init()
+    sim.run(12)
+    o.run(12)
+    g = sim.criteria()
+    lf = o.get("leafs")
+    U = o.get("U")
+    gm = o.info()["gamma"] - 1
+    W = U.copy()
+    W[:, 1:4] = U[:, 1:4] / U[:, :1]
+    p = gm * (U[:, 4] - 0.5 * U[:, 0] * (W[:, 1] * W[:, 1] + W[:, 2] * W[:, 2] + W[:, 3] * W[:, 3]))
+    W[:, 4] = p - gm * (0.5 * (U[:, 5] * U[:, 5] + U[:, 6] * U[:, 6] + U[:, 7] * U[:, 7]))
+    ref = P.criteria_grad(W, 2)
+    assert np.array_equal(g[lf], ref[lf])
+    assert np.all(g[~lf] == -1.0)
