@@ -16,22 +16,25 @@ namespace amr {
   } while (0)
 
 // copy blocks [0, lastActive) of one field between a dense float64 host
-// array [block][var][j][i] and the slot pool
+// array [block][var][j][i] and the slot pool.  The bulk copy goes straight
+// between the caller's (pageable) array and a device staging buffer: the
+// driver's pageable path (direct DMA on a coherent CPU-GPU link) beats a host
+// memcpy into pinned memory followed by a pinned copy; a scatter / gather
+// kernel then moves the blocks between the staging buffer and their slots.
 int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
   const int nblk = in.tree.lastActive;
   const int per = field_nv(field) * nn_;
   const size_t bytes = static_cast<size_t>(nblk) * per * sizeof(double);
   if (nblk == 0) return AMR_OK;
   CK(d_slots_.ensure(sizeof(int) * nblk), "alloc");
-  CK(h_stage_.ensure(bytes + sizeof(int) * nblk), "alloc");
+  CK(h_stage_.ensure(sizeof(int) * nblk), "alloc");
   CK(d_stage_.ensure(bytes), "alloc");
-  int *hs = reinterpret_cast<int *>(h_stage_.as<char>() + bytes);
+  int *hs = h_stage_.as<int>();
   std::memcpy(hs, in.slot.data(), sizeof(int) * nblk);
   CK(cudaMemcpyAsync(d_slots_.p, hs, sizeof(int) * nblk, cudaMemcpyHostToDevice, stream_), "h2d");
   void *fp = field_ptr(field);
   if (to_device) {
-    std::memcpy(h_stage_.p, host, bytes);
-    CK(cudaMemcpyAsync(d_stage_.p, h_stage_.p, bytes, cudaMemcpyHostToDevice, stream_), "h2d");
+    CK(cudaMemcpyAsync(d_stage_.p, host, bytes, cudaMemcpyHostToDevice, stream_), "h2d");
     CK(launch_scatter(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
        "scatter");
     prof_.h2d_bytes += static_cast<int64_t>(bytes + sizeof(int) * nblk);
@@ -43,9 +46,8 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
     prof_.h2d_bytes += static_cast<int64_t>(sizeof(int) * nblk);
     prof_.d2h_bytes += static_cast<int64_t>(bytes);
     prof_.launches += 1;
-    CK(cudaMemcpyAsync(h_stage_.p, d_stage_.p, bytes, cudaMemcpyDeviceToHost, stream_), "d2h");
+    CK(cudaMemcpyAsync(host, d_stage_.p, bytes, cudaMemcpyDeviceToHost, stream_), "d2h");
     CK(cudaStreamSynchronize(stream_), "sync");
-    std::memcpy(host, h_stage_.p, bytes);
   }
   return AMR_OK;
 }
