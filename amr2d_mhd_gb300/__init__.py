@@ -63,7 +63,8 @@ class Profile(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64), ("stage_launches", ctypes.c_int64), ("stage_ms", ctypes.c_double),
                 ("stage_cells", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
                 ("host_compile_ms", ctypes.c_double), ("host_admesh_ms", ctypes.c_double),
-                ("wait_ms", ctypes.c_double), ("steps", ctypes.c_int64)]
+                ("wait_ms", ctypes.c_double), ("steps", ctypes.c_int64), ("step_gpu_ms", ctypes.c_double),
+                ("host_capture_ms", ctypes.c_double)]
 
 
 _lib = None

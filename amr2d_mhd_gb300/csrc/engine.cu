@@ -93,6 +93,8 @@ Engine::~Engine() {
   if (adj_exec_) cudaGraphExecDestroy(adj_exec_);
   if (cap_stream_) cudaStreamDestroy(cap_stream_);
   for (cudaEvent_t e : ev_) cudaEventDestroy(e);
+  for (cudaEvent_t e : step_ev_)
+    if (e) cudaEventDestroy(e);
   for (GhostCompiler *g : gcs_) delete g;
 }
 
@@ -768,9 +770,24 @@ int Engine::enqueue_step() {
 }
 
 int Engine::launch_step() {
+  if (prof_on_) {
+    for (cudaEvent_t &e : step_ev_)
+      if (!e) CK(cudaEventCreate(&e), "event");
+    CK(cudaEventRecord(step_ev_[0], stream_), "event");
+  }
+  if (int rc = launch_step_work()) return rc;
+  if (prof_on_) {
+    CK(cudaEventRecord(step_ev_[1], stream_), "event");
+    step_ev_pending_ = true;
+  }
+  return AMR_OK;
+}
+
+int Engine::launch_step_work() {
   const int64_t launches0 = prof_.launches;
   if (!graph_on_) return enqueue_step();
   if (!exec_ || captured_gen_ != gen_) {
+    const auto t0 = std::chrono::steady_clock::now();
     // capture on a private stream; the graph is then launched on stream_
     cudaStream_t user = stream_;
     stream_ = cap_stream_;
@@ -811,6 +828,7 @@ int Engine::launch_step() {
     cudaGraphDestroy(g);
     captured_gen_ = gen_;
     graph_launches_ = prof_.launches - launches0;
+    prof_.host_capture_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   } else {
     fill_params_host();  // the graph's first node copies these to the device
     prof_.launches += graph_launches_;
@@ -848,6 +866,12 @@ void Engine::prof_collect() {
     else cudaGetLastError();  // a failed timing query must not surface in a later launch check
   }
   ev_used_ = 0;
+  if (step_ev_pending_) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, step_ev_[0], step_ev_[1]) == cudaSuccess) prof_.step_gpu_ms += ms;
+    else cudaGetLastError();
+    step_ev_pending_ = false;
+  }
   prof_.stage_cells += stage_cells_pending_;
   stage_cells_pending_ = 0;
 }
@@ -856,6 +880,7 @@ int Engine::profile_enable(bool on) {
   if (stream_) CK(cudaStreamSynchronize(stream_), "sync");
   prof_ = amr_profile{};
   ev_used_ = 0;
+  step_ev_pending_ = false;
   stage_cells_pending_ = 0;
   if (prof_on_ != on) gen_++;
   prof_on_ = on;

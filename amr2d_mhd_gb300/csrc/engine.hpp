@@ -118,7 +118,8 @@ class Engine {
   void fill_params_host();
   int enqueue_stage_sequence();
   int enqueue_step();              // params upload, stage sequence, dt kernels, result copies
-  int launch_step();               // enqueue_step directly or as a replayed CUDA graph
+  int launch_step();               // launch_step_work, bracketed by events when profiling
+  int launch_step_work();          // enqueue_step directly or as a replayed CUDA graph
   int fill(std::initializer_list<std::pair<FillKind, int>> what);
   int stage(int step);
   int ct2d(int step);
@@ -177,6 +178,8 @@ class Engine {
   amr_profile prof_{};
   std::vector<cudaEvent_t> ev_;     // start/stop pairs of this step's stage launches
   int ev_used_ = 0;
+  cudaEvent_t step_ev_[2] = {nullptr, nullptr};  // brackets the step's device work (profiling)
+  bool step_ev_pending_ = false;
   int64_t stage_cells_pending_ = 0;
   void prof_collect();
 

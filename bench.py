@@ -625,11 +625,15 @@ def main():
         "fp64_pipe": fp64,
         "schedule": r64["schedule"],
         "host_compile_ms_per_step": prof["host_compile_ms"] / args.steps,
+        "host_capture_ms_per_step": prof["host_capture_ms"] / args.steps,
+        "step_gpu_ms_per_step": prof["step_gpu_ms"] / args.steps,
         "fp32": {"value": value32, "speedup_vs_fp64": value32 / value, "l1_rel_density_vs_fp64_at_t_end": l1,
                  "schedule": r32["schedule"], "host_compile_ms_per_step": r32["prof"]["host_compile_ms"] / args.steps,
                  "t_end_fp32": r32["t_end"], "t_end_fp64": r64["t_end"], "ms_per_step": r32["ms"] / args.steps,
                  "host_ms_per_step": (r32["prof"]["host_compile_ms"] + r32["prof"]["host_admesh_ms"]) / args.steps,
-                 "wait_ms_per_step": r32["prof"]["wait_ms"] / args.steps},
+                 "wait_ms_per_step": r32["prof"]["wait_ms"] / args.steps,
+                 "host_capture_ms_per_step": r32["prof"]["host_capture_ms"] / args.steps,
+                 "step_gpu_ms_per_step": r32["prof"]["step_gpu_ms"] / args.steps},
         "host_ms_per_step": (prof["host_compile_ms"] + prof["host_admesh_ms"]) / args.steps,
         "rotor_batch": None if "rotor_batch" not in res else {
             "workload": "%d copies of the bench rotor in one handle (one launch per kernel over all their leaf "

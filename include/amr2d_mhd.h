@@ -179,6 +179,9 @@ typedef struct amr_profile {
   double host_admesh_ms;   /* host: quadtree admesh */
   double wait_ms;          /* host: waiting for the device at step end */
   int64_t steps;
+  double step_gpu_ms;      /* CUDA-event time, on the launch stream, of each step's device work
+                              (its graph, or its kernel sequence when graphs are off) */
+  double host_capture_ms;  /* host: capturing and instantiating / updating the step graph */
 } amr_profile;
 /* on != 0 starts recording events around the stage kernels; both reset the counters */
 int amr_profile_enable(amr_handle *h, int32_t on);
