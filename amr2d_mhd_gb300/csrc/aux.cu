@@ -80,17 +80,21 @@ cudaError_t launch_resid(const Method &m, const SplitArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_ghost(const Method &m, const GhostLaunch &g, cudaStream_t s) {
+cudaError_t launch_ghost(const Method &m, const GhostLaunch &in, cudaStream_t s) {
   const int B = m.ghost_block == 128 || m.ghost_block == 512 ? m.ghost_block : 256;
   const int ng = m.ng;
-  const int ns = g.nsnaps * g.nseg, no = g.nops * g.nseg;
-  if (ns > 0) {
-    if (ng == 2) k_ghost_snap<Geo<2>::N><<<(ns + B - 1) / B, B, 0, s>>>(g);
-    else k_ghost_snap<Geo<4>::N><<<(ns + B - 1) / B, B, 0, s>>>(g);
+  GhostLaunch g = in;
+  g.row0[0] = 0;
+  for (int q = 0; q < g.nseg; q++) g.row0[q + 1] = g.row0[q] + g.seg[q].nv;
+  const unsigned rows = static_cast<unsigned>(g.row0[g.nseg]);
+  const dim3 gs((g.nsnaps + B - 1) / B, rows), go((g.nops + B - 1) / B, rows);
+  if (g.nsnaps > 0 && rows > 0) {
+    if (ng == 2) k_ghost_snap<Geo<2>::N><<<gs, B, 0, s>>>(g);
+    else k_ghost_snap<Geo<4>::N><<<gs, B, 0, s>>>(g);
   }
-  if (no > 0) {
-    if (ng == 2) k_ghost_apply<Geo<2>::N><<<(no + B - 1) / B, B, 0, s>>>(g);
-    else k_ghost_apply<Geo<4>::N><<<(no + B - 1) / B, B, 0, s>>>(g);
+  if (g.nops > 0 && rows > 0) {
+    if (ng == 2) k_ghost_apply<Geo<2>::N><<<go, B, 0, s>>>(g);
+    else k_ghost_apply<Geo<4>::N><<<go, B, 0, s>>>(g);
   }
   return cudaGetLastError();
 }

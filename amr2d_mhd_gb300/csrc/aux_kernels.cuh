@@ -25,25 +25,37 @@ struct GhostLaunch {
   GhostSeg seg[kMaxSeg];
   int nseg;
   double *snapbuf;    // [nseg][nsnaps][8]
+  // variable rows of the launch: segment q owns rows [row0[q], row0[q+1]);
+  // set by launch_ghost
+  int row0[kMaxSeg + 1];
 };
 
-template <int N, typename F>
-__device__ __forceinline__ void ghost_snap_one(const GhostSeg &s, const GhostSnap &sn, double *row) {
-  const F *f = static_cast<const F *>(s.field) + static_cast<size_t>(sn.slot) * s.nv * (N * N) + sn.pos;
-  for (int k = 0; k < s.nv; k++) row[k] = static_cast<double>(f[k * N * N]);
+// A fill kernel runs on a 2-D grid: blockIdx.y is the variable row, so that
+// consecutive threads take consecutive items (ops or snapshots) of the same
+// variable and every load of an item is independent of the others.  The
+// segment is picked with constant indices into the parameter block.
+__device__ __forceinline__ GhostSeg ghost_seg(const GhostLaunch &g, int row, int &q, int &k) {
+  GhostSeg s = g.seg[0];
+  q = 0;
+  k = row;
+  if (g.nseg > 1 && row >= g.row0[1]) { s = g.seg[1]; q = 1; k = row - g.row0[1]; }
+  if (g.nseg > 2 && row >= g.row0[2]) { s = g.seg[2]; q = 2; k = row - g.row0[2]; }
+  return s;
 }
 
 // save the pre-fill values the same fill overwrites
 template <int N>
 __global__ void k_ghost_snap(GhostLaunch g) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= g.nsnaps * g.nseg) return;
-  const int q = t / g.nsnaps, r = t % g.nsnaps;
-  const GhostSeg &s = g.seg[q];
-  if (g.snaps[r].slot < 0) return;  // padding of an instance's range
-  double *row = g.snapbuf + (static_cast<size_t>(q) * g.nsnaps + r) * 8;
-  if (s.f32) ghost_snap_one<N, float>(s, g.snaps[r], row);
-  else ghost_snap_one<N, double>(s, g.snaps[r], row);
+  constexpr int NN = N * N;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.nsnaps) return;
+  const GhostSnap sn = g.snaps[r];
+  if (sn.slot < 0) return;  // padding of an instance's range
+  int q, k;
+  const GhostSeg s = ghost_seg(g, blockIdx.y, q, k);
+  const size_t at = (static_cast<size_t>(sn.slot) * s.nv + k) * NN + sn.pos;
+  g.snapbuf[(static_cast<size_t>(q) * g.nsnaps + r) * 8 + k] =
+      s.f32 ? static_cast<double>(static_cast<const float *>(s.field)[at]) : static_cast<const double *>(s.field)[at];
 }
 
 // fine-to-coarse value of one variable from the patch (i,j) (i,j+1) (i+1,j)
@@ -63,37 +75,34 @@ __device__ __forceinline__ F fine_value(int kind, int k, F a00, F a01, F a10, F 
   return a00;
 }
 
+// variable k of one gather
 template <int N, typename F>
-__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, const double *snap) {
+__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, int k, const double *snap) {
   constexpr int NN = N * N;
-  if (op.type == GOP_NOP) return;  // padding of an instance's range
   F *fld = static_cast<F *>(s.field);
-  F *dst = fld + static_cast<size_t>(op.dst_slot) * s.nv * NN + op.dst_pos;
+  F *dst = fld + (static_cast<size_t>(op.dst_slot) * s.nv + k) * NN + op.dst_pos;
   if (op.type == GOP_COPY || op.type == GOP_FINE) {
-    const F *src = fld + static_cast<size_t>(op.src_slot) * s.nv * NN + op.src_pos;
-    for (int k = 0; k < s.nv; k++) {
-      const F *c = src + k * NN;
-      dst[k * NN] = op.type == GOP_COPY ? c[0] : fine_value<F>(s.kind, k, c[0], c[N], c[1], c[1 + N]);
-    }
+    const F *c = fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos;
+    *dst = op.type == GOP_COPY ? c[0] : fine_value<F>(s.kind, k, c[0], c[N], c[1], c[1 + N]);
   } else {
-    const double *r = snap + static_cast<size_t>(op.src_slot) * 8;
-    for (int k = 0; k < s.nv; k++) {
-      if (op.type == GOP_SNAP) dst[k * NN] = static_cast<F>(r[k]);
-      else dst[k * NN] = fine_value<F>(s.kind, k, static_cast<F>(r[k]), static_cast<F>(r[8 + k]),
-                                       static_cast<F>(r[16 + k]), static_cast<F>(r[24 + k]));
-    }
+    const double *r = snap + static_cast<size_t>(op.src_slot) * 8 + k;
+    *dst = op.type == GOP_SNAP ? static_cast<F>(r[0])
+                               : fine_value<F>(s.kind, k, static_cast<F>(r[0]), static_cast<F>(r[8]),
+                                               static_cast<F>(r[16]), static_cast<F>(r[24]));
   }
 }
 
 template <int N>
 __global__ void k_ghost_apply(GhostLaunch g) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= g.nops * g.nseg) return;
-  const int q = t / g.nops, r = t % g.nops;
-  const GhostSeg &s = g.seg[q];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.nops) return;
+  const GhostOp op = g.ops[r];
+  if (op.type == GOP_NOP) return;  // padding of an instance's range
+  int q, k;
+  const GhostSeg s = ghost_seg(g, blockIdx.y, q, k);
   const double *snap = g.snapbuf + static_cast<size_t>(q) * g.nsnaps * 8;
-  if (s.f32) ghost_apply_one<N, float>(s, g.ops[r], snap);
-  else ghost_apply_one<N, double>(s, g.ops[r], snap);
+  if (s.f32) ghost_apply_one<N, float>(s, op, k, snap);
+  else ghost_apply_one<N, double>(s, op, k, snap);
 }
 
 // ------------------------------------------------------------- CT2D.cpp

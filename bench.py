@@ -536,6 +536,8 @@ def main():
     ap.add_argument("--batch-advance", type=int, default=120)
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: the rotor from its initial condition for this many steps, then exit")
+    ap.add_argument("--ncu-t0", type=float, default=0.0,
+                    help="with --ncu-case: first advance the rotor to this time (untimed), then run the steps")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="precision of --ncu-case")
     ap.add_argument("--ncu-rotor-batch", type=int, default=0,
                     help="profiling case: the %d-rotor batch, fused stage kernel, this many steps, then exit"
@@ -568,8 +570,12 @@ def main():
     if args.ncu_case:
         import amr2d_mhd_gb300 as amr
         sim = amr.Simulation(precision=args.precision, **WORKLOAD).init()
+        sim.profile(True)
+        if args.ncu_t0 > 0:
+            advance_to(sim, args.ncu_t0)
+        before = sim.profile()["launches"]
         sim.run(args.ncu_case)
-        print(json.dumps(sim.info()))
+        print(json.dumps(dict(sim.info(), launches_before=before, launches=sim.profile()["launches"] - before)))
         return 0
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
