@@ -141,7 +141,7 @@ __global__ void k_ct_face_adj(CtAdjArgs a) {
   const LeafTask t = a.tasks[blockIdx.x];
   const double dt = a.inst[t.inst].dt;
   const double s = a.step == 1 ? 1.0 : 0.5;
-  const double cx = s * dt * (1. / t.dy), cy = s * dt * (1. / t.dx);
+  const double cx = s * dt * t.rcp_dy, cy = s * dt * t.rcp_dx;
   const double *aBx = a.aBnew + static_cast<size_t>(t.slot) * 2 * NN, *aBy = aBx + NN;
   double *aS = a.aBsrc + static_cast<size_t>(t.slot) * 2 * NN;
   double *aE = a.aE + static_cast<size_t>(t.slot) * NN;

@@ -33,6 +33,9 @@ struct LeafTask {
   // 1/dx and 1/dy when dx, dy are powers of two (then x/dx == x*(1/dx)
   // exactly, and the residual multiplies instead of dividing); 0 otherwise
   double inv_dx, inv_dy;
+  // 1./dx and 1./dy rounded as the device division rounds them (IEEE), for
+  // the formulas that multiply by the rounded reciprocal (CT2D.cpp:80,86)
+  double rcp_dx, rcp_dy;
 };
 
 // 1/v if v is a power of two (exact reciprocal), else 0

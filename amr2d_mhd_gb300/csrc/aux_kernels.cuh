@@ -128,9 +128,13 @@ __global__ void k_ct_emf(CtArgs a) {
   for (int c = threadIdx.x; c < NN; c += blockDim.x) {
     const int i = c % N, j = c / N;
     if (i < 1 || j < 1) continue;
-    const double g5a = gg[5 * NN + j * N + i - 1], g5b = gg[5 * NN + c];
-    const double f6a = ff[6 * NN + (j - 1) * N + i], f6b = ff[6 * NN + c];
-    E[c] = 0.25 * ((g5a + g5b) - (f6a + f6b));
+    // in the storage type of the fluxes: FP64 on the FP64 path (the
+    // reference's arithmetic); FP32 fluxes give an FP32 EMF, stored in the
+    // FP64 array (the face update below stays FP64, so div B keeps FP64
+    // round-off whatever the EMF's precision)
+    const S g5a = gg[5 * NN + j * N + i - 1], g5b = gg[5 * NN + c];
+    const S f6a = ff[6 * NN + (j - 1) * N + i], f6b = ff[6 * NN + c];
+    E[c] = static_cast<double>(S(0.25) * ((g5a + g5b) - (f6a + f6b)));
   }
 }
 
@@ -146,10 +150,10 @@ __global__ void k_ct_face(CtArgs a) {
   for (int c = threadIdx.x; c < NN; c += blockDim.x) {
     const int i = c % N, j = c / N;
     const int ip = i < N - 1 ? i + 1 : i, jp = j < N - 1 ? j + 1 : j;
-    double res = (1. / t.dy) * (E[jp * N + i] - E[c]);
+    double res = t.rcp_dy * (E[jp * N + i] - E[c]);
     if (a.step == 1) B1[c] = B0[c] - dt * res;
     else B1[c] = 0.5 * (B0[c] + B1[c] - dt * res);
-    res = -(1. / t.dx) * (E[j * N + ip] - E[c]);
+    res = -t.rcp_dx * (E[j * N + ip] - E[c]);
     if (a.step == 1) B1[NN + c] = B0[NN + c] - dt * res;
     else B1[NN + c] = 0.5 * (B0[NN + c] + B1[NN + c] - dt * res);
   }
@@ -167,13 +171,14 @@ __global__ void k_ct_cell(CtArgs a) {
     const int i = c % N, j = c / N;
     const int ip = i < N - 1 ? i + 1 : i, ii = ip - 1;
     const int jp = j < N - 1 ? j + 1 : j, jj = jp - 1;
-    const double bx = 0.5 * (B[j * N + ip] + B[j * N + ii]);
-    const double by = 0.5 * (B[NN + jp * N + i] + B[NN + jj * N + i]);
-    const double q5 = q[5 * NN + c], q6 = q[6 * NN + c];
-    q[4 * NN + c] = static_cast<S>(static_cast<double>(q[4 * NN + c]) +
-                                   0.5 * ((bx * bx + by * by) - (q5 * q5 + q6 * q6)));
-    q[5 * NN + c] = static_cast<S>(bx);
-    q[6 * NN + c] = static_cast<S>(by);
+    // face averages from the FP64 face field, rounded once to the storage
+    // type; the energy correction in the storage type (FP64 on the FP64 path)
+    const S bx = static_cast<S>(0.5 * (B[j * N + ip] + B[j * N + ii]));
+    const S by = static_cast<S>(0.5 * (B[NN + jp * N + i] + B[NN + jj * N + i]));
+    const S q5 = q[5 * NN + c], q6 = q[6 * NN + c];
+    q[4 * NN + c] = q[4 * NN + c] + S(0.5) * ((bx * bx + by * by) - (q5 * q5 + q6 * q6));
+    q[5 * NN + c] = bx;
+    q[6 * NN + c] = by;
   }
 }
 

@@ -495,7 +495,7 @@ int Engine::rebuild() {
       if (!in.tree.leafs[nb]) continue;
       const int lev = in.tree.lp[nb][0];
       tasks_.push_back(LeafTask{in.slot[nb], a, in.dx[lev], in.dy[lev], exact_reciprocal(in.dx[lev]),
-                                exact_reciprocal(in.dy[lev])});
+                                exact_reciprocal(in.dy[lev]), 1. / in.dx[lev], 1. / in.dy[lev]});
       task_blk_.push_back(nb);
     }
     in.task_end = static_cast<int>(tasks_.size());

@@ -254,6 +254,7 @@ def run_rotor_batch(stream, steps):
             sim.run(50)
         tune = sim.autotune(2)
         sim.run(3)
+        sim.profile(True)
         c0 = sum(sim.info(q)["cell_updates"] for q in range(ROTOR_BATCH))
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -263,8 +264,14 @@ def run_rotor_batch(stream, steps):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         c1 = sum(sim.info(q)["cell_updates"] for q in range(ROTOR_BATCH))
+        p = sim.profile()
         out[prec] = dict(value=(c1 - c0) / (ms * 1e-3), ms_per_step=ms / steps,
-                         schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"))
+                         schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"),
+                         step_gpu_ms_per_step=p["step_gpu_ms"] / steps,
+                         stage_kernel_ms_per_step=p["stage_ms"] / steps,
+                         host_compile_ms_per_step=p["host_compile_ms"] / steps,
+                         host_admesh_ms_per_step=p["host_admesh_ms"] / steps,
+                         host_capture_ms_per_step=p["host_capture_ms"] / steps)
         sim.close()
     return out
 
@@ -302,6 +309,8 @@ def run_batch(stream, steps, advance):
         out[prec] = dict(value=(c1 - c0) / (ms * 1e-3), ms_per_step=ms / steps,
                          leaves=sum(sim.info(q)["n_leaves"] for q in range(BATCH_N)),
                          host_ms_per_step=(p["host_compile_ms"] + p["host_admesh_ms"]) / steps,
+                         step_gpu_ms_per_step=p["step_gpu_ms"] / steps,
+                         stage_kernel_ms_per_step=p["stage_ms"] / steps,
                          gpu_launches=int(p["launches"]),
                          schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"))
         sim.close()
@@ -537,7 +546,7 @@ def main():
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: the rotor from its initial condition for this many steps, then exit")
     ap.add_argument("--ncu-t0", type=float, default=0.0,
-                    help="with --ncu-case: first advance the rotor to this time (untimed), then run the steps")
+                    help="with --ncu-case / --ncu-rotor-batch: first advance to this time (untimed), then run the steps")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="precision of --ncu-case")
     ap.add_argument("--ncu-rotor-batch", type=int, default=0,
                     help="profiling case: the %d-rotor batch, fused stage kernel, this many steps, then exit"
@@ -564,8 +573,13 @@ def main():
         os.environ["AMR2D_STAGE_KERNEL"] = "fused"
         sim = amr.Simulation([amr.make_config(precision=args.precision, **WORKLOAD) for _ in range(ROTOR_BATCH)])
         sim.init()
+        sim.profile(True)
+        if args.ncu_t0 > 0:
+            while sim.info(0)["t"] < args.ncu_t0:
+                sim.run(50)
+        before = sim.profile()["launches"]
         sim.run(args.ncu_rotor_batch)
-        print(json.dumps(sim.info()))
+        print(json.dumps(dict(sim.info(), launches_before=before, launches=sim.profile()["launches"] - before)))
         return 0
     if args.ncu_case:
         import amr2d_mhd_gb300 as amr
