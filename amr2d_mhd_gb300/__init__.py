@@ -48,7 +48,8 @@ class Config(ctypes.Structure):
                 ("nroots_x", ctypes.c_int32), ("nroots_y", ctypes.c_int32), ("periodic", ctypes.c_int32),
                 ("geometry", ctypes.c_int32), ("gamma", ctypes.c_double), ("t_end", ctypes.c_double),
                 ("ic_param", ctypes.c_double * 24), ("precision", ctypes.c_int32),
-                ("reserved0", ctypes.c_int32), ("dt_fixed", ctypes.c_double), ("reserved", ctypes.c_int32 * 4)]
+                ("reserved0", ctypes.c_int32), ("dt_fixed", ctypes.c_double), ("ct_type", ctypes.c_int32),
+                ("diffusion", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class Info(ctypes.Structure):
@@ -131,7 +132,7 @@ def load(build_if_missing: bool = True):
 
 def make_config(ic="rotor", limiter="MC", flux="RUSA", cfl=0.5, maxlevs=5, nghosts=2, nroots=(2, 2),
                 periodic=False, geometry=0, gamma=0.0, t_end=0.0, ic_param=None, precision="fp64",
-                lenx=1.0, leny=1.0, nx=16, ny=16, input_txt=None) -> Config:
+                lenx=1.0, leny=1.0, nx=16, ny=16, input_txt=None, ct_type=1, diffusion=False) -> Config:
     """An amr_config; defaults are the reference's input.txt and defs.hpp."""
     L = load()
     c = Config()
@@ -150,6 +151,7 @@ def make_config(ic="rotor", limiter="MC", flux="RUSA", cfl=0.5, maxlevs=5, nghos
     for i, v in enumerate(ic_param or []):
         c.ic_param[i] = v
     c.precision = {"fp64": 0, "fp32": 1}[precision]
+    c.ct_type, c.diffusion = ct_type, int(diffusion)
     return c
 
 

@@ -37,6 +37,8 @@ int Engine::adjoint_supported() {
       return fail(AMR_E_UNSUPPORTED, "the adjoint covers the MC and minmod limiters");
     if (in.cfg.maxlevs != 1) return fail(AMR_E_UNSUPPORTED, "the adjoint needs a frozen mesh (maxlevs 1)");
     if (!(in.cfg.dt_fixed > 0)) return fail(AMR_E_UNSUPPORTED, "the adjoint needs a fixed dt (dt_fixed > 0)");
+    if (in.cfg.ct_type == 2 || in.cfg.diffusion)
+      return fail(AMR_E_UNSUPPORTED, "the adjoint covers the basic CT EMF without diffusion");
   }
   return AMR_OK;
 }
@@ -123,6 +125,7 @@ int Engine::ct2d_taped(int step) {
   a.Bsrc = step == 1 ? Bi_ : Bis_;
   a.Bnew = step == 1 ? Bis_ : Bi_;
   a.q = step == 1 ? Us_ : U_;
+  a.err = d_err_.as<DevError>();
   a.step = step;
   const int n = static_cast<int>(tasks_.size());
   const size_t cell = sizeof(double) * 8 * nn_ * used_slots_, face = sizeof(double) * 2 * nn_ * used_slots_;

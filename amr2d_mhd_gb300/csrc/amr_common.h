@@ -17,7 +17,8 @@ enum Recon { REC_MUSCL = 0, REC_WENO3 = 1, REC_WENO5 = 2 };
 enum Flux { FLX_RUSA = 0, FLX_HLLE, FLX_HLLC, FLX_HLLD, FLX_ROE };
 
 // device error word: first failure wins (code, block, i, j)
-enum DevErr { DERR_NONE = 0, DERR_PRESSURE = 1, DERR_NAN = 2, DERR_HLLC = 3, DERR_REFINE_NAN = 4, DERR_TIMEOUT = 5 };
+enum DevErr { DERR_NONE = 0, DERR_PRESSURE = 1, DERR_NAN = 2, DERR_HLLC = 3, DERR_REFINE_NAN = 4, DERR_TIMEOUT = 5,
+              DERR_PSI = 6 };
 struct DevError {
   int code;
   int blk;
@@ -36,7 +37,11 @@ struct LeafTask {
   // 1./dx and 1./dy rounded as the device division rounds them (IEEE), for
   // the formulas that multiply by the rounded reciprocal (CT2D.cpp:80,86)
   double rcp_dx, rcp_dy;
+  int flags;      // TASK_DIFFUSE
+  int pad;
 };
+// the block takes diffusivity.cpp after stage 2 (main.cpp:190-193)
+constexpr int TASK_DIFFUSE = 1;
 
 // 1/v if v is a power of two (exact reciprocal), else 0
 inline double exact_reciprocal(double v) {
@@ -51,7 +56,7 @@ struct InstParams {
   double gamma;
   double dt;      // dom.dt of the current step
   int limiter;
-  int pad;
+  int ct_type;    // 2 = upwind-switched EMF (CT2D.cpp:28-75), else the average
 };
 
 // One gather of a compiled ghost fill (see ghost_compile.cpp).  The same op

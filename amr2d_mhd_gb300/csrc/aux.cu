@@ -120,6 +120,12 @@ cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int n, cudaStream_t
   return cudaGetLastError();
 }
 
+cudaError_t launch_diffuse(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  AMR_DISPATCH_NG_S(m, k_diffuse, n, 128, 0, s, a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   AMR_DISPATCH_NG_S(m, k_ct_cell, n, 128, 0, s, a);

@@ -114,14 +114,68 @@ struct CtArgs {
   const double *Bsrc;     // CT2D's Bi argument
   double *Bnew;           // CT2D's Binew argument
   void *q;                // cell state corrected by the face average
+  DevError *err;
   int step;
 };
+
+// CT2D.cpp:28-75, CTtype 2 ("upwind (not ready)", defs.hpp:34), for the block
+// of task t: pressure and speed of every cell of q in shared memory (:36-40),
+// then the corner EMF weighting the two flux averages by psi, which stays 1/2
+// unless the corner sits at a strong pressure jump (beta = 0.5) in a strongly
+// compressive flow (delta = 0.1).  Two terms of the divergence divide rho*v
+// by itself (:53), as the reference does.  Arithmetic in the storage type S
+// (FP64 on the FP64 path, in the reference's order).
+template <int NG, typename S>
+__device__ __forceinline__ void ct_emf_upwind(const CtArgs &a, const LeafTask &t, S *sp, S *sC) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  const S g = static_cast<S>(a.inst[t.inst].gamma);
+  const S *q = static_cast<const S *>(a.q) + static_cast<size_t>(t.slot) * 8 * NN;
+  const S *ff = static_cast<const S *>(a.ff) + static_cast<size_t>(t.slot) * 8 * NN;
+  const S *gg = static_cast<const S *>(a.gg) + static_cast<size_t>(t.slot) * 8 * NN;
+  double *E = a.EMF + static_cast<size_t>(t.slot) * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const S q0 = q[c], q1 = q[NN + c], q2 = q[2 * NN + c], q3 = q[3 * NN + c];
+    const S q4 = q[4 * NN + c], q5 = q[5 * NN + c], q6 = q[6 * NN + c], q7 = q[7 * NN + c];
+    sp[c] = (g - S(1)) * (q4 - S(0.5) * ((q1 * q1 + q2 * q2 + q3 * q3) / q0 + (q5 * q5 + q6 * q6 + q7 * q7)));
+    sC[c] = sqrt((g * sp[c] + (q5 * q5 + q6 * q6 + q7 * q7)) / q0);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    if (i < 1 || j < 1) continue;
+    const int w = c - 1, s = c - N, sw = c - N - 1;  // (i-1,j), (i,j-1), (i-1,j-1)
+    const S beta = S(0.5), delta = S(0.1);
+    const S dPx = S(0.5) * fabs(sp[c] + sp[s] - sp[w] - sp[sw]);
+    const S dPy = S(0.5) * fabs(sp[c] + sp[w] - sp[s] - sp[sw]);
+    const S divV = S(0.5) * (q[NN + c] / q[c] + q[NN + s] / q[s] - q[NN + w] / q[w] - q[NN + sw] / q[sw]) +
+                   S(0.5) * (q[2 * NN + c] / q[c] + q[2 * NN + w] / q[2 * NN + w] - q[2 * NN + s] / q[2 * NN + s] -
+                             q[2 * NN + sw] / q[sw]);
+    S tempP = mmin(sp[sw], sp[s]);
+    const S tempP1 = mmin(sp[w], sp[c]);
+    tempP = mmin(tempP, tempP1);
+    const bool sw1 = (dPx + dPy) > beta * tempP;
+    S tempC = mmin(sC[sw], sC[s]);
+    const S tempC1 = mmin(sC[w], sC[c]);
+    tempC = mmin(tempC, tempC1);
+    const bool sw2 = (-delta * tempC) > divV;
+    S psi = S(0.5);
+    if (sw1 && sw2) psi = dPx / (dPx + dPy);
+    if (psi < S(0) || psi > S(1)) dev_fail(a.err, DERR_PSI, t.slot, i, j, static_cast<double>(psi));
+    E[c] = static_cast<double>(S(0.5) * (S(1.) - psi) * (gg[5 * NN + c - 1] + gg[5 * NN + c]) -
+                               S(0.5) * psi * (ff[6 * NN + c - N] + ff[6 * NN + c]));
+  }
+}
 
 // CT2D.cpp:16-26 corner EMF for i, j in [1, N)
 template <int NG, typename S>
 __global__ void k_ct_emf(CtArgs a) {
   constexpr int N = Geo<NG>::N, NN = N * N;
   const LeafTask t = a.tasks[blockIdx.x];
+  if (a.inst[t.inst].ct_type == 2) {
+    __shared__ S sp[NN], sC[NN];
+    ct_emf_upwind<NG, S>(a, t, sp, sC);
+    return;
+  }
   const S *ff = static_cast<const S *>(a.ff) + static_cast<size_t>(t.slot) * 8 * NN;
   const S *gg = static_cast<const S *>(a.gg) + static_cast<size_t>(t.slot) * 8 * NN;
   double *E = a.EMF + static_cast<size_t>(t.slot) * NN;
@@ -179,6 +233,38 @@ __global__ void k_ct_cell(CtArgs a) {
     q[4 * NN + c] = q[4 * NN + c] + S(0.5) * ((bx * bx + by * by) - (q5 * q5 + q6 * q6));
     q[5 * NN + c] = bx;
     q[6 * NN + c] = by;
+  }
+}
+
+// diffusivity.cpp:6-17 on the blocks flagged TASK_DIFFUSE (main.cpp:190-193:
+// after stage 2, level >= maxlevs - 2): U += eta * (5-point Laplacian) over
+// the interior, eta = 0.001 (defs.hpp:50).  The reference sweeps in place
+// with i outer and j inner, so a cell sees the new (i-1, j) and (i, j-1) and
+// the old (i+1, j) and (i, j+1): the CTA sweeps the anti-diagonals i + j of
+// the block in shared memory, 8 variables x 16 cells per diagonal.
+template <int NG, typename S>
+__global__ void __launch_bounds__(128) k_diffuse(CtArgs a) {
+  constexpr int N = Geo<NG>::N, NN = N * N, I0 = NG;  // interior [nxmin, nxmax] = [NG, NG + NI - 1]
+  const LeafTask t = a.tasks[blockIdx.x];
+  if (!(t.flags & TASK_DIFFUSE)) return;
+  __shared__ S u[8 * NN];
+  S *q = static_cast<S *>(a.q) + static_cast<size_t>(t.slot) * 8 * NN;
+  for (int e = threadIdx.x; e < 8 * NN; e += blockDim.x) u[e] = q[e];
+  __syncthreads();
+  const S eta = S(0.001);
+  const int k = threadIdx.x / NI, m = threadIdx.x % NI;
+  for (int d = 0; d <= 2 * (NI - 1); d++) {
+    const int i0 = (d > NI - 1 ? d - (NI - 1) : 0) + m;
+    if (i0 <= (d < NI - 1 ? d : NI - 1)) {
+      S *c = u + k * NN + (I0 + d - i0) * N + (I0 + i0);
+      *c = *c + eta * (c[1] + c[-1] + c[N] + c[-N] - S(4.) * *c);
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < 8 * NI * NI; e += blockDim.x) {
+    const int kk = e / (NI * NI), r = e % (NI * NI);
+    const int at = kk * NN + (I0 + r / NI) * N + I0 + r % NI;
+    q[at] = u[at];
   }
 }
 

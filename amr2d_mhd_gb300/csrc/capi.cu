@@ -52,6 +52,7 @@ const char *amr_status_string(int s) {
     case AMR_E_UNSUPPORTED: return "unsupported option";
     case AMR_E_ARG: return "bad argument";
     case AMR_E_TOO_LARGE: return "size above a fixed scratch capacity";
+    case AMR_E_CT: return "incorrect psi produced (upwind CT EMF)";
     default: return "unknown status";
   }
 }

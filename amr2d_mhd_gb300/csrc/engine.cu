@@ -68,6 +68,7 @@ int map_dev_error(int code) {
     case DERR_PRESSURE: return AMR_E_PRESSURE;
     case DERR_HLLC: return AMR_E_HLLC;
     case DERR_TIMEOUT: return AMR_E_TIMEOUT;
+    case DERR_PSI: return AMR_E_CT;
     default: return AMR_E_NAN;
   }
 }
@@ -135,6 +136,8 @@ int Engine::create(const amr_config *cfgs, int n) {
     if (fl == FLX_ROE) return fail(AMR_E_UNSUPPORTED, "ROE not ready with magnetic field (riemannS.cpp:39-40)");
     if (ic_from_name(c.ic) == IC_INVALID) return fail(AMR_E_CONFIG, std::string("no valid initial condition '") + c.ic + "'");
     if (lim == LIM_WENO5 && c.nghosts < 4) return fail(AMR_E_CONFIG, "WENO5 needs nghosts = 4");
+    if (c.ct_type < 0 || c.ct_type > 2) return fail(AMR_E_CONFIG, "ct_type must be 1 (or 0) or 2");
+    if (c.diffusion != 0 && c.diffusion != 1) return fail(AMR_E_CONFIG, "diffusion must be 0 or 1");
     // a batch shares the kernels: same method and block shape
     auto family = [](int l) { return l == LIM_WENO3 ? 1 : (l == LIM_WENO5 ? 2 : 0); };
     if (q > 0 && family(lim) != family(lim_from_name(c0.limiter)))
@@ -488,14 +491,17 @@ int Engine::rebuild() {
   if (int rc = compile_programs()) return rc;
   tasks_.clear();
   task_blk_.clear();
+  diffuse_any_ = false;
   for (int a : active_) {
     Instance &in = inst_[a];
     in.task_begin = static_cast<int>(tasks_.size());
     for (int nb = 0; nb < in.tree.lastActive; nb++) {
       if (!in.tree.leafs[nb]) continue;
       const int lev = in.tree.lp[nb][0];
+      const int flags = in.cfg.diffusion && lev >= in.cfg.maxlevs - 2 ? TASK_DIFFUSE : 0;
+      diffuse_any_ |= flags != 0;
       tasks_.push_back(LeafTask{in.slot[nb], a, in.dx[lev], in.dy[lev], exact_reciprocal(in.dx[lev]),
-                                exact_reciprocal(in.dy[lev]), 1. / in.dx[lev], 1. / in.dy[lev]});
+                                exact_reciprocal(in.dy[lev]), 1. / in.dx[lev], 1. / in.dy[lev], flags, 0});
       task_blk_.push_back(nb);
     }
     in.task_end = static_cast<int>(tasks_.size());
@@ -526,7 +532,7 @@ void Engine::fill_params_host() {
     p[q].gamma = inst_[q].gamma;
     p[q].dt = inst_[q].dt;
     p[q].limiter = inst_[q].limiter;
-    p[q].pad = 0;
+    p[q].ct_type = inst_[q].cfg.ct_type == 2 ? 2 : 1;
   }
 }
 
@@ -614,6 +620,13 @@ int Engine::stage(int step) {
     if (int rc = ev_begin()) return rc;
     CK(launch_stage(m_, a, n, stream_), "stage kernel");
     if (int rc = ev_end()) return rc;
+    prof_.launches += 1;
+  }
+  if (step == 2 && diffuse_any_) {  // main.cpp:190-193, after each block's stage-2 update
+    CtArgs d{};
+    d.tasks = d_tasks_.as<LeafTask>();
+    d.q = U_;
+    CK(launch_diffuse(m_, d, n, stream_), "diffusion kernel");
     prof_.launches += 1;
   }
   prof_.stage_launches += 1;
@@ -708,6 +721,7 @@ int Engine::ct2d(int step) {
   a.Bsrc = step == 1 ? Bi_ : Bis_;
   a.Bnew = step == 1 ? Bis_ : Bi_;
   a.q = step == 1 ? Us_ : U_;
+  a.err = d_err_.as<DevError>();
   a.step = step;
   const int n = static_cast<int>(tasks_.size());
   CK(launch_ct_emf(m_, a, n, stream_), "ct emf");

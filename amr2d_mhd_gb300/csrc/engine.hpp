@@ -178,6 +178,7 @@ class Engine {
   amr_profile prof_{};
   std::vector<cudaEvent_t> ev_;     // start/stop pairs of this step's stage launches
   int ev_used_ = 0;
+  bool diffuse_any_ = false;  // some leaf task carries TASK_DIFFUSE
   cudaEvent_t step_ev_[2] = {nullptr, nullptr};  // brackets the step's device work (profiling)
   bool step_ev_pending_ = false;
   int64_t stage_cells_pending_ = 0;

@@ -55,6 +55,8 @@ cudaError_t launch_ghost(const Method &m, const GhostLaunch &g, cudaStream_t s);
 cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
+// diffusivity.cpp on the tasks flagged TASK_DIFFUSE (a.q = U after stage 2)
+cudaError_t launch_diffuse(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 // per-leaf max wave speed and refinement criterion from the primitive state
 cudaError_t launch_dt_cell(const Method &m, const DtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int nops, cudaStream_t s);

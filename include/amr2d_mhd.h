@@ -40,7 +40,8 @@ typedef enum amr_status {
   AMR_E_TIMEOUT = -10,    /* a bounded device wait gave up */
   AMR_E_UNSUPPORTED = -11,/* ROE with a magnetic field (riemannS.cpp:39-40), block size != 16 */
   AMR_E_ARG = -12,        /* bad pointer, size or index */
-  AMR_E_TOO_LARGE = -13   /* more blocks than a fixed-size scratch array holds */
+  AMR_E_TOO_LARGE = -13,  /* more blocks than a fixed-size scratch array holds */
+  AMR_E_CT = -14          /* CT2D.cpp:67 "Incorrect psi produced" (ct_type 2) */
 } amr_status;
 
 typedef enum amr_precision {
@@ -83,7 +84,11 @@ typedef struct amr_config {
   int32_t reserved0;
   double dt_fixed;        /* extension: > 0 = every step uses this dt (no CFL
                              reduction, no lag); 0 = main.cpp:322-347 */
-  int32_t reserved[4];
+  int32_t ct_type;        /* defs.hpp:34 CTtype: 0 or 1 = basic EMF average, 2 = the
+                             upwind-switched EMF of CT2D.cpp:28-75 */
+  int32_t diffusion;      /* defs.hpp:35 diffusion: 1 = diffusivity.cpp after stage 2
+                             on blocks at level >= maxlevs - 2 (main.cpp:190-193) */
+  int32_t reserved[2];
 } amr_config;
 
 typedef struct amr_info {

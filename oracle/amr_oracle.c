@@ -1076,21 +1076,92 @@ static void locate_bounds(oracle *o) {
   }
 }
 
+/* diffusivity.cpp:6-17 on one block (main.cpp:190-193 applies it after the
+ * stage-2 update of every leaf at level >= maxlevs - 2 when `diffusion` is
+ * on): U += eta * (5-point Laplacian) over the interior, in place with i
+ * outer and j inner, so a cell sees the new values of its (i-1, j) and
+ * (i, j-1) neighbours; eta = 0.001 (defs.hpp:50). */
+static void diffuse(oracle *o, double *U, int nb) {
+  const double eta = 0.001;
+  for (int i = o->nxmin; i <= o->nxmax; i++)
+    for (int j = o->nymin; j <= o->nymax; j++)
+      for (int k = 0; k < 8; k++)
+        Qc(U, nb, k, i, j) = Qc(U, nb, k, i, j) + eta * (Qc(U, nb, k, i + 1, j) + Qc(U, nb, k, i - 1, j) +
+                                                         Qc(U, nb, k, i, j + 1) + Qc(U, nb, k, i, j - 1) -
+                                                         4. * Qc(U, nb, k, i, j));
+}
+
 /* ---------------------------------------------------------------- CT2D.cpp */
-/* CT2D.cpp:11-124 with CTtype==1 (defs.hpp:34).  q is the cell state being
- * corrected, Bi the face field at the start of the stage, Binew the output. */
+/* CT2D.cpp:28-75, CTtype == 2 ("upwind (not ready)", defs.hpp:34) for one
+ * block: pressure p and speed C of every cell of q (:36-40), then the corner
+ * EMF weighting the two flux averages by psi, which leaves 1/2 unless the
+ * corner sits at a strong pressure jump (switch 1, beta = 0.5) in a strongly
+ * compressive flow (switch 2, delta = 0.1).  The divergence term divides
+ * rho*v by itself at two of its corners (:53), as the reference does.
+ * Returns 1 on the reference's "Incorrect psi produced" (:67). */
+static int emf_upwind(oracle *o, const double *q, int nb) {
+  const int nx = o->nx, ny = o->ny;
+  const double g = o->gamma;
+  double *p = (double *)malloc(sizeof(double) * 2 * nx * ny), *C = p + nx * ny;
+  int bad = 0;
+#define PC(A, i, j) (A)[(j) * nx + (i)]
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      double q0 = Qc(q, nb, 0, i, j), q1 = Qc(q, nb, 1, i, j), q2 = Qc(q, nb, 2, i, j), q3 = Qc(q, nb, 3, i, j);
+      double q4 = Qc(q, nb, 4, i, j), q5 = Qc(q, nb, 5, i, j), q6 = Qc(q, nb, 6, i, j), q7 = Qc(q, nb, 7, i, j);
+      PC(p, i, j) = (g - 1) * (q4 - 0.5 * ((q1 * q1 + q2 * q2 + q3 * q3) / q0 + (q5 * q5 + q6 * q6 + q7 * q7)));
+      PC(C, i, j) = sqrt((g * PC(p, i, j) + (q5 * q5 + q6 * q6 + q7 * q7)) / q0);
+    }
+  for (int i = 1; i < nx; i++)
+    for (int j = 1; j < ny; j++) {
+      const double beta = 0.5, delta = 0.1;
+      double dPx = 0.5 * fabs(PC(p, i, j) + PC(p, i, j - 1) - PC(p, i - 1, j) - PC(p, i - 1, j - 1));
+      double dPy = 0.5 * fabs(PC(p, i, j) + PC(p, i - 1, j) - PC(p, i, j - 1) - PC(p, i - 1, j - 1));
+      double divV = 0.5 * (Qc(q, nb, 1, i, j) / Qc(q, nb, 0, i, j) + Qc(q, nb, 1, i, j - 1) / Qc(q, nb, 0, i, j - 1) -
+                           Qc(q, nb, 1, i - 1, j) / Qc(q, nb, 0, i - 1, j) -
+                           Qc(q, nb, 1, i - 1, j - 1) / Qc(q, nb, 0, i - 1, j - 1)) +
+                    0.5 * (Qc(q, nb, 2, i, j) / Qc(q, nb, 0, i, j) + Qc(q, nb, 2, i - 1, j) / Qc(q, nb, 2, i - 1, j) -
+                           Qc(q, nb, 2, i, j - 1) / Qc(q, nb, 2, i, j - 1) -
+                           Qc(q, nb, 2, i - 1, j - 1) / Qc(q, nb, 0, i - 1, j - 1));
+      double tempP = MMIN(PC(p, i - 1, j - 1), PC(p, i, j - 1));
+      double tempP1 = MMIN(PC(p, i - 1, j), PC(p, i, j));
+      tempP = MMIN(tempP, tempP1);
+      int sw1 = (dPx + dPy) > beta * tempP;
+      double tempC = MMIN(PC(C, i - 1, j - 1), PC(C, i, j - 1));
+      double tempC1 = MMIN(PC(C, i - 1, j), PC(C, i, j));
+      tempC = MMIN(tempC, tempC1);
+      int sw2 = (-delta * tempC) > divV;
+      double psi = 0.5;
+      if (sw1 && sw2) psi = dPx / (dPx + dPy);
+      if (psi < 0 || psi > 1) bad = 1;
+      Qe(o->EMF, nb, i, j) = 0.5 * (1. - psi) * (Qc(o->gg, nb, 5, i - 1, j) + Qc(o->gg, nb, 5, i, j)) -
+                             0.5 * psi * (Qc(o->ff, nb, 6, i, j - 1) + Qc(o->ff, nb, 6, i, j));
+    }
+#undef PC
+  free(p);
+  return bad;
+}
+
+/* CT2D.cpp:11-124.  q is the cell state being corrected, Bi the face field
+ * at the start of the stage, Binew the output. */
 static int ct2d(oracle *o, double *q, double *Bi, int step, double *Binew) {
   int nL = 0;
   int *leaf = (int *)malloc(sizeof(int) * (o->lastActive + 1));
   for (int nb = 0; nb < o->lastActive; nb++) if (o->leafs[nb]) leaf[nL++] = nb;
-#pragma omp parallel for schedule(static) num_threads(o->nthreads)
+  int bad = 0;
+#pragma omp parallel for schedule(static) num_threads(o->nthreads) reduction(| : bad)
   for (int l = 0; l < nL; l++) {
     int nb = leaf[l];
+    if (o->c.ct_type == 2) {
+      bad |= emf_upwind(o, q, nb);
+      continue;
+    }
     for (int i = 1; i < o->nx; i++)
       for (int j = 1; j < o->ny; j++)
         Qe(o->EMF, nb, i, j) = 0.25 * ((Qc(o->gg, nb, 5, i - 1, j) + Qc(o->gg, nb, 5, i, j)) -
                                        (Qc(o->ff, nb, 6, i, j - 1) + Qc(o->ff, nb, 6, i, j)));
   }
+  if (bad) { free(leaf); return fail(o, "Incorrect psi produced"); }
   fill_ec(o, o->EMF);
   double dt = o->dt;
 #pragma omp parallel for schedule(static) num_threads(o->nthreads)
@@ -1688,14 +1759,19 @@ int oracle_step(oracle *o) {
   fill_fc(o, o->Bi, 2);
   fill_fc(o, o->ff, 8);
   fill_fc(o, o->gg, 8);
-  ct2d(o, o->Us, o->Bi, 1, o->Bis);
+  if (ct2d(o, o->Us, o->Bi, 1, o->Bis)) { free(leaf); return -1; }
   fill_cc(o, o->Us);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(o->nthreads) reduction(| : bad)
   for (int l = 0; l < nL; l++) bad |= muscl_rk(o, leaf[l], 2) != 0;
   if (bad) { free(leaf); return -1; }
+  if (o->c.diffusion) {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(o->nthreads)
+    for (int l = 0; l < nL; l++)
+      if (o->lp[leaf[l]][0] >= o->c.maxlevs - 2) diffuse(o, o->U, leaf[l]);
+  }
   fill_fc(o, o->ff, 8);
   fill_fc(o, o->gg, 8);
-  ct2d(o, o->U, o->Bis, 2, o->Bi);
+  if (ct2d(o, o->U, o->Bis, 2, o->Bi)) { free(leaf); return -1; }
   fill_cc(o, o->U);
   /* main.cpp:322-343 dt; note lambda1 takes |rho| + c_f,x (W[..][0], main.cpp:335) */
   double lambda = 1.E6;

@@ -49,6 +49,8 @@ typedef struct oracle_cfg {
   double ic_param[24];   /* extension ICs: blast / KH parameters */
   int nthreads;          /* OpenMP threads over blocks (0 = default) */
   double dt_fixed;       /* extension: > 0 = every step uses this dt */
+  int ct_type;           /* defs.hpp:34 CTtype: 1 (0 = 1) basic, 2 upwind EMF */
+  int diffusion;         /* defs.hpp:35 diffusion: 0 off, 1 on */
 } oracle_cfg;
 
 /* what oracle_get copies */

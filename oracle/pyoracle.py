@@ -51,7 +51,8 @@ class _Cfg(ctypes.Structure):
                 ("lenx", ctypes.c_double), ("leny", ctypes.c_double), ("cfl", ctypes.c_double),
                 ("ic", ctypes.c_int), ("limiter", ctypes.c_int), ("flux", ctypes.c_int),
                 ("gamma_override", ctypes.c_double), ("tend_override", ctypes.c_double),
-                ("ic_param", ctypes.c_double * 24), ("nthreads", ctypes.c_int), ("dt_fixed", ctypes.c_double)]
+                ("ic_param", ctypes.c_double * 24), ("nthreads", ctypes.c_int), ("dt_fixed", ctypes.c_double),
+                ("ct_type", ctypes.c_int), ("diffusion", ctypes.c_int)]
 
 
 _lib = None
@@ -97,7 +98,7 @@ class Oracle:
 
     def __init__(self, ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=4, nx=16, ny=16,
                  nghosts=2, nroots=(2, 2), periodic=False, geom_ref=True, lenx=1.0, leny=1.0,
-                 gamma=0.0, tend=0.0, ic_param=None, nthreads=1, dt_fixed=0.0):
+                 gamma=0.0, tend=0.0, ic_param=None, nthreads=1, dt_fixed=0.0, ct_type=1, diffusion=False):
         c = _Cfg()
         c.nx_int, c.ny_int, c.nghosts, c.maxlevs = nx, ny, nghosts, maxlevs
         c.nroots_x, c.nroots_y = nroots
@@ -109,6 +110,7 @@ class Oracle:
             c.ic_param[i] = v
         c.nthreads = nthreads
         c.dt_fixed = dt_fixed
+        c.ct_type, c.diffusion = ct_type, int(diffusion)
         self._cfg = c
         self.h = lib().oracle_create(ctypes.byref(c))
         if not self.h:

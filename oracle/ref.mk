@@ -8,16 +8,23 @@
 #   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=shipped   # makefile:9-13 flags
 #   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=nofma     # same + -ffp-contract=off
 #   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=omp       # same as shipped + USE_OMP
+#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=nofma CTTYPE=2 DIFFUSION=true
 #
-# The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>/main.x; run it in a directory
+# The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>[_CT2][_DIFF]/main.x; run it in a directory
 # holding input.txt with stdin "2\n0\n" (main.cpp:188,388).
 
 REF     ?= /root/reference
 MAXLEVS ?= 5
 NGHOSTS ?= 2
 FLAVOR  ?= shipped
+# CTtype (defs.hpp:34, 1 basic / 2 upwind) and diffusion (defs.hpp:35), also
+# compile-time constants of the reference; non-default values get their own
+# build directory
+CTTYPE    ?= 1
+DIFFUSION ?= false
 HERE    := $(dir $(lastword $(MAKEFILE_LIST)))
-OUT     := $(HERE)_ref/L$(MAXLEVS)_G$(NGHOSTS)_$(FLAVOR)
+VARIANT := $(if $(filter-out 1,$(CTTYPE)),_CT$(CTTYPE))$(if $(filter true,$(DIFFUSION)),_DIFF)
+OUT     := $(HERE)_ref/L$(MAXLEVS)_G$(NGHOSTS)_$(FLAVOR)$(VARIANT)
 
 CXX     ?= g++
 # makefile:9-13 of the reference
@@ -55,9 +62,13 @@ $(OUT)/kat.x: $(OUT)/ref_kat.o $(OUT)/riemannS.o $(OUT)/misc.o $(OUT)/slopelimit
 $(OUT)/defs.hpp: $(REF)/defs.hpp
 	@mkdir -p $(OUT)
 	sed -e 's/^const int maxlevs=5;/const int maxlevs=$(MAXLEVS);/' \
-	    -e 's/^const int nghosts=2; /const int nghosts=$(NGHOSTS); /' $< > $@
+	    -e 's/^const int nghosts=2; /const int nghosts=$(NGHOSTS); /' \
+	    -e 's/^const int CTtype=1;/const int CTtype=$(CTTYPE);/' \
+	    -e 's/^const bool diffusion=false;/const bool diffusion=$(DIFFUSION);/' $< > $@
 	@grep -q 'const int maxlevs=$(MAXLEVS);' $@ || (echo "maxlevs patch failed" && rm -f $@ && false)
 	@grep -q 'const int nghosts=$(NGHOSTS); ' $@ || (echo "nghosts patch failed" && rm -f $@ && false)
+	@grep -q 'const int CTtype=$(CTTYPE);' $@ || (echo "CTtype patch failed" && rm -f $@ && false)
+	@grep -q 'const bool diffusion=$(DIFFUSION);' $@ || (echo "diffusion patch failed" && rm -f $@ && false)
 
 $(OUT)/%.o: $(REF)/%.cpp $(OUT)/defs.hpp
 	$(CXX) -c $(CFLAGS) $(INC) $< -o $@

@@ -22,19 +22,21 @@ def available() -> bool:
     return os.path.isfile(os.path.join(REF, "main.cpp"))
 
 
-def build(maxlevs: int, nghosts: int = 2, flavor: str = "nofma") -> str:
-    out = os.path.join(HERE, "_ref", "L%d_G%d_%s" % (maxlevs, nghosts, flavor), "main.x")
+def build(maxlevs: int, nghosts: int = 2, flavor: str = "nofma", ct_type: int = 1, diffusion: bool = False) -> str:
+    variant = ("_CT%d" % ct_type if ct_type != 1 else "") + ("_DIFF" if diffusion else "")
+    out = os.path.join(HERE, "_ref", "L%d_G%d_%s%s" % (maxlevs, nghosts, flavor, variant), "main.x")
     subprocess.check_call(["make", "-s", "-j8", "-f", os.path.join(HERE, "ref.mk"),
                            "REF=" + REF, "MAXLEVS=%d" % maxlevs, "NGHOSTS=%d" % nghosts,
-                           "FLAVOR=" + flavor], cwd=REPO, stderr=subprocess.DEVNULL)
+                           "FLAVOR=" + flavor, "CTTYPE=%d" % ct_type, "DIFFUSION=" + ("true" if diffusion else "false")],
+                          cwd=REPO, stderr=subprocess.DEVNULL)
     return out
 
 
 def run(ic: str, limiter: str, flux: str, cfl: float, maxlevs: int, steps: int,
         nghosts: int = 2, every: int = 1, flavor: str = "nofma", nx: int = 16, ny: int = 16,
-        workdir: str | None = None, threads: int = 1):
+        workdir: str | None = None, threads: int = 1, ct_type: int = 1, diffusion: bool = False):
     """Run the reference for `steps` steps; return {step: dump dict}."""
-    exe = build(maxlevs, nghosts, flavor)
+    exe = build(maxlevs, nghosts, flavor, ct_type, diffusion)
     wd = workdir or tempfile.mkdtemp(prefix="amrref_")
     with open(os.path.join(wd, "input.txt"), "w") as f:
         f.write("%d %d 8\n1.0 1.0\n%r\n%s %s %s\n" % (nx, ny, cfl, ic, limiter, flux))

@@ -47,6 +47,11 @@ RUNS = {
     "bw_L3_weno3_rusa_40": ("BWx", "WENO3", "RUSA", 0.4, 3, 2, 40),
     "bw_L3_weno5_hlld_40": ("BWx", "WENO5", "HLLD", 0.4, 3, 4, 40),
     "rotor_L3_weno5_rusa_40": ("rotor", "WENO5", "RUSA", 0.4, 3, 4, 40),
+    # compile-time options of the reference (defs.hpp:34-35), built with them
+    "bw_L4_mc_rusa_ct2_100": ("BWx", "MC", "RUSA", 0.4, 4, 2, 100, dict(ct_type=2)),
+    "rotor_L5_mc_hlld_ct2_60": ("rotor", "MC", "HLLD", 0.4, 5, 2, 60, dict(ct_type=2)),
+    "bw_L4_mc_rusa_diff_100": ("BWx", "MC", "RUSA", 0.4, 4, 2, 100, dict(diffusion=True)),
+    "rotor_L5_mc_hlld_ct2diff_60": ("rotor", "MC", "HLLD", 0.4, 5, 2, 60, dict(ct_type=2, diffusion=True)),
 }
 STATES = {  # name: (ic, limiter, flux, cfl, maxlevs, nghosts, step)
     "bw_L2_mc_rusa_step10": ("BWx", "MC", "RUSA", 0.4, 2, 2, 10),
@@ -54,11 +59,12 @@ STATES = {  # name: (ic, limiter, flux, cfl, maxlevs, nghosts, step)
 
 
 def make_run(name):
-    ic, lim, fl, cfl, L, ng, steps = RUNS[name]
-    refs, wd = ref_runner.run(ic, lim, fl, cfl, L, steps, nghosts=ng, every=1)
+    ic, lim, fl, cfl, L, ng, steps = RUNS[name][:7]
+    opts = RUNS[name][7] if len(RUNS[name]) > 7 else {}
+    refs, wd = ref_runner.run(ic, lim, fl, cfl, L, steps, nghosts=ng, every=1, **opts)
     n = max(refs)
     recs = [record(refs[s], ng) for s in range(n + 1)]
-    meta = dict(ic=ic, limiter=lim, flux=fl, cfl=cfl, maxlevs=L, nghosts=ng, steps=n)
+    meta = dict(ic=ic, limiter=lim, flux=fl, cfl=cfl, maxlevs=L, nghosts=ng, steps=n, **opts)
     np.savez_compressed(os.path.join(HERE, "run_%s.npz" % name), meta=np.array(repr(meta)), **pack(recs))
     for f in os.listdir(wd):
         os.remove(os.path.join(wd, f))

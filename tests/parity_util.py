@@ -34,4 +34,5 @@ def to_gpu_cfg(c):
                 nroots=c.get("nroots", (2, 2)), periodic=c.get("periodic", False),
                 geometry=0 if c.get("geom_ref", True) else 1, gamma=c.get("gamma", 0.0),
                 t_end=c.get("tend", 0.0), ic_param=c.get("ic_param"),
-                precision=c.get("precision", "fp64"), lenx=c.get("lenx", 1.0), leny=c.get("leny", 1.0))
+                precision=c.get("precision", "fp64"), lenx=c.get("lenx", 1.0), leny=c.get("leny", 1.0),
+                ct_type=c.get("ct_type", 1), diffusion=c.get("diffusion", False))

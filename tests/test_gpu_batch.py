@@ -11,7 +11,8 @@ def oracle_kw(c, nthreads=8):
     return dict(ic=c.ic.decode(), limiter=c.limiter.decode(), flux=c.flux.decode(), cfl=c.cfl,
                 maxlevs=c.maxlevs, nghosts=c.nghosts, nroots=(c.nroots_x, c.nroots_y),
                 periodic=bool(c.periodic), geom_ref=c.geometry == 0, gamma=c.gamma, tend=c.t_end,
-                ic_param=list(c.ic_param), nthreads=nthreads, dt_fixed=c.dt_fixed)
+                ic_param=list(c.ic_param), nthreads=nthreads, dt_fixed=c.dt_fixed, ct_type=c.ct_type or 1,
+                diffusion=bool(c.diffusion))
 
 
 def blast_batch(gpu, seed, n, cap_levels, precision="fp64", t_end=None):
@@ -44,6 +45,40 @@ def test_blast_batch_matches_oracle(gpu):
             assert a["t"] == b["t"]
             leaves.append(int(b["leafs"].sum()))
     assert len(set(leaves)) > 1  # uneven instances
+
+
+@pytest.mark.gpu
+def test_batch_mixed_ct_and_diffusion_matches_oracle(gpu):
+    """Rotor instances with the basic and the upwind CT EMF, with and without
+    diffusion, in one handle: each reproduces the oracle bit for bit."""
+    opts = [dict(), dict(ct_type=2), dict(diffusion=True), dict(ct_type=2, diffusion=True)]
+    cfgs = [gpu.make_config(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4, **o) for o in opts]
+    sim = gpu.Simulation(cfgs).init()
+    orc = [P.Oracle(**oracle_kw(c)).init() for c in cfgs]
+    sim.run(30)
+    states = []
+    for i, o in enumerate(orc):
+        o.run(30)
+        a, b = sim.state(i), o.state()
+        assert P.compare_states(a, b, 2)[0], i
+        assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["Bi"], b["Bi"]), i
+        states.append(a)
+    # the options change the solution
+    assert not np.array_equal(states[0]["U"], states[1]["U"]) and not np.array_equal(states[0]["U"], states[2]["U"])
+
+
+@pytest.mark.gpu
+def test_ct2_diffusion_fp32_close_to_fp64(gpu):
+    """FP32 bulk path with the upwind CT EMF and diffusion: rotor (4 levels)
+    to t = 0.05 against FP64, relative L1 density on the finest grid."""
+    kw = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4, ct_type=2, diffusion=True, t_end=0.05)
+    a = gpu.Simulation(**kw).init()
+    b = gpu.Simulation(precision="fp32", **kw).init()
+    a.run()
+    b.run()
+    r64, r32 = a.uniform(0), b.uniform(0)
+    l1 = np.abs(r32 - r64).sum() / np.abs(r64).sum()
+    assert l1 < 1e-3, l1
 
 
 @pytest.mark.gpu

@@ -24,7 +24,8 @@ def test_gpu_run_fingerprints(gpu, name):
     d = np.load(os.path.join(GOLDEN, "run_%s.npz" % name))
     m = ast.literal_eval(str(d["meta"]))
     sim = gpu.Simulation(**to_gpu_cfg(dict(ic=m["ic"], limiter=m["limiter"], flux=m["flux"], cfl=m["cfl"],
-                                           maxlevs=m["maxlevs"], nghosts=m["nghosts"]))).init()
+                                           maxlevs=m["maxlevs"], nghosts=m["nghosts"],
+                                           ct_type=m.get("ct_type", 1), diffusion=m.get("diffusion", False)))).init()
     for s in range(m["steps"] + 1):
         if s:
             sim.step()

@@ -32,11 +32,25 @@ CASES = [
          geom_ref=False, lenx=2 * 3.141592653589793, leny=2 * 3.141592653589793, steps=30),
     dict(ic="OT", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4, nroots=(4, 4), periodic=True,
          geom_ref=False, lenx=2 * 3.141592653589793, leny=2 * 3.141592653589793, steps=30),
+    # compile-time options of the reference: the upwind CT EMF (CT2D.cpp:28-75)
+    # and diffusivity.cpp on the finest two levels
+    dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, ct_type=2, diffusion=True, steps=40),
+    dict(ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=4, ct_type=2, steps=60),
+    dict(ic="BWx", limiter="WENO5", flux="HLLD", cfl=0.4, maxlevs=3, nghosts=4, ct_type=2, diffusion=True,
+         steps=30),
+    dict(ic="OT", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4, nroots=(4, 4), periodic=True,
+         geom_ref=False, lenx=2 * 3.141592653589793, leny=2 * 3.141592653589793, ct_type=2, diffusion=True,
+         steps=30),
 ]
 
 
+def case_id(c):
+    extra = ("-CT%d" % c["ct_type"] if c.get("ct_type", 1) != 1 else "") + ("-diff" if c.get("diffusion") else "")
+    return "%s-%s-%s-L%d%s" % (c["ic"], c["limiter"], c["flux"], c["maxlevs"], extra)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", CASES, ids=lambda c: "%s-%s-%s-L%d" % (c["ic"], c["limiter"], c["flux"], c["maxlevs"]))
+@pytest.mark.parametrize("case", CASES, ids=case_id)
 def test_fp64_matches_oracle(gpu, case):
     case = dict(case)
     steps = case.pop("steps")

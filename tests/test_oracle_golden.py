@@ -54,7 +54,8 @@ def test_run_fingerprints(name):
     d = np.load(os.path.join(GOLDEN, "run_%s.npz" % name))
     meta = ast.literal_eval(str(d["meta"]))
     o = P.Oracle(ic=meta["ic"], limiter=meta["limiter"], flux=meta["flux"], cfl=meta["cfl"],
-                 maxlevs=meta["maxlevs"], nghosts=meta["nghosts"]).init()
+                 maxlevs=meta["maxlevs"], nghosts=meta["nghosts"], ct_type=meta.get("ct_type", 1),
+                 diffusion=meta.get("diffusion", False)).init()
     n = min(meta["steps"], CPU_STEPS)
     for s in range(n + 1):
         if s:
