@@ -292,7 +292,7 @@ int Engine::adjoint_step() {
     inst_[q].dtn = c.meta[q].dtn;
   }
   if (int rc = upload_params()) return rc;
-  CK(a_take_.ensure(sizeof(double) * 8 * kMaxSeg * static_cast<size_t>(nops_ > 0 ? nops_ : 1)), "alloc");
+  CK(a_take_.ensure(sizeof(double) * 16 * kMaxSeg * static_cast<size_t>(nops_ > 0 ? nops_ : 1)), "alloc");
   CK(cudaMemcpyAsync(U_, d.p, u, cudaMemcpyDeviceToDevice, stream_), "restore");
   CK(cudaMemcpyAsync(Bi_, static_cast<char *>(d.p) + u, b, cudaMemcpyDeviceToDevice, stream_), "restore");
   if (!graph_on_ || prof_on_) {

@@ -23,7 +23,7 @@ struct GhostAdjLaunch {
   int nops;
   GhostSeg seg[kMaxSeg];   // adjoint arrays (double), nv and kind of the forward field
   int nseg;
-  double *take;            // [nseg][nops][8]
+  double *take;            // [nseg][nops][16]: per variable, the op's cell (and its pair)
 };
 
 template <int N>
@@ -35,10 +35,14 @@ __global__ void k_ghost_adj_take(GhostAdjLaunch g) {
   if (op.type == GOP_NOP) return;
   const GhostSeg &s = g.seg[q];
   double *a = static_cast<double *>(s.field) + static_cast<size_t>(op.dst_slot) * s.nv * (N * N) + op.dst_pos;
-  double *out = g.take + (static_cast<size_t>(q) * g.nops + r) * 8;
+  double *out = g.take + (static_cast<size_t>(q) * g.nops + r) * 16;
   for (int k = 0; k < s.nv; k++) {
     out[k] = a[k * N * N];
     a[k * N * N] = 0.0;
+    if (op.type == GOP_COPY2) {  // the pair's second cell
+      out[8 + k] = a[k * N * N + 1];
+      a[k * N * N + 1] = 0.0;
+    }
   }
 }
 
@@ -60,9 +64,15 @@ __global__ void k_ghost_adj_give(GhostAdjLaunch g) {
   if (op.type == GOP_NOP) return;
   const GhostSeg &s = g.seg[q];
   double *fld = static_cast<double *>(s.field);
-  const double *in = g.take + (static_cast<size_t>(q) * g.nops + r) * 8;
+  const double *in = g.take + (static_cast<size_t>(q) * g.nops + r) * 16;
   for (int k = 0; k < s.nv; k++) {
     const double v = in[k];
+    if (op.type == GOP_COPY2) {
+      double *src = fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos;
+      if (v != 0.0) atomicAdd(src, v);
+      if (in[8 + k] != 0.0) atomicAdd(src + 1, in[8 + k]);
+      continue;
+    }
     if (v == 0.0) continue;
     if (op.type == GOP_COPY) {
       atomicAdd(fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos, v);

@@ -72,7 +72,10 @@ struct InstParams {
 //             edge  s(i,j)                                       boundaryec.cpp:46
 //   SFINE:  the same from four saved pre-fill values (snapshot rows src_slot..
 //           src_slot+3 in the order (i,j) (i,j+1) (i+1,j) (i+1,j+1))
-enum GhostOpType : uint8_t { GOP_COPY = 0, GOP_SNAP = 1, GOP_FINE = 2, GOP_SFINE = 3, GOP_NOP = 4 };
+// GOP_COPY2: two horizontally adjacent cells (dst_pos, dst_pos + 1) from
+// (src_pos, src_pos + 1) of one source block; both positions even, so the
+// pair is one aligned 8-byte (float) or 16-byte (double) access.
+enum GhostOpType : uint8_t { GOP_COPY = 0, GOP_SNAP = 1, GOP_FINE = 2, GOP_SFINE = 3, GOP_NOP = 4, GOP_COPY2 = 5 };
 struct GhostOp {
   int dst_slot;
   int src_slot;     // physical slot, or first snapshot row for SNAP / SFINE

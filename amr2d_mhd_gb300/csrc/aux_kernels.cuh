@@ -2,6 +2,8 @@
 // and the prolongation / restriction kernels.
 #pragma once
 
+#include <type_traits>
+
 #include "amr_common.h"
 #include "physics.cuh"
 #include "stage.cuh"
@@ -81,6 +83,12 @@ __device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp
   constexpr int NN = N * N;
   F *fld = static_cast<F *>(s.field);
   F *dst = fld + (static_cast<size_t>(op.dst_slot) * s.nv + k) * NN + op.dst_pos;
+  if (op.type == GOP_COPY2) {  // even positions in an even-sized plane: aligned pair
+    using P2 = typename std::conditional<sizeof(F) == 4, float2, double2>::type;
+    *reinterpret_cast<P2 *>(dst) =
+        *reinterpret_cast<const P2 *>(fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos);
+    return;
+  }
   if (op.type == GOP_COPY || op.type == GOP_FINE) {
     const F *c = fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos;
     *dst = op.type == GOP_COPY ? c[0] : fine_value<F>(s.kind, k, c[0], c[N], c[1], c[1 + N]);

@@ -320,10 +320,12 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     cur_.resize(need);
     snap_stamp_.resize(need, 0);
     snap_row_.resize(need);
+    emit_stamp_.resize(need, 0);
   }
   if (++gen_ == 0) {  // stamp wrap-around
     std::fill(stamp_.begin(), stamp_.end(), 0u);
     std::fill(snap_stamp_.begin(), snap_stamp_.end(), 0u);
+    std::fill(emit_stamp_.begin(), emit_stamp_.end(), 0u);
     gen_ = 1;
   }
   touched_.clear();
@@ -338,11 +340,25 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     }
     return snap_row_[idx];
   };
+  // a plain copy into an even position whose right neighbour is a plain copy
+  // of the next source cell of the same block (not yet emitted) becomes one
+  // paired op (same-level column and row copies, ~two thirds of a program)
+  auto pairs_with = [&](int blk, int pos, const Desc &d) {
+    if ((pos & 1) || (d.pos & 1)) return false;
+    const size_t nxt = static_cast<size_t>(blk) * nn_ + pos + 1;
+    if (stamp_[nxt] != gen_ || emit_stamp_[nxt] == gen_) return false;
+    const Desc &e = cur_[nxt];
+    if (e.type != GOP_COPY || e.blk != d.blk || e.pos != d.pos + 1) return false;
+    if (e.blk == blk && e.pos == pos + 1) return false;  // unchanged cell
+    return !overwritten(e.blk, e.pos);
+  };
   out.ops.reserve(out.ops.size() + touched_.size());
   for (const int idx : touched_) {
     const Desc &d = cur_[idx];
     const int blk = idx / nn_, pos = idx % nn_;
     if (d.type == GOP_COPY && d.blk == blk && d.pos == pos) continue;  // unchanged
+    if (emit_stamp_[idx] == gen_) continue;                             // second cell of a pair
+    emit_stamp_[idx] = gen_;
     GhostOp op{};
     op.dst_slot = slot[blk];
     op.dst_pos = static_cast<int16_t>(pos);
@@ -354,6 +370,10 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
         op.type = GOP_COPY;
         op.src_slot = slot[d.blk];
         op.src_pos = d.pos;
+        if (pairs_with(blk, pos, d)) {
+          op.type = GOP_COPY2;
+          emit_stamp_[idx + 1] = gen_;
+        }
       }
     } else {
       const int c[4] = {d.pos, d.pos + n_, d.pos + 1, d.pos + 1 + n_};  // sum_irjr order

@@ -56,6 +56,7 @@ class GhostCompiler {
   std::vector<int> touched_;
   std::vector<uint32_t> snap_stamp_;
   std::vector<int> snap_row_;
+  std::vector<uint32_t> emit_stamp_;  // cell already written by an emitted op
 };
 
 }  // namespace amr

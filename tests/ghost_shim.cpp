@@ -48,16 +48,22 @@ extern "C" int ghost_shim_apply(int last_active, const int *lp, const int *icoor
       const double *src = field + (static_cast<size_t>(op.src_slot) * nv + k) * nn + op.src_pos;
       const double *r = snap.data() + static_cast<size_t>(op.src_slot) * 8 + k;
       double v;
-      if (op.type == GOP_COPY) v = src[0];
+      if (op.type == GOP_COPY || op.type == GOP_COPY2) v = src[0];
       else if (op.type == GOP_SNAP) v = r[0];
       else if (op.type == GOP_FINE) v = fine(k, src[0], src[n], src[1], src[1 + n]);
       else v = fine(k, r[0], r[8], r[16], r[24]);
       out.push_back(v);
+      if (op.type == GOP_COPY2) {
+        if ((op.dst_pos & 1) || (op.src_pos & 1)) return -2;  // a pair must be aligned
+        out.push_back(src[1]);
+      }
     }
   size_t q = 0;
   for (const GhostOp &op : p.ops)
-    for (int k = 0; k < nv; k++)
+    for (int k = 0; k < nv; k++) {
       field[(static_cast<size_t>(op.dst_slot) * nv + k) * nn + op.dst_pos] = out[q++];
+      if (op.type == GOP_COPY2) field[(static_cast<size_t>(op.dst_slot) * nv + k) * nn + op.dst_pos + 1] = out[q++];
+    }
   *n_ops = static_cast<int>(p.ops.size());
   *n_snaps = static_cast<int>(p.snaps.size());
   return 0;
