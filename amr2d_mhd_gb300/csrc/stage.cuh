@@ -92,7 +92,7 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
 }
 
 // 4 resident CTAs per SM (64 registers, ~170 B of spills to L1): on the
-// 64-rotor FP32 batch 0.91 ms per stage launch against 1.00 ms at 3 CTAs
+// 64-rotor FP32 batch 2.11 ms per stage launch against 2.31 ms at 3 CTAs
 #ifndef AMR_STAGE_F32_MINB
 #define AMR_STAGE_F32_MINB 4
 #endif
