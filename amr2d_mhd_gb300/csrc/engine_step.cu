@@ -6,6 +6,7 @@
 
 #include "aux_kernels.cuh"
 #include "engine.hpp"
+#include "host_par.hpp"
 
 namespace amr {
 
@@ -54,24 +55,38 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
 
 // admesh.cpp:17-102 for the instances in `which`; the criterion comes from the
 // device reduction of the last dt_crit (or, at initialisation, from the IC's
-// primitive state on the host)
+// primitive state on the host).  The refine / coarsen kernels run while the
+// host compiles the changed instances' ghost programs; the device error check
+// (U2W("refine") traps) follows, so errors surface before the call returns.
 int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad) {
   const auto t0 = std::chrono::steady_clock::now();
   std::vector<TreeOp> ref, crs;
-  for (int q : which) {
-    Instance &in = inst_[q];
-    if (in.cfg.maxlevs <= 1) continue;
+  // the quadtrees of a batch are independent: admesh them on host threads,
+  // then give the new blocks slots in instance order (the pool may grow)
+  std::vector<AdmeshPlan> plans(which.size());
+  std::vector<std::string> errs(which.size());
+  std::vector<char> ok(which.size(), 1);
+  size_t blocks = 0;
+  for (int q : which) blocks += static_cast<size_t>(inst_[q].tree.lastActive);
+  parallel_items(which.size(), host_threads(blocks), [&](size_t, size_t w) {
+    Instance &in = inst_[which[w]];
+    if (in.cfg.maxlevs <= 1) return;
     std::vector<double> grad(in.tree.lastActive, 0.0);
     if (host_grad) {
-      grad = (*host_grad)[q];
+      grad = (*host_grad)[which[w]];
     } else {
       const double *hg = h_grad_.as<double>();
       for (int t = in.task_begin; t < in.task_end; t++) grad[task_blk_[t]] = hg[t];
     }
-    AdmeshPlan plan;
-    std::string err;
-    if (!in.tree.admesh(grad, plan, err)) return fail(AMR_E_MAXBLOCKS, err);
+    ok[w] = in.tree.admesh(grad, plans[w], errs[w]) ? 1 : 0;
+  });
+  for (size_t w = 0; w < which.size(); w++) {
+    const int q = which[w];
+    Instance &in = inst_[q];
+    if (in.cfg.maxlevs <= 1) continue;
+    if (!ok[w]) return fail(AMR_E_MAXBLOCKS, errs[w]);
     if (int rc = assign_slots(in)) return rc;
+    const AdmeshPlan &plan = plans[w];
     for (const auto &r : plan.refine)
       ref.push_back(TreeOp{in.slot[r[0]], {in.slot[r[1]], in.slot[r[2]], in.slot[r[3]], in.slot[r[4]]}, q});
     for (const auto &c : plan.coarsen)
@@ -96,6 +111,11 @@ int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vec
   CK(launch_coarsen(m_, a, static_cast<int>(crs.size()), stream_), "coarsen");
   prof_.launches += (ref.empty() ? 0 : 1) + (crs.empty() ? 0 : 1);
   prof_.h2d_bytes += static_cast<int64_t>(sizeof(TreeOp) * all.size());
+  if (initialised_) {
+    const auto t1 = std::chrono::steady_clock::now();
+    if (int rc = compile_programs()) return rc;
+    prof_.host_compile_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+  }
   return check_device_error();  // also keeps `all` alive until the copy is done
 }
 

@@ -309,6 +309,8 @@ def run_batch(stream, steps, advance):
         out[prec] = dict(value=(c1 - c0) / (ms * 1e-3), ms_per_step=ms / steps,
                          leaves=sum(sim.info(q)["n_leaves"] for q in range(BATCH_N)),
                          host_ms_per_step=(p["host_compile_ms"] + p["host_admesh_ms"]) / steps,
+                         host_compile_ms_per_step=p["host_compile_ms"] / steps,
+                         host_admesh_ms_per_step=p["host_admesh_ms"] / steps,
                          step_gpu_ms_per_step=p["step_gpu_ms"] / steps,
                          stage_kernel_ms_per_step=p["stage_ms"] / steps,
                          gpu_launches=int(p["launches"]),
