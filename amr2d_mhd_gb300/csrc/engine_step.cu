@@ -22,17 +22,20 @@ namespace amr {
 // driver's pageable path (direct DMA on a coherent CPU-GPU link) beats a host
 // memcpy into pinned memory followed by a pinned copy; a scatter / gather
 // kernel then moves the blocks between the staging buffer and their slots.
+// A pageable host-to-device copy has read its source when it returns, so an
+// upload returns without waiting for the device (later work on the stream is
+// ordered after the scatter); a download waits for its copy.
 int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
   const int nblk = in.tree.lastActive;
   const int per = field_nv(field) * nn_;
   const size_t bytes = static_cast<size_t>(nblk) * per * sizeof(double);
   if (nblk == 0) return AMR_OK;
+  // a growing staging buffer is freed and reallocated: let an earlier
+  // upload's scatter finish reading it first
+  if (sizeof(int) * nblk > d_slots_.bytes || bytes > d_stage_.bytes) CK(cudaStreamSynchronize(stream_), "sync");
   CK(d_slots_.ensure(sizeof(int) * nblk), "alloc");
-  CK(h_stage_.ensure(sizeof(int) * nblk), "alloc");
   CK(d_stage_.ensure(bytes), "alloc");
-  int *hs = h_stage_.as<int>();
-  std::memcpy(hs, in.slot.data(), sizeof(int) * nblk);
-  CK(cudaMemcpyAsync(d_slots_.p, hs, sizeof(int) * nblk, cudaMemcpyHostToDevice, stream_), "h2d");
+  CK(cudaMemcpyAsync(d_slots_.p, in.slot.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice, stream_), "h2d");
   void *fp = field_ptr(field);
   if (to_device) {
     CK(cudaMemcpyAsync(d_stage_.p, host, bytes, cudaMemcpyHostToDevice, stream_), "h2d");
@@ -40,7 +43,7 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
        "scatter");
     prof_.h2d_bytes += static_cast<int64_t>(bytes + sizeof(int) * nblk);
     prof_.launches += 1;
-    CK(cudaStreamSynchronize(stream_), "sync");
+    CK(cudaGetLastError(), "scatter");
   } else {
     CK(launch_gather(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
        "gather");
