@@ -88,7 +88,7 @@ Engine::~Engine() {
     b->release();
   for (DevBuf &b : a_C_) b.release();
   for (DevBuf &b : ckpt_) b.release();
-  for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_stage_, &h_ops_, &h_snaps_, &h_tasks_})
+  for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_ops_, &h_snaps_, &h_tasks_})
     b->release();
   if (own_stream_ && stream_) cudaStreamDestroy(stream_);
   if (exec_) cudaGraphExecDestroy(exec_);

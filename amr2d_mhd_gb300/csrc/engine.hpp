@@ -161,7 +161,7 @@ class Engine {
   int layout_programs(bool relayout);
   DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_, d_snaps_;
   DevBuf d_treeops_, d_stage_, d_slots_;
-  HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_stage_, h_ops_, h_snaps_, h_tasks_;
+  HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_ops_, h_snaps_, h_tasks_;
   std::vector<GhostCompiler *> gcs_;  // one per compile thread
 
   // CUDA graph of one step, re-captured when gen_ moves (tree, pool, profiling)
