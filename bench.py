@@ -51,6 +51,19 @@ def dist_env():
     return world, rank, local
 
 
+def reduce_over_ranks(ms, cells, device):
+    """Replicas (one process per GPU, no exchange in the data path): the job's
+    time is the slowest rank's, its work the sum over ranks.  Called on every
+    rank of an initialised process group (NCCL on GPUs, gloo in the CPU tests)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms, float(cells)], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(t[1])
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -191,11 +204,7 @@ def run_ours(args):
         clk = clocks.stop() if clocks else None
         cells = i1["cell_updates"] - i0["cell_updates"]
         if world > 1:
-            t = torch.tensor([ms, float(cells)], dtype=torch.float64, device="cuda")
-            mx = t.clone()
-            torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-            ms, cells = float(mx[0]), float(t[1])
+            ms, cells = reduce_over_ranks(ms, cells, "cuda")
         results[prec] = dict(ms=ms, cells=cells, prof=prof, clocks=clk, leaves=i1["n_leaves"],
                              steps=i1["steps"] - i0["steps"],
                              schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"))
