@@ -652,7 +652,9 @@ def main():
                 "h2d_bytes_per_step": int(e2e["h2d"]), "d2h_bytes_per_step": int(e2e["d2h"])},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "kernel": "k_faces<2,MUSCL,HLLD,double>",
-                     "bytes_per_launch": alg_bytes, "launch_ms": stage_ms_avg},
+                     "bytes_per_launch": alg_bytes, "launch_ms": stage_ms_avg,
+                     "note": "the FP64 path is bound by the FP64 pipe (2 FMA/clk/SM on GB300; k_faces keeps it "
+                             "79% busy while active, ncu), not by HBM: see fp64_pipe"},
         "fp64_pipe": fp64,
         "schedule": r64["schedule"],
         "host_compile_ms_per_step": prof["host_compile_ms"] / args.steps,
