@@ -27,7 +27,7 @@ STATUS = {0: "AMR_OK", -1: "AMR_E_CONFIG", -2: "AMR_E_CUDA", -3: "AMR_E_OOM", -4
 # every entry point declared in include/amr2d_mhd.h
 EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "amr_config_kh", "amr_abi_version", "amr_status_string",
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
-           "amr_init", "amr_step", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
+           "amr_init", "amr_step", "amr_step_begin", "amr_step_end", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
            "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_autotune", "amr_save4py",
            "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
@@ -230,6 +230,14 @@ class Simulation:
 
     def step(self):
         self._ck(load().amr_step(self.h))
+
+    def step_begin(self):
+        """Launch one step's device work and return (amr_step_begin)."""
+        self._ck(load().amr_step_begin(self.h))
+
+    def step_end(self):
+        """Finish the step in flight: wait, advance t / dt, remesh (amr_step_end)."""
+        self._ck(load().amr_step_end(self.h))
 
     def run(self, max_steps=-1):
         self._ck(load().amr_run(self.h, max_steps))

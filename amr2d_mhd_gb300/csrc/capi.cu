@@ -13,10 +13,14 @@ struct amr_handle {
 };
 
 namespace {
+// Every entry point but amr_step_end first finishes a step that
+// amr_step_begin left in flight, so each sees the state after that step.
 template <typename F>
-int guarded(amr_handle *h, F &&f) {
+int guarded(amr_handle *h, F &&f, bool finish_pending = true) {
   if (!h) return AMR_E_ARG;
   try {
+    if (finish_pending && h->engine.step_pending())
+      if (int rc = h->engine.step_end()) return rc;
     return f(h->engine);
   } catch (const std::bad_alloc &) {
     h->engine.last_error = "host out of memory";
@@ -167,6 +171,8 @@ int amr_last_error(const amr_handle *h, char *buf, size_t len) {
 
 int amr_init(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.init(); }); }
 int amr_step(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.step(); }); }
+int amr_step_begin(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.step_begin(); }); }
+int amr_step_end(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.step_end(); }, false); }
 int amr_run(amr_handle *h, int64_t n) { return guarded(h, [&](amr::Engine &e) { return e.run(n); }); }
 int amr_get_info(amr_handle *h, int32_t q, amr_info *o) {
   return guarded(h, [&](amr::Engine &e) { return e.info(q, o); });

@@ -68,6 +68,9 @@ class Engine {
   int create(const amr_config *cfgs, int n);
   int init();
   int step();
+  int step_begin();                // rebuild + launch_step, no wait (amr_step_begin)
+  int step_end();                  // finish_step of the step in flight (amr_step_end)
+  bool step_pending() const { return step_pending_; }
   int run(int64_t max_steps);
   int info(int inst, amr_info *out);
   int set_stream(cudaStream_t s);
@@ -179,6 +182,7 @@ class Engine {
   std::vector<cudaEvent_t> ev_;     // start/stop pairs of this step's stage launches
   int ev_used_ = 0;
   bool diffuse_any_ = false;  // some leaf task carries TASK_DIFFUSE
+  bool step_pending_ = false; // step_begin launched a step that step_end has not finished
   cudaEvent_t step_ev_[2] = {nullptr, nullptr};  // brackets the step's device work (profiling)
   bool step_ev_pending_ = false;
   int64_t stage_cells_pending_ = 0;

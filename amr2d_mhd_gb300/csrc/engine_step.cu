@@ -186,8 +186,16 @@ int Engine::finish_step() {
 
 // one iteration of main.cpp:241-360 for every instance with t <= t_end
 int Engine::step() {
+  if (int rc = step_begin()) return rc;
+  return step_end();
+}
+
+// the device half of a step: leaf list and ghost programs of the current
+// trees, then the step's launches; returns without waiting for the device
+int Engine::step_begin() {
   if (!initialised_) return fail(AMR_E_STATE, "amr_init has not been called");
   if (poisoned_) return fail(AMR_E_STATE, "engine stopped by an earlier error: " + last_error);
+  if (step_pending_) return fail(AMR_E_STATE, "a step is already in flight");
   active_.clear();
   for (size_t q = 0; q < inst_.size(); q++) {
     Instance &in = inst_[q];
@@ -199,6 +207,15 @@ int Engine::step() {
   if (adj_on_)
     if (int rc = adjoint_record()) return rc;
   if (int rc = launch_step()) return rc;
+  step_pending_ = true;
+  return AMR_OK;
+}
+
+// the host half: wait for the step, advance t / dt, remesh (and compile the
+// changed trees' ghost programs while the refine / coarsen kernels run)
+int Engine::step_end() {
+  if (!step_pending_) return AMR_OK;
+  step_pending_ = false;
   return finish_step();
 }
 

@@ -237,6 +237,7 @@ def run_ours(args):
     if not args.no_batch:
         results["rotor_batch"] = run_rotor_batch(stream, args.batch_steps)
         results["batch"] = run_batch(stream, args.batch_steps, args.batch_advance)
+        results["batch"]["fp32_two_handles_pipelined"] = run_batch_pipelined(args.batch_steps, args.batch_advance)
     if not args.no_adjoint:
         results["adjoint"] = run_adjoint(stream)
     if not args.no_ot:
@@ -287,6 +288,50 @@ def run_rotor_batch(stream, steps):
 
 BATCH_SEED = 2026
 BATCH_N = 512
+
+
+def run_batch_pipelined(steps, advance, prec="fp32"):
+    """The blast batch as two handles of 256 instances, each on its own
+    stream, stepped with amr_step_begin / amr_step_end interleaved so that
+    one handle's host half of a step (remesh, ghost-program compile) runs
+    while the other's step is on the GPU.  Timed on the host between device
+    synchronisations (two streams)."""
+    import torch
+
+    import amr2d_mhd_gb300 as amr
+    cfgs = [amr.blast_config(BATCH_SEED, i, prec) for i in range(BATCH_N)]
+    sims = [amr.Simulation(cfgs[:BATCH_N // 2]).init(), amr.Simulation(cfgs[BATCH_N // 2:]).init()]
+    a, b = sims
+
+    def pipelined(n):
+        a.step_begin()
+        for k in range(n):
+            b.step_begin()
+            a.step_end()
+            if k + 1 < n:
+                a.step_begin()
+            b.step_end()
+
+    pipelined(advance)
+    for s in sims:
+        s.autotune(2)
+    pipelined(3)
+
+    def cells():
+        return sum(s.info(q)["cell_updates"] for s in sims for q in range(BATCH_N // 2))
+
+    c0 = cells()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pipelined(steps)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    c1 = cells()
+    for s in sims:
+        s.close()
+    return dict(value=(c1 - c0) / sec, ms_per_step=sec * 1e3 / steps,
+                workload="the same 512 instances as two handles of 256, host and device halves of their "
+                         "steps interleaved (amr_step_begin / amr_step_end), %d timed steps" % steps)
 
 
 def run_batch(stream, steps, advance):
@@ -680,6 +725,7 @@ def main():
                         "maxlevs U{3..6}, MUSCL-MC + HLLE + CT, CFL 0.2, outflow; %d untimed batch steps, then "
                         "%d timed" % (BATCH_N, BATCH_SEED, args.batch_advance, args.batch_steps),
             "fp64": res["batch"]["fp64"], "fp32": res["batch"]["fp32"],
+            "fp32_two_handles_pipelined": res["batch"]["fp32_two_handles_pipelined"],
             "fp32_vs_plain_fp64_rotor": res["batch"]["fp32"]["value"] / value,
             "l1_rel_density_fp32_vs_fp64_max": res["batch"]["l1_rel_density_fp32_vs_fp64_max"],
             "l1_sample": "4 instances of the batch (maxlevs capped at 4) run to t = 0.1, finest uniform grid"},

@@ -144,6 +144,14 @@ int amr_init(amr_handle *h);
  * with CT2D, the CFL dt reduction and admesh.  Instances that are done are
  * skipped. */
 int amr_step(amr_handle *h);
+/* amr_step in two halves (extension; the reference's loop has no such split):
+ * amr_step_begin launches the step's device work on the handle's stream and
+ * returns; amr_step_end waits for it and does the host half (t and dt, the
+ * remesh, the ghost programs of the new trees).  Between the two the caller's
+ * thread is free, e.g. for the host half of another handle's step on another
+ * stream.  Any other call on the handle ends a step in flight first. */
+int amr_step_begin(amr_handle *h);
+int amr_step_end(amr_handle *h);
 /* step until every instance is done, or `max_steps` steps (< 0: no limit) */
 int amr_run(amr_handle *h, int64_t max_steps);
 int amr_get_info(amr_handle *h, int32_t instance, amr_info *info);
