@@ -456,7 +456,8 @@ def run_adjoint(stream, steps=200):
     """Gradient of the KH loss (total density in [0.4,0.6]^2 after `steps`
     steps of dt 2e-4 on the frozen 256^2 periodic mesh) w.r.t. the 16
     perturbation amplitudes: adjoint cost against a forward step, and the
-    gradient against central differences (h = 1e-7)."""
+    gradient against central differences (h = 1e-7); the same for the
+    kinetic energy of the transverse motion (h = 1e-6 and 1e-7)."""
     import torch
 
     import amr2d_mhd_gb300 as amr
@@ -507,31 +508,61 @@ def run_adjoint(stream, steps=200):
     torch.cuda.synchronize()
     adj_ms = e0.elapsed_time(e1)
     gU = sim.adjoint_read("U")
-    # chain rule through the IC: U2 = rho v, U4 = ... + rho v^2 / 2
-    k = np.arange(1, 17)
-    g = np.zeros(16)
-    for b, (x0, y0) in enumerate(ic):
-        x = (((x0 + np.arange(20) - ng) % 256) + 0.5) / 256
-        y = (((y0 + np.arange(20) - ng) % 256) + 0.5) / 256
-        Y, X = np.meshgrid(y, x, indexing="ij")
-        inside = np.abs(Y - 0.5) <= 0.25
-        rho = np.where(inside, 2.0, 1.0)
-        env = np.exp(-(Y - 0.25) ** 2 / 0.01) + np.exp(-(Y - 0.75) ** 2 / 0.01)
-        basis = np.sin(2.0 * np.pi * k[:, None, None] * X[None]) * env    # dv/da_k
-        v = np.tensordot(a0, basis, axes=1)
-        w = gU[b, 2] * rho + gU[b, 4] * rho * v
-        g += (basis * w[None]).sum(axis=(1, 2))
-    h = 1e-7
-    fd = np.zeros(16)
-    for q in range(16):
-        e = np.zeros(16)
-        e[q] = h
-        fd[q] = (forward(a0 + e)[0] - forward(a0 - e)[0]) / (2 * h)
+
+    def grad_a(gU):
+        # chain rule through the IC: U2 = rho v, U4 = ... + rho v^2 / 2
+        k = np.arange(1, 17)
+        out = np.zeros(16)
+        for b, (x0, y0) in enumerate(ic):
+            x = (((x0 + np.arange(20) - ng) % 256) + 0.5) / 256
+            y = (((y0 + np.arange(20) - ng) % 256) + 0.5) / 256
+            Y, X = np.meshgrid(y, x, indexing="ij")
+            rho = np.where(np.abs(Y - 0.5) <= 0.25, 2.0, 1.0)
+            env = np.exp(-(Y - 0.25) ** 2 / 0.01) + np.exp(-(Y - 0.75) ** 2 / 0.01)
+            basis = np.sin(2.0 * np.pi * k[:, None, None] * X[None]) * env    # dv/da_k
+            v = np.tensordot(a0, basis, axes=1)
+            out += (basis * (gU[b, 2] * rho + gU[b, 4] * rho * v)[None]).sum(axis=(1, 2))
+        return out
+
+    def fd_of(loss_of, h):
+        fd = np.zeros(16)
+        for q in range(16):
+            e = np.zeros(16)
+            e[q] = h
+            fd[q] = (loss_of(a0 + e) - loss_of(a0 - e)) / (2 * h)
+        return fd
+
+    g = grad_a(gU)
+    fd = fd_of(lambda a: forward(a)[0], 1e-7)
+    # second loss: kinetic energy of the transverse motion, sum of m_y^2 / rho
+    # dA over the interior; it scales with the perturbation, so central
+    # differences resolve its gradient far below the kink error of the first
+    inner = np.zeros((len(ic), 20, 20))
+    inner[:, ng:-ng, ng:-ng] = 1.0 / 256.0 ** 2
+
+    def ke_loss(a, record=False):
+        forward(a, record)
+        U = sim.download("U")
+        return float((U[:, 2] ** 2 / U[:, 0] * inner).sum()), U
+
+    _, U = ke_loss(a0, record=True)
+    lam = np.zeros((len(ic), 8, 20, 20))
+    lam[:, 2] = 2 * U[:, 2] / U[:, 0] * inner
+    lam[:, 0] = -(U[:, 2] / U[:, 0]) ** 2 * inner
+    sim.adjoint_seed("U", lam)
+    for _ in range(steps):
+        sim.adjoint_step()
+    g_ke = grad_a(sim.adjoint_read("U"))
+    fd_ke = {h: fd_of(lambda a: ke_loss(a)[0], h) for h in (1e-6, 1e-7)}
     sim.close()
     return dict(forward_ms_per_step=fwd_ms / steps, recording_ms_per_step=rec_ms / steps,
                 adjoint_ms_per_step=adj_ms / steps, cost_ratio=adj_ms / fwd_ms, loss=L,
                 grad_max_abs=float(np.abs(g).max()),
-                fd_max_rel_diff=float(np.abs(g - fd).max() / np.abs(fd).max()))
+                fd_max_rel_diff=float(np.abs(g - fd).max() / np.abs(fd).max()),
+                ke_loss={"loss": "sum of m_y^2 / rho dA over the domain after the same 200 steps",
+                         "grad_max_abs": float(np.abs(g_ke).max()),
+                         "fd_max_rel_diff_h1e-6": float(np.abs(g_ke - fd_ke[1e-6]).max() / np.abs(fd_ke[1e-6]).max()),
+                         "fd_max_rel_diff_h1e-7": float(np.abs(g_ke - fd_ke[1e-7]).max() / np.abs(fd_ke[1e-7]).max())})
 
 
 def cpu_baseline(steps, threads):
@@ -733,7 +764,8 @@ def main():
             workload="Kelvin-Helmholtz, frozen 256^2 periodic mesh (256 blocks), gamma 5/3, MUSCL-MC + RUSA + CT, "
                      "RK2, 200 steps of dt 2e-4, loss = total density in [0.4,0.6]^2, gradient w.r.t. the 16 "
                      "amplitudes (seed %d); cost ratio = adjoint incl. recompute / plain forward, per step; "
-                     "fd = central differences h = 1e-7 (first-order error from MC kinks)" % KH_SEED,
+                     "fd = central differences h = 1e-7 (first-order error from MC kinks); ke_loss: the same for "
+                     "the transverse kinetic energy, a loss that scales with the perturbation" % KH_SEED,
             **res["adjoint"]),
         "orszag_tang": None if "orszag_tang" not in res else {
             "workload": "Orszag-Tang on [0,2pi]^2, periodic, 4x4 roots, gamma 5/3, HLLD + CT, RK2, to t=pi on a fixed "

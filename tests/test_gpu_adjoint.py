@@ -11,6 +11,7 @@ import torch
 import kh_reference as K
 
 DT, GAMMA, N = 2e-4, 5.0 / 3.0, 256
+N_BLK = 20   # block edge with 2 ghost layers
 
 
 def kh_sim(gpu, seed=5):
@@ -162,3 +163,51 @@ def test_kh_gradient_fd_and_reference(gpu):
             errs.append(np.abs(g_adj - g_fd).max() / np.abs(g_fd).max())
     assert errs[0] > errs[1] > errs[2], errs
     assert errs[1] < 1e-2 and errs[2] < 2e-3, errs
+
+
+@pytest.mark.gpu
+def test_kh_kinetic_energy_gradient_matches_fd(gpu):
+    """A loss that scales with the perturbation, the transverse kinetic energy
+    sum(m_y^2 / rho) dA after 200 steps: the adjoint gradient w.r.t. the 16
+    amplitudes matches central differences with h = 1e-6 to 1e-5 relative
+    (the density-box loss above cannot, its gradient being 1e-4 of the loss)."""
+    steps = 200
+    sim, c = kh_sim(gpu)
+    ic = sim.tree()[1]
+    B0 = sim.download("Bi")
+    gi, gj = block_index(ic)
+    inner = interior_only(np.ones((len(ic), N_BLK, N_BLK))) / float(N * N)
+    a0 = torch.tensor(list(c.ic_param[:16]), dtype=torch.float64)
+
+    def run(a, record):
+        U, _, _ = K.kh_ic(a)
+        sim.upload("U", blocks_of(U, gi, gj).detach().numpy())
+        sim.upload("Bi", B0)
+        sim.adjoint_enable(record)
+        sim.run(steps)
+        return sim.download("U")
+
+    def loss(U):
+        return float((U[:, 2] ** 2 / U[:, 0] * inner).sum())
+
+    a = a0.clone().requires_grad_(True)
+    U0b = blocks_of(K.kh_ic(a)[0], gi, gj)
+    U = run(a0, True)
+    lam = np.zeros(U.shape)
+    lam[:, 2] = 2 * U[:, 2] / U[:, 0] * inner
+    lam[:, 0] = -(U[:, 2] / U[:, 0]) ** 2 * inner
+    sim.adjoint_seed("U", lam)
+    for _ in range(steps):
+        sim.adjoint_step()
+    gU = torch.from_numpy(sim.adjoint_read("U"))
+    (U0b * gU).sum().backward()          # chain rule through the IC
+    g = a.grad.numpy()
+    h = 1e-6
+    fd = np.zeros(16)
+    with torch.no_grad():
+        for k in range(16):
+            e = torch.zeros(16, dtype=torch.float64)
+            e[k] = h
+            fd[k] = (loss(run(a0 + e, False)) - loss(run(a0 - e, False))) / (2 * h)
+    err = np.abs(g - fd).max() / np.abs(fd).max()
+    assert err < 1e-5, (err, g, fd)
