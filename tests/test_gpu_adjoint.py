@@ -169,8 +169,11 @@ def test_kh_gradient_fd_and_reference(gpu):
 def test_kh_kinetic_energy_gradient_matches_fd(gpu):
     """A loss that scales with the perturbation, the transverse kinetic energy
     sum(m_y^2 / rho) dA after 200 steps: the adjoint gradient w.r.t. the 16
-    amplitudes matches central differences with h = 1e-6 to 1e-5 relative
-    (the density-box loss above cannot, its gradient being 1e-4 of the loss)."""
+    amplitudes matches central differences to 1e-5 relative (the density-box
+    loss above cannot, its gradient being 1e-4 of the loss).  The step is
+    h = 1e-7: the MC kinks still give a first-order term, 1e-5 to 4e-5 at
+    h = 1e-6 depending on the draw (seeds 42 and 5), ~1e-6 at h = 1e-7, while
+    roundoff stays below 1e-9."""
     steps = 200
     sim, c = kh_sim(gpu)
     ic = sim.tree()[1]
@@ -202,7 +205,7 @@ def test_kh_kinetic_energy_gradient_matches_fd(gpu):
     gU = torch.from_numpy(sim.adjoint_read("U"))
     (U0b * gU).sum().backward()          # chain rule through the IC
     g = a.grad.numpy()
-    h = 1e-6
+    h = 1e-7
     fd = np.zeros(16)
     with torch.no_grad():
         for k in range(16):
