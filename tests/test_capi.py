@@ -51,6 +51,14 @@ def test_create_rejects_bad_options_before_touching_the_gpu():
     L = amr.load()
     h = ctypes.c_void_p()
     for kw, code in [(dict(limiter="bogus"), -1), (dict(flux="ROE"), -11), (dict(flux="XYZ"), -1),
-                     (dict(limiter="WENO5", nghosts=2), -1), (dict(nx=8, ny=8), -11), (dict(ic="nope"), -1)]:
+                     (dict(limiter="WENO5", nghosts=2), -1), (dict(nx=8, ny=8), -11), (dict(ic="nope"), -1),
+                     (dict(ct_type=3), -1), (dict(ct_type=-1), -1), (dict(diffusion=2), -1)]:
         c = amr.make_config(**kw)
         assert L.amr_create(ctypes.byref(c), ctypes.byref(h)) == code, kw
+
+
+def test_step_halves_need_an_initialised_handle():
+    """amr_step_begin / amr_step_end on a NULL handle: argument error, no crash."""
+    L = amr.load()
+    assert L.amr_step_begin(None) == -12
+    assert L.amr_step_end(None) == -12
