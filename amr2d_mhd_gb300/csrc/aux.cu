@@ -60,11 +60,10 @@ cudaError_t launch_prim(const Method &m, const SplitArgs &a, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const int b = cell_threads(m);
   const unsigned g = static_cast<unsigned>((n + b - 1) / b);
-  if (m.ng == 2 && !m.f32) k_prim<2, double><<<g, b, 0, s>>>(a);
-  else if (m.ng == 2) k_prim<2, float><<<g, b, 0, s>>>(a);
-  else if (!m.f32) k_prim<4, double><<<g, b, 0, s>>>(a);
-  else k_prim<4, float><<<g, b, 0, s>>>(a);
-  return cudaGetLastError();
+  if (m.ng == 2 && !m.f32) return launch_k(m.pdl, k_prim<2, double>, g, b, 0, s, a);
+  if (m.ng == 2) return launch_k(m.pdl, k_prim<2, float>, g, b, 0, s, a);
+  if (!m.f32) return launch_k(m.pdl, k_prim<4, double>, g, b, 0, s, a);
+  return launch_k(m.pdl, k_prim<4, float>, g, b, 0, s, a);
 }
 
 cudaError_t launch_resid(const Method &m, const SplitArgs &a, cudaStream_t s) {
@@ -73,11 +72,10 @@ cudaError_t launch_resid(const Method &m, const SplitArgs &a, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const int b = cell_threads(m);
   const unsigned g = static_cast<unsigned>((n + b - 1) / b);
-  if (m.ng == 2 && !m.f32) k_resid<2, double><<<g, b, 0, s>>>(a);
-  else if (m.ng == 2) k_resid<2, float><<<g, b, 0, s>>>(a);
-  else if (!m.f32) k_resid<4, double><<<g, b, 0, s>>>(a);
-  else k_resid<4, float><<<g, b, 0, s>>>(a);
-  return cudaGetLastError();
+  if (m.ng == 2 && !m.f32) return launch_k(m.pdl, k_resid<2, double>, g, b, 0, s, a);
+  if (m.ng == 2) return launch_k(m.pdl, k_resid<2, float>, g, b, 0, s, a);
+  if (!m.f32) return launch_k(m.pdl, k_resid<4, double>, g, b, 0, s, a);
+  return launch_k(m.pdl, k_resid<4, float>, g, b, 0, s, a);
 }
 
 cudaError_t launch_ghost(const Method &m, const GhostLaunch &in, cudaStream_t s) {
@@ -89,14 +87,14 @@ cudaError_t launch_ghost(const Method &m, const GhostLaunch &in, cudaStream_t s)
   const unsigned rows = static_cast<unsigned>(g.row0[g.nseg]);
   const dim3 gs((g.nsnaps + B - 1) / B, rows), go((g.nops + B - 1) / B, rows);
   if (g.nsnaps > 0 && rows > 0) {
-    if (ng == 2) k_ghost_snap<Geo<2>::N><<<gs, B, 0, s>>>(g);
-    else k_ghost_snap<Geo<4>::N><<<gs, B, 0, s>>>(g);
+    const cudaError_t e = ng == 2 ? launch_k(m.pdl, k_ghost_snap<Geo<2>::N>, gs, B, 0, s, g)
+                                  : launch_k(m.pdl, k_ghost_snap<Geo<4>::N>, gs, B, 0, s, g);
+    if (e != cudaSuccess) return e;
   }
-  if (g.nops > 0 && rows > 0) {
-    if (ng == 2) k_ghost_apply<Geo<2>::N><<<go, B, 0, s>>>(g);
-    else k_ghost_apply<Geo<4>::N><<<go, B, 0, s>>>(g);
-  }
-  return cudaGetLastError();
+  if (g.nops > 0 && rows > 0)
+    return ng == 2 ? launch_k(m.pdl, k_ghost_apply<Geo<2>::N>, go, B, 0, s, g)
+                   : launch_k(m.pdl, k_ghost_apply<Geo<4>::N>, go, B, 0, s, g);
+  return cudaSuccess;
 }
 
 #define AMR_DISPATCH_NG_S(m, KERNEL, grid, block, smem, s, args)                 \
@@ -107,35 +105,36 @@ cudaError_t launch_ghost(const Method &m, const GhostLaunch &in, cudaStream_t s)
     else KERNEL<4, float><<<grid, block, smem, s>>>(args);                        \
   } while (0)
 
+// the same for the step's kernels, as programmatic dependents (Method::pdl)
+#define AMR_DISPATCH_NG_S_PDL(m, KERNEL, grid, block, smem, s, args)                                          \
+  (((m).ng == 2 && !(m).f32) ? launch_k((m).pdl, KERNEL<2, double>, dim3(grid), dim3(block), smem, s, args) \
+   : ((m).ng == 2)           ? launch_k((m).pdl, KERNEL<2, float>, dim3(grid), dim3(block), smem, s, args)  \
+   : !(m).f32                ? launch_k((m).pdl, KERNEL<4, double>, dim3(grid), dim3(block), smem, s, args) \
+                             : launch_k((m).pdl, KERNEL<4, float>, dim3(grid), dim3(block), smem, s, args))
+
 cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  AMR_DISPATCH_NG_S(m, k_ct_emf, n, 128, 0, s, a);
-  return cudaGetLastError();
+  return AMR_DISPATCH_NG_S_PDL(m, k_ct_emf, n, 128, 0, s, a);
 }
 
 cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  if (m.ng == 2) k_ct_face<2><<<n, 128, 0, s>>>(a);
-  else k_ct_face<4><<<n, 128, 0, s>>>(a);
-  return cudaGetLastError();
+  return m.ng == 2 ? launch_k(m.pdl, k_ct_face<2>, n, 128, 0, s, a) : launch_k(m.pdl, k_ct_face<4>, n, 128, 0, s, a);
 }
 
 cudaError_t launch_diffuse(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  AMR_DISPATCH_NG_S(m, k_diffuse, n, 128, 0, s, a);
-  return cudaGetLastError();
+  return AMR_DISPATCH_NG_S_PDL(m, k_diffuse, n, 128, 0, s, a);
 }
 
 cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  AMR_DISPATCH_NG_S(m, k_ct_cell, n, 128, 0, s, a);
-  return cudaGetLastError();
+  return AMR_DISPATCH_NG_S_PDL(m, k_ct_cell, n, 128, 0, s, a);
 }
 
 cudaError_t launch_dt_cell(const Method &m, const DtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  AMR_DISPATCH_NG_S(m, k_dt_cell, n, 256, 0, s, a);
-  return cudaGetLastError();
+  return AMR_DISPATCH_NG_S_PDL(m, k_dt_cell, n, 256, 0, s, a);
 }
 
 cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int n, cudaStream_t s) {

@@ -48,6 +48,7 @@ __device__ __forceinline__ GhostSeg ghost_seg(const GhostLaunch &g, int row, int
 // save the pre-fill values the same fill overwrites
 template <int N>
 __global__ void k_ghost_snap(GhostLaunch g) {
+  pdl_wait();
   constexpr int NN = N * N;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= g.nsnaps) return;
@@ -102,6 +103,7 @@ __device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp
 
 template <int N>
 __global__ void k_ghost_apply(GhostLaunch g) {
+  pdl_wait();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= g.nops) return;
   const GhostOp op = g.ops[r];
@@ -177,6 +179,7 @@ __device__ __forceinline__ void ct_emf_upwind(const CtArgs &a, const LeafTask &t
 // CT2D.cpp:16-26 corner EMF for i, j in [1, N)
 template <int NG, typename S>
 __global__ void k_ct_emf(CtArgs a) {
+  pdl_wait();
   constexpr int N = Geo<NG>::N, NN = N * N;
   const LeafTask t = a.tasks[blockIdx.x];
   if (a.inst[t.inst].ct_type == 2) {
@@ -203,6 +206,7 @@ __global__ void k_ct_emf(CtArgs a) {
 // CT2D.cpp:78-92 face update with the RK2 combine
 template <int NG>
 __global__ void k_ct_face(CtArgs a) {
+  pdl_wait();
   constexpr int N = Geo<NG>::N, NN = N * N;
   const LeafTask t = a.tasks[blockIdx.x];
   const double dt = a.inst[t.inst].dt;
@@ -225,6 +229,7 @@ __global__ void k_ct_face(CtArgs a) {
 // every cell of the block (ghosts included)
 template <int NG, typename S>
 __global__ void k_ct_cell(CtArgs a) {
+  pdl_wait();
   constexpr int N = Geo<NG>::N, NN = N * N;
   const LeafTask t = a.tasks[blockIdx.x];
   const double *B = a.Bnew + static_cast<size_t>(t.slot) * 2 * NN;
@@ -252,6 +257,7 @@ __global__ void k_ct_cell(CtArgs a) {
 // the block in shared memory, 8 variables x 16 cells per diagonal.
 template <int NG, typename S>
 __global__ void __launch_bounds__(128) k_diffuse(CtArgs a) {
+  pdl_wait();
   constexpr int N = Geo<NG>::N, NN = N * N, I0 = NG;  // interior [nxmin, nxmax] = [NG, NG + NI - 1]
   const LeafTask t = a.tasks[blockIdx.x];
   if (!(t.flags & TASK_DIFFUSE)) return;
@@ -301,6 +307,7 @@ struct DtArgs {
 
 template <int NG, typename S>
 __global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
+  pdl_wait();
   using G = Geo<NG>;
   using T = S;
   constexpr int N = G::N, NN = G::NN;

@@ -155,6 +155,7 @@ int Engine::create(const amr_config *cfgs, int n) {
   f32_ = m_.f32 != 0;
   if (const char *k = std::getenv("AMR2D_STAGE_KERNEL")) split_ = std::strcmp(k, "fused") != 0;
   if (const char *g = std::getenv("AMR2D_GRAPHS")) graph_on_ = std::strcmp(g, "0") != 0;
+  if (const char *p = std::getenv("AMR2D_PDL")) m_.pdl = std::strcmp(p, "0") != 0 ? 1 : 0;
   ng_ = m_.ng;
   n_ = NI + 2 * ng_;
   nn_ = n_ * n_;

@@ -25,7 +25,29 @@ struct Method {
   int cell_block = 256;
   int ghost_block = 256;
   int persistent = 0;   // face fluxes by a grid of resident CTAs looping over the face list
+  // the step's kernels are launched as programmatic dependents of their
+  // predecessor (each begins with pdl_wait()); AMR2D_PDL=0 turns it off
+  int pdl = 1;
 };
+
+// Launches kernel `k` on stream `s`, as a programmatic dependent of the
+// stream's previous kernel when `pdl` is set (the kernel must begin with
+// pdl_wait()).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(int pdl, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                            Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 // true if the (ng, recon, flux, precision) combination is compiled
 bool method_supported(const Method &m);

@@ -35,6 +35,14 @@ struct StageArgs {
   int step;
 };
 
+// First statement of every kernel of the step: when the kernel was launched
+// as a programmatic dependent of the previous one (Method::pdl), wait until
+// that grid has completed and its memory is visible; without that launch
+// attribute it returns at once.  The kernel may then be scheduled while its
+// predecessor drains, which hides most of the gap between the step's many
+// small kernels.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ void dev_fail(DevError *e, int code, int blk, int i, int j, double v) {
   if (atomicCAS(&e->code, 0, code) == 0) {
     e->blk = blk;
@@ -138,6 +146,7 @@ template <> struct StageMinBlocks<float> { static constexpr int value = AMR_STAG
 
 template <int NG, int RECON, int FLUX, typename S>
 __global__ void __launch_bounds__(256, StageMinBlocks<S>::value) k_stage(StageArgs a) {
+  pdl_wait();
   using G = Geo<NG>;
   using T = S;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI, NF = G::NF, NFX = G::NFX;

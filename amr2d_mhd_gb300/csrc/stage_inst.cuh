@@ -10,7 +10,7 @@
 namespace amr {
 
 template <int NG, int RECON, int FLUX, typename S>
-cudaError_t launch_stage_t(const StageArgs &a, int ntasks, cudaStream_t s) {
+cudaError_t launch_stage_t(const StageArgs &a, int ntasks, int pdl, cudaStream_t s) {
   constexpr int smem = stage_smem_bytes<NG, S>();
   static bool attr_set = false;
   if (!attr_set) {
@@ -20,17 +20,16 @@ cudaError_t launch_stage_t(const StageArgs &a, int ntasks, cudaStream_t s) {
     attr_set = true;
   }
   if (ntasks <= 0) return cudaSuccess;
-  k_stage<NG, RECON, FLUX, S><<<ntasks, 256, smem, s>>>(a);
-  return cudaGetLastError();
+  return launch_k(pdl, k_stage<NG, RECON, FLUX, S>, ntasks, 256, smem, s, a);
 }
 
 template <int FLUX, typename S>
 cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s) {
-  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_stage_t<2, REC_MUSCL, FLUX, S>(a, ntasks, s);
-  if (m.ng == 2 && m.recon == REC_WENO3) return launch_stage_t<2, REC_WENO3, FLUX, S>(a, ntasks, s);
-  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_stage_t<4, REC_MUSCL, FLUX, S>(a, ntasks, s);
-  if (m.ng == 4 && m.recon == REC_WENO3) return launch_stage_t<4, REC_WENO3, FLUX, S>(a, ntasks, s);
-  if (m.ng == 4 && m.recon == REC_WENO5) return launch_stage_t<4, REC_WENO5, FLUX, S>(a, ntasks, s);
+  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_stage_t<2, REC_MUSCL, FLUX, S>(a, ntasks, m.pdl, s);
+  if (m.ng == 2 && m.recon == REC_WENO3) return launch_stage_t<2, REC_WENO3, FLUX, S>(a, ntasks, m.pdl, s);
+  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_stage_t<4, REC_MUSCL, FLUX, S>(a, ntasks, m.pdl, s);
+  if (m.ng == 4 && m.recon == REC_WENO3) return launch_stage_t<4, REC_WENO3, FLUX, S>(a, ntasks, m.pdl, s);
+  if (m.ng == 4 && m.recon == REC_WENO5) return launch_stage_t<4, REC_WENO5, FLUX, S>(a, ntasks, m.pdl, s);
   return cudaErrorInvalidValue;
 }
 
@@ -39,7 +38,7 @@ cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, c
 #endif
 
 template <int NG, int RECON, int FLUX, typename S>
-cudaError_t launch_faces_t(const SplitArgs &a, int block, bool persistent, cudaStream_t s) {
+cudaError_t launch_faces_t(const SplitArgs &a, int block, bool persistent, int pdl, cudaStream_t s) {
   constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
   const size_t n = static_cast<size_t>(a.ntasks) * PER;
   if (n == 0) return cudaSuccess;
@@ -63,22 +62,21 @@ cudaError_t launch_faces_t(const SplitArgs &a, int block, bool persistent, cudaS
     }
     const size_t cap = static_cast<size_t>(sms) * ps;
     if (grid > cap) grid = cap;
-    k_faces_persist<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>(grid), block, 0, s>>>(a);
-  } else {
-    k_faces<NG, RECON, FLUX, S, AMR_FACES_MINB><<<static_cast<unsigned>(grid), block, 0, s>>>(a);
+    return launch_k(pdl, k_faces_persist<NG, RECON, FLUX, S, AMR_FACES_MINB>, static_cast<unsigned>(grid), block, 0,
+                    s, a);
   }
-  return cudaGetLastError();
+  return launch_k(pdl, k_faces<NG, RECON, FLUX, S, AMR_FACES_MINB>, static_cast<unsigned>(grid), block, 0, s, a);
 }
 
 template <int FLUX, typename S>
 cudaError_t launch_faces_flux(const Method &m, const SplitArgs &a, cudaStream_t s) {
   const int b = m.faces_block;
   const bool p = m.persistent != 0;
-  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, b, p, s);
-  if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, b, p, s);
-  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, b, p, s);
-  if (m.ng == 4 && m.recon == REC_WENO3) return launch_faces_t<4, REC_WENO3, FLUX, S>(a, b, p, s);
-  if (m.ng == 4 && m.recon == REC_WENO5) return launch_faces_t<4, REC_WENO5, FLUX, S>(a, b, p, s);
+  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, b, p, m.pdl, s);
+  if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, b, p, m.pdl, s);
+  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, b, p, m.pdl, s);
+  if (m.ng == 4 && m.recon == REC_WENO3) return launch_faces_t<4, REC_WENO3, FLUX, S>(a, b, p, m.pdl, s);
+  if (m.ng == 4 && m.recon == REC_WENO5) return launch_faces_t<4, REC_WENO5, FLUX, S>(a, b, p, m.pdl, s);
   return cudaErrorInvalidValue;
 }
 

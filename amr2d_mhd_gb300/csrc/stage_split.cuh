@@ -27,6 +27,7 @@ struct SplitArgs {
 // U2W / Us2W (meshblock.cpp:119-179) for every cell of every leaf
 template <int NG, typename S>
 __global__ void __launch_bounds__(512) k_prim(SplitArgs a) {
+  pdl_wait();
   using G = Geo<NG>;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
   const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -121,6 +122,7 @@ __device__ __forceinline__ void face_flux(const SplitArgs &a, size_t e) {
 
 template <int NG, int RECON, int FLUX, typename S, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_faces(SplitArgs a) {
+  pdl_wait();
   constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
   const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= static_cast<size_t>(a.ntasks) * PER) return;
@@ -131,6 +133,7 @@ __global__ void __launch_bounds__(128, MINB) k_faces(SplitArgs a) {
 // the whole face list of the step (all leaf blocks of all instances)
 template <int NG, int RECON, int FLUX, typename S, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_faces_persist(SplitArgs a) {
+  pdl_wait();
   constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
   const size_t n = static_cast<size_t>(a.ntasks) * PER;
   const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
@@ -142,6 +145,7 @@ __global__ void __launch_bounds__(128, MINB) k_faces_persist(SplitArgs a) {
 // (main.cpp:260-270 / 292-302)
 template <int NG, typename S>
 __global__ void __launch_bounds__(512) k_resid(SplitArgs a) {
+  pdl_wait();
   using G = Geo<NG>;
   using T = S;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
