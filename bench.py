@@ -64,6 +64,43 @@ def reduce_over_ranks(ms, cells, device):
     return float(mx[0]), float(t[1])
 
 
+L2_NOTE = ("L2 flushed before every timed step: 256 MB written on the launch stream outside the step's timing "
+           "events (the state, ~10-20 MB, would otherwise stay in the 129 MB L2)")
+
+
+class L2Flush:
+    """Writes 256 MB (more than the 129 MB L2) on `stream`, so that the next
+    timed step finds none of its state in L2."""
+
+    def __init__(self, stream):
+        import torch
+        self.torch = torch
+        self.buf = torch.empty(64 * 2 ** 20, dtype=torch.float32, device="cuda")
+        self.stream = stream
+        self.v = 0.0
+
+    def __call__(self):
+        self.v += 1.0
+        with self.torch.cuda.stream(self.stream):
+            self.buf.fill_(self.v)
+
+
+def timed_steps(step, n, stream, flush):
+    """n calls of `step` (one time step each), the L2 flushed before each and
+    each between its own CUDA events on the launch stream; summed ms."""
+    import torch
+    pairs = []
+    for _ in range(n):
+        flush()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        pairs.append((e0, e1))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in pairs)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -180,6 +217,7 @@ def run_ours(args):
         return sim.init()
 
     results = {}
+    flush = L2Flush(stream)
     for prec in ("fp64", "fp32"):
         sim = make(prec)
         advance_to(sim, T0)
@@ -192,13 +230,9 @@ def run_ours(args):
         i0 = sim.info()
         barrier()
         torch.cuda.synchronize()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        sim.run(K)
-        ev1.record(stream)
+        ms = timed_steps(sim.step, K, stream, flush)
         torch.cuda.synchronize()
         barrier()
-        ms = ev0.elapsed_time(ev1)
         i1 = sim.info()
         prof = sim.profile()
         clk = clocks.stop() if clocks else None
@@ -214,16 +248,17 @@ def run_ours(args):
             B = sim.download("Bi")
             sim.profile(False)
             j0 = sim.info()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            e2e_s = 0.0
             for _ in range(K):
+                flush()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
                 sim.upload("U", U)
                 sim.upload("Bi", B)
                 sim.step()
                 U = sim.download("U")
                 B = sim.download("Bi")
-            torch.cuda.synchronize()
-            e2e_s = time.perf_counter() - t0
+                e2e_s += time.perf_counter() - t0
             j1 = sim.info()
             p2 = sim.profile()
             results["e2e"] = dict(s=e2e_s, cells=j1["cell_updates"] - j0["cell_updates"],
@@ -400,6 +435,7 @@ def run_orszag_tang(stream):
 
     import amr2d_mhd_gb300 as amr
     out = []
+    flush = L2Flush(stream)
     for ml, lim, dt in OT_RUNS:
         res, rate = {}, {}
         for prec in ("fp64", "fp32"):
@@ -407,13 +443,11 @@ def run_orszag_tang(stream):
             sim.set_stream(stream.cuda_stream)
             sim.init()
             torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            sim.run()
-            e1.record(stream)
-            torch.cuda.synchronize()
+            ms = 0.0
+            while not sim.info()["done"]:   # steps past the end are no-ops
+                ms += timed_steps(sim.step, 50, stream, flush)
             inf = sim.info()
-            rate[prec] = inf["cell_updates"] / (e0.elapsed_time(e1) * 1e-3)
+            rate[prec] = inf["cell_updates"] / (ms * 1e-3)
             res[prec] = [sim.uniform(k) for k in range(8)]
             steps = inf["steps"]
             sim.close()
@@ -480,33 +514,29 @@ def run_adjoint(stream, steps=200):
         m[:ng, :] = 0; m[-ng:, :] = 0; m[:, :ng] = 0; m[:, -ng:] = 0
         mask[b] = m
 
-    def forward(a, record=False):
+    flush = L2Flush(stream)
+
+    def forward(a, record=False, timed=False):
         sim.upload("U", kh_u0(a, ic))
         sim.upload("Bi", B0)
         sim.adjoint_enable(record)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        e0.record(stream)
-        sim.run(steps)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        if timed:
+            ms = timed_steps(sim.step, steps, stream, flush)
+        else:
+            sim.run(steps)
+            ms = 0.0
         U = sim.download("U")
-        return float((U[:, 0] * mask).sum()), e0.elapsed_time(e1)
+        return float((U[:, 0] * mask).sum()), ms
 
     forward(a0)                                   # warm-up (graph capture)
-    _, fwd_ms = forward(a0)
-    L, rec_ms = forward(a0, record=True)
+    _, fwd_ms = forward(a0, timed=True)
+    L, rec_ms = forward(a0, record=True, timed=True)
     lam = np.zeros((len(ic), 8, 20, 20))
     lam[:, 0] = mask
     sim.adjoint_seed("U", lam)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(steps):
-        sim.adjoint_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    adj_ms = e0.elapsed_time(e1)
+    adj_ms = timed_steps(sim.adjoint_step, steps, stream, flush)
     gU = sim.adjoint_read("U")
 
     def grad_a(gU):
@@ -722,8 +752,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": r64["ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (rotor initial condition)",
         "config": {"workload": WORKLOAD_NAME, "leaves": r64["leaves"], "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "l2": "no flush: every step reads and writes the whole state (~%d MB FP64, below the 129 MB L2)"
-                         % int(r64["leaves"] * 1.25 * 8 * 400 * 8 / 1e6)},
+                   "l2": L2_NOTE + "; batches: state above L2 (no flush)"},
         "e2e": {"value": e2e["cells"] / e2e["s"], "unit": "cell-updates/s",
                 "h2d_bytes_per_step": int(e2e["h2d"]), "d2h_bytes_per_step": int(e2e["d2h"])},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -750,7 +779,8 @@ def main():
                         "error is the fp32 entry's" % (ROTOR_BATCH, T0),
             "fp64": res["rotor_batch"]["fp64"], "fp32": res["rotor_batch"]["fp32"],
             "fp32_batched_vs_plain_fp64": res["rotor_batch"]["fp32"]["value"] / value,
-            "l1_rel_density_vs_fp64_at_t_end": l1},
+            "l1_rel_density_vs_fp64_at_t_end": l1,
+            "l2": "no flush: the 64 states (~0.5 GB FP32, ~1 GB FP64) exceed the 129 MB L2"},
         "batch": None if "batch" not in res else {
             "workload": "%d seeded cylindrical blasts (seed %d, amr_config_blast): [0,1]^2, gamma 1.4, 4 roots, "
                         "maxlevs U{3..6}, MUSCL-MC + HLLE + CT, CFL 0.2, outflow; %d untimed batch steps, then "
@@ -759,7 +789,8 @@ def main():
             "fp32_two_handles_pipelined": res["batch"]["fp32_two_handles_pipelined"],
             "fp32_vs_plain_fp64_rotor": res["batch"]["fp32"]["value"] / value,
             "l1_rel_density_fp32_vs_fp64_max": res["batch"]["l1_rel_density_fp32_vs_fp64_max"],
-            "l1_sample": "4 instances of the batch (maxlevs capped at 4) run to t = 0.1, finest uniform grid"},
+            "l1_sample": "4 instances of the batch (maxlevs capped at 4) run to t = 0.1, finest uniform grid",
+            "l2": "no flush: the 512 states (several GB) exceed the 129 MB L2"},
         "adjoint": None if "adjoint" not in res else dict(
             workload="Kelvin-Helmholtz, frozen 256^2 periodic mesh (256 blocks), gamma 5/3, MUSCL-MC + RUSA + CT, "
                      "RK2, 200 steps of dt 2e-4, loss = total density in [0.4,0.6]^2, gradient w.r.t. the 16 "
