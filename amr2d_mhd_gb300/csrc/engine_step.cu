@@ -23,8 +23,11 @@ namespace amr {
 // memcpy into pinned memory followed by a pinned copy; a scatter / gather
 // kernel then moves the blocks between the staging buffer and their slots.
 // A pageable host-to-device copy has read its source when it returns, so an
-// upload returns without waiting for the device (later work on the stream is
-// ordered after the scatter); a download waits for its copy.
+// upload from pageable memory returns without waiting for the device (later
+// work on the stream is ordered after the scatter); from page-locked or
+// managed memory the copy is truly asynchronous, and the upload waits for it
+// so that the caller may reuse the array at once.  A download waits for its
+// copy.
 int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
   const int nblk = in.tree.lastActive;
   const int per = field_nv(field) * nn_;
@@ -44,6 +47,12 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
     prof_.h2d_bytes += static_cast<int64_t>(bytes + sizeof(int) * nblk);
     prof_.launches += 1;
     CK(cudaGetLastError(), "scatter");
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
+      cudaGetLastError();  // an unknown (pageable) pointer on older runtimes
+    } else if (pa.type == cudaMemoryTypeHost || pa.type == cudaMemoryTypeManaged) {
+      CK(cudaStreamSynchronize(stream_), "sync");
+    }
   } else {
     CK(launch_gather(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
        "gather");

@@ -90,3 +90,20 @@ def test_checkpoint_batch_and_errors(gpu, tmp_path):
         other.checkpoint_load(path)
     with pytest.raises(gpu.AmrError):
         a.checkpoint_load(path)
+
+
+@pytest.mark.gpu
+def test_upload_from_pinned_memory_may_be_reused_at_once(gpu):
+    """amr_upload from page-locked host memory (truly asynchronous copies):
+    overwriting the array right after the call must not change what the
+    device received."""
+    import torch
+    sim = gpu.Simulation(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4).init()
+    sim.run(5)
+    U = sim.download("U")
+    pinned = torch.empty(U.shape, dtype=torch.float64, pin_memory=True)
+    arr = pinned.numpy()
+    arr[...] = U * 1.0001
+    sim.upload("U", arr)
+    arr[...] = -1.0          # the caller reuses its buffer at once
+    assert np.array_equal(sim.download("U"), U * 1.0001)
