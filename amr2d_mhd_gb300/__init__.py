@@ -277,11 +277,18 @@ class Simulation:
         self._ck(load().amr_get_tree(self.h, instance, lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, na))
         return lp, ic, lf.astype(bool)
 
-    def download(self, field, instance=0):
+    def download(self, field, instance=0, out=None):
+        """Blocks 0..last_active-1 of `field` as float64 [block][var][j][i];
+        into `out` when it is a C-contiguous float64 array of that shape."""
         inf = self.info(instance)
         nv = {"Bi": 2, "Bis": 2, "EMF": 1}.get(field, 8)
         n = inf["nx_tot"]
-        a = np.empty((inf["last_active"], nv, n, n), np.float64)
+        shape = (inf["last_active"], nv, n, n)
+        if (out is not None and out.shape == shape and out.dtype == np.float64
+                and out.flags["C_CONTIGUOUS"] and out.flags["WRITEABLE"]):
+            a = out
+        else:
+            a = np.empty(shape, np.float64)
         self._ck(load().amr_download(self.h, instance, FIELDS[field], a.ctypes.data, a.size))
         return a
 

@@ -256,8 +256,8 @@ def run_ours(args):
                 sim.upload("U", U)
                 sim.upload("Bi", B)
                 sim.step()
-                U = sim.download("U")
-                B = sim.download("Bi")
+                U = sim.download("U", out=U)     # the caller's arrays are reused
+                B = sim.download("Bi", out=B)
                 e2e_s += time.perf_counter() - t0
             j1 = sim.info()
             p2 = sim.profile()

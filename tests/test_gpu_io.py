@@ -107,3 +107,17 @@ def test_upload_from_pinned_memory_may_be_reused_at_once(gpu):
     sim.upload("U", arr)
     arr[...] = -1.0          # the caller reuses its buffer at once
     assert np.array_equal(sim.download("U"), U * 1.0001)
+
+
+@pytest.mark.gpu
+def test_download_into_callers_array(gpu):
+    """download(out=...) fills the caller's array when it has the field's
+    shape, and allocates otherwise."""
+    sim = gpu.Simulation(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4).init()
+    sim.run(3)
+    U = sim.download("U")
+    buf = np.zeros_like(U)
+    got = sim.download("U", out=buf)
+    assert got is buf and np.array_equal(buf, U)
+    other = sim.download("U", out=np.zeros((1, 8, 20, 20)))
+    assert other.shape == U.shape and np.array_equal(other, U)
