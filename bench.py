@@ -737,6 +737,16 @@ def main():
         if ps and "dp_flops_per_cell" in ps:
             fp64["achieved_tflops"] = ps["dp_flops_per_cell"] * cells_per_launch / (stage_ms_avg * 1e-3) / 1e12
             fp64["frac"] = fp64["achieved_tflops"] / fp64["peak_tflops_dgemm"]
+        if ps and "fp64_pipe_inst_per_face" in ps and r64["clocks"]:
+            # issue slots of the FP64 pipe: 2 thread-instructions per SM per clock
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+            slots = 2.0 * sms * r64["clocks"]["sm_mhz"] * 1e6 * stage_ms_avg * 1e-3
+            faces = cells_per_launch / 256.0 * 578.0      # 2 x 17 x 17 faces per 16 x 16 block
+            fp64["pipe_busy_frac"] = ps["fp64_pipe_inst_per_face"] * faces / slots
+            fp64["arith_issue_frac"] = ps["fp64_arith_inst_per_face"] * faces / slots
+            fp64["issue_note"] = ("FP64-pipe instructions per face from ncu (profiles/faces_fp64_rotor_hlld.md) x faces "
+                                  "per launch / (2 x SMs x SM clock x launch time); DGEMM-relative frac counts an FMA as "
+                                  "2 flops per issue slot, this kernel issues mostly DADD / DMUL")
     except Exception as ex:  # noqa: BLE001
         fp64["error"] = str(ex)
     cpu = None
