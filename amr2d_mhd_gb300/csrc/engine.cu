@@ -290,7 +290,7 @@ int Engine::compile_programs() {
   const size_t nth = host_threads(blocks);
   while (gcs_.size() < nth) gcs_.push_back(new GhostCompiler(n_, ng_));
   std::vector<std::vector<Bound>> bounds(nth);
-  const std::string err = parallel_items(todo.size(), nth, [&](size_t w, size_t q) {
+  const std::string err = parallel_items(pool_, todo.size(), nth, [&](size_t w, size_t q) {
     Instance &in = inst_[todo[q]];
     in.tree.locate_bounds(bounds[w]);
     in.prog.clear();
@@ -402,7 +402,7 @@ int Engine::layout_programs(bool relayout) {
       up_ops.emplace_back(inst_[a].ops_off, inst_[a].ops_cap);
       up_snaps.emplace_back(inst_[a].snaps_off, inst_[a].snaps_cap);
     }
-  parallel_items(dirty.size(), host_threads(blocks), [&](size_t, size_t q) {
+  parallel_items(pool_, dirty.size(), host_threads(blocks), [&](size_t, size_t q) {
     Instance &in = inst_[dirty[q]];
     const int64_t no = static_cast<int64_t>(in.prog.ops.size()), ns = static_cast<int64_t>(in.prog.snaps.size());
     GhostOp *d = ho + in.ops_off;

@@ -12,6 +12,7 @@
 #include "../../include/amr2d_mhd.h"
 #include "amr_common.h"
 #include "ghost_compile.hpp"
+#include "host_par.hpp"
 #include "ic.hpp"
 #include "launch.hpp"
 #include "tree.hpp"
@@ -166,6 +167,7 @@ class Engine {
   DevBuf d_treeops_, d_stage_, d_slots_;
   HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_ops_, h_snaps_, h_tasks_;
   std::vector<GhostCompiler *> gcs_;  // one per compile thread
+  HostPool pool_;                      // host threads of the parallel loops (remesh, compile, layout)
 
   // CUDA graph of one step, re-captured when gen_ moves (tree, pool, profiling)
   bool graph_on_ = true;

@@ -80,7 +80,7 @@ int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vec
   std::vector<char> ok(which.size(), 1);
   size_t blocks = 0;
   for (int q : which) blocks += static_cast<size_t>(inst_[q].tree.lastActive);
-  parallel_items(which.size(), host_threads(blocks), [&](size_t, size_t w) {
+  parallel_items(pool_, which.size(), host_threads(blocks), [&](size_t, size_t w) {
     Instance &in = inst_[which[w]];
     if (in.cfg.maxlevs <= 1) return;
     std::vector<double> grad(in.tree.lastActive, 0.0);

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "ghost_compile.hpp"
+#include "host_par.hpp"
 
 extern "C" int ghost_shim_apply(int last_active, const int *lp, const int *icoord, const unsigned char *leafs,
                                 int maxlevs, int nrx, int nry, int periodic, int ng, int kind, int nv,
@@ -100,4 +101,22 @@ extern "C" int tree_shim_admesh(int *last_active, int *lp, int *icoord, unsigned
   *n_ref = static_cast<int>(plan.refine.size());
   *n_crs = static_cast<int>(plan.coarsen.size());
   return 0;
+}
+
+// The engine's host thread pool: `rounds` parallel loops of n items on up to
+// `threads` threads (the calling one included); each item adds its index to a
+// per-round sum.  Returns the number of rounds whose sum is wrong.
+extern "C" int host_pool_shim(int rounds, int n, int threads) {
+  amr::HostPool pool;
+  int bad = 0;
+  for (int r = 0; r < rounds; r++) {
+    std::vector<long long> part(static_cast<size_t>(threads), 0);
+    const std::string err = amr::parallel_items(pool, static_cast<size_t>(n), static_cast<size_t>(threads),
+                                                [&](size_t w, size_t q) { part[w] += static_cast<long long>(q) + r; });
+    long long sum = 0;
+    for (long long v : part) sum += v;
+    const long long want = static_cast<long long>(n) * (n - 1) / 2 + static_cast<long long>(n) * r;
+    bad += (sum != want || !err.empty()) ? 1 : 0;
+  }
+  return bad;
 }

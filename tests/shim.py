@@ -30,6 +30,7 @@ def lib():
             [ctypes.c_void_p] * 3
         L.tree_shim_admesh.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int,
                                                                                  ctypes.c_void_p, ctypes.c_void_p]
+        L.host_pool_shim.argtypes = [ctypes.c_int] * 3
         _lib = L
     return _lib
 
@@ -63,3 +64,7 @@ def admesh(st, grad, maxlevs, ng=2, nroots=(2, 2), periodic=False, cap=100000):
     assert rc == 0, rc
     n = na.value
     return dict(lastActive=n, nbleafs=nbl.value, lp=lp[:n], icoord=ic[:n], leafs=lf[:n].astype(bool)), nr.value, nc.value
+
+
+def host_pool(rounds, n, threads):
+    return lib().host_pool_shim(rounds, n, threads)

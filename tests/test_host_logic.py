@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as P
-from shim import admesh, ghost_apply
+from shim import admesh, ghost_apply, host_pool
 
 GHOST_CASES = [("BWx", "MC", 4, 2, 3), ("rotor", "MC", 5, 2, 30), ("BWx", "WENO5", 3, 4, 10),
                ("rotor", "WENO5", 3, 4, 25)]
@@ -56,3 +56,10 @@ def test_admesh_matches_oracle(ic, flux, L, steps):
         assert np.array_equal(got["icoord"], ref["icoord"])
         assert got["nbleafs"] == ref["nbleafs"]
     assert changes > 0
+
+
+@pytest.mark.parametrize("threads", [1, 2, 8])
+def test_host_pool_parallel_loops(threads):
+    """The engine's persistent host threads (remesh, compile and layout loops
+    of a batch): 300 consecutive loops of 1000 items, every item once."""
+    assert host_pool(300, 1000, threads) == 0
