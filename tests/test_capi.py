@@ -62,3 +62,13 @@ def test_step_halves_need_an_initialised_handle():
     L = amr.load()
     assert L.amr_step_begin(None) == -12
     assert L.amr_step_end(None) == -12
+
+
+def test_python_config_mirror_matches_the_c_struct():
+    """The ctypes mirror of amr_config has the C layout's size (the library
+    writes sizeof(amr_config) into struct_size) and the new fields land where
+    the C code reads them (ct_type / diffusion validated by amr_create)."""
+    c = amr.make_config(ct_type=2, diffusion=True)
+    assert c.struct_size == ctypes.sizeof(amr.Config)
+    assert (c.ct_type, c.diffusion, c.reserved[0], c.reserved[1]) == (2, 1, 0, 0)
+    assert ctypes.sizeof(amr.Profile) == 8 * 12   # 12 eight-byte fields of amr_profile
