@@ -28,7 +28,7 @@ STATUS = {0: "AMR_OK", -1: "AMR_E_CONFIG", -2: "AMR_E_CUDA", -3: "AMR_E_OOM", -4
 EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "amr_config_kh", "amr_abi_version", "amr_status_string",
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_step_begin", "amr_step_end", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
-           "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_download",
+           "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_set_tree", "amr_download",
            "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_autotune", "amr_save4py",
            "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
            "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
@@ -97,6 +97,8 @@ def load(build_if_missing: bool = True):
         "amr_last_error": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t]),
         "amr_init": (ctypes.c_int, [vp]),
         "amr_step": (ctypes.c_int, [vp]),
+        "amr_step_begin": (ctypes.c_int, [vp]),
+        "amr_step_end": (ctypes.c_int, [vp]),
         "amr_run": (ctypes.c_int, [vp, i64]),
         "amr_get_info": (ctypes.c_int, [vp, i32, ctypes.POINTER(Info)]),
         "amr_locate_bounds": (ctypes.c_int, [vp]),
@@ -106,6 +108,8 @@ def load(build_if_missing: bool = True):
         "amr_cfl_dt": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
         "amr_admesh": (ctypes.c_int, [vp]),
         "amr_get_tree": (ctypes.c_int, [vp, i32, dp, dp, dp, i32]),
+        "amr_set_tree": (ctypes.c_int, [vp, i32, i32, i32, dp, dp, dp, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, i64]),
         "amr_download": (ctypes.c_int, [vp, i32, i32, dp, i64]),
         "amr_upload": (ctypes.c_int, [vp, i32, i32, dp, i64]),
         "amr_profile_enable": (ctypes.c_int, [vp, i32]),
@@ -276,6 +280,16 @@ class Simulation:
         lf = np.zeros(na, np.uint8)
         self._ck(load().amr_get_tree(self.h, instance, lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, na))
         return lp, ic, lf.astype(bool)
+
+    def set_tree(self, lp, icoord, leafs, nb_leafs, t, dt, dt_next, steps, instance=0):
+        """Take over the quadtree and time state of a run (amr_set_tree), in
+        place of init(); then upload U, Bi (and ff, gg) before stepping."""
+        lp = np.ascontiguousarray(lp, np.int32)
+        ic = np.ascontiguousarray(icoord, np.int32)
+        lf = np.ascontiguousarray(np.asarray(leafs).astype(np.uint8))
+        self._ck(load().amr_set_tree(self.h, instance, lp.shape[0], int(nb_leafs), lp.ctypes.data, ic.ctypes.data,
+                                     lf.ctypes.data, float(t), float(dt), float(dt_next), int(steps)))
+        return self
 
     def download(self, field, instance=0, out=None):
         """Blocks 0..last_active-1 of `field` as float64 [block][var][j][i];

@@ -183,6 +183,10 @@ int amr_muscl2d_rk(amr_handle *h, int32_t s) { return guarded(h, [&](amr::Engine
 int amr_ct2d(amr_handle *h, int32_t s) { return guarded(h, [&](amr::Engine &e) { return e.api_ct2d(s); }); }
 int amr_cfl_dt(amr_handle *h, double *l) { return guarded(h, [&](amr::Engine &e) { return e.api_cfl_dt(l); }); }
 int amr_admesh(amr_handle *h) { return guarded(h, [](amr::Engine &e) { return e.api_admesh(); }); }
+int amr_set_tree(amr_handle *h, int32_t q, int32_t na, int32_t nbl, const int32_t *lp, const int32_t *ic,
+                 const uint8_t *lf, double t, double dt, double dtn, int64_t steps) {
+  return guarded(h, [&](amr::Engine &e) { return e.api_set_tree(q, na, nbl, lp, ic, lf, t, dt, dtn, steps); });
+}
 int amr_get_tree(amr_handle *h, int32_t q, int32_t *lp, int32_t *ic, uint8_t *lf, int32_t cap) {
   return guarded(h, [&](amr::Engine &e) { return e.get_tree(q, lp, ic, lf, cap); });
 }

@@ -49,6 +49,7 @@ struct Instance {
   int64_t count = 0;
   int64_t cell_updates = 0;
   bool done = false;
+  bool handed = false;        // state given by amr_set_tree
   int limiter = 0;
   std::vector<int> slot;      // block ID -> physical slot, -1 if none yet
   double dx[16] = {0}, dy[16] = {0};
@@ -83,6 +84,8 @@ class Engine {
   int api_cfl_dt(double *lambda_min);
   int api_admesh();
   int api_criteria(double *grad, int32_t cap);
+  int api_set_tree(int q, int32_t last_active, int32_t nb_leafs, const int32_t *lp, const int32_t *icoord,
+                   const uint8_t *leafs, double t, double dt, double dtn, int64_t steps);
   // host <-> device state
   int get_tree(int inst, int32_t *lp, int32_t *icoord, uint8_t *leafs, int32_t cap);
   int download(int inst, int field, double *dst, int64_t count);

@@ -375,6 +375,46 @@ int Engine::download(int q, int field, double *dst, int64_t count) {
   return AMR_OK;
 }
 
+// the quadtree and time state of a run the caller owns (amr_set_tree); the
+// handle counts as initialised once every instance has one
+int Engine::api_set_tree(int q, int32_t na, int32_t nbl, const int32_t *lp, const int32_t *icoord,
+                         const uint8_t *leafs, double t, double dt, double dtn, int64_t steps) {
+  if (initialised_) return fail(AMR_E_STATE, "amr_set_tree takes the place of amr_init");
+  if (q < 0 || q >= static_cast<int>(inst_.size()) || !lp || !icoord || !leafs)
+    return fail(AMR_E_ARG, "bad instance or pointer");
+  Instance &in = inst_[q];
+  Tree &tr = in.tree;
+  if (na < 1 || na > tr.maxblocks()) return fail(AMR_E_MAXBLOCKS, "last_active outside [1, maxblocks]");
+  for (int b = 0; b < tr.maxblocks(); b++) {
+    tr.leafs[b] = b < na ? (leafs[b] ? 1 : 0) : 0;
+    tr.iref[b] = 0;
+    tr.icoarse[b] = 0;
+  }
+  for (int b = 0; b < na; b++) {
+    for (int k = 0; k < 8; k++) tr.lp[b][k] = lp[8 * b + k];
+    tr.icoord[b] = {icoord[2 * b], icoord[2 * b + 1]};
+    if (tr.lp[b][0] < 0 || tr.lp[b][0] >= in.cfg.maxlevs) return fail(AMR_E_CONFIG, "block level outside maxlevs");
+  }
+  tr.lastActive = na;
+  tr.nbleafs = nbl;
+  tr.version++;
+  in.t = t;
+  in.dt = dt;
+  in.dtn = dtn;
+  in.count = steps;
+  in.cell_updates = 0;
+  in.done = false;
+  if (int rc = assign_slots(in)) return rc;
+  in.handed = true;
+  bool all = true;
+  for (const Instance &x : inst_) all = all && x.handed;
+  if (all) {
+    programs_valid_ = false;
+    initialised_ = true;
+  }
+  return AMR_OK;
+}
+
 int Engine::upload(int q, int field, const double *src, int64_t count) {
   if (q < 0 || q >= static_cast<int>(inst_.size()) || !src) return fail(AMR_E_ARG, "bad instance or pointer");
   Instance &in = inst_[q];

@@ -169,6 +169,18 @@ int amr_admesh(amr_handle *h);
  * cap >= amr_info.last_active */
 int amr_criteria(amr_handle *h, double *grad, int32_t cap);                               /* admesh.cpp:17 */
 
+/* ---- handing over a run (extension: no counterpart in the reference) -----
+ * Instance `instance` of a created handle takes the quadtree and time state
+ * of a run the caller owns, e.g. a reference run stopped after some step:
+ * lp[last_active][8], icoord[last_active][2] and leafs[last_active] (the
+ * meshblock records, defs.hpp:52-62), the reference's nbleafs counter, t, dt
+ * and dt_next as amr_get_info reports them, and the step count.  Call it for
+ * every instance instead of amr_init; then amr_upload U and Bi (and ff / gg,
+ * whose low ghost face the next residual reads as the last stage left it,
+ * main.cpp:150, for a bit-identical continuation) before stepping. */
+int amr_set_tree(amr_handle *h, int32_t instance, int32_t last_active, int32_t nb_leafs, const int32_t *lp,
+                 const int32_t *icoord, const uint8_t *leafs, double t, double dt, double dt_next, int64_t steps);
+
 /* ---- state exchange with host buffers ----------------------------------- */
 /* Tree of one instance: lp[last_active][8], icoord[last_active][2], leafs[last_active] */
 int amr_get_tree(amr_handle *h, int32_t instance, int32_t *lp, int32_t *icoord, uint8_t *leafs,

@@ -136,3 +136,28 @@ def test_criteria_matches_oracle(gpu):
     ref = P.criteria_grad(W, 2)
     assert np.array_equal(g[lf], ref[lf])
     assert np.all(g[~lf] == -1.0)
+
+
+@pytest.mark.gpu
+def test_set_tree_continues_a_run_bit_for_bit(gpu):
+    """A run handed over mid-way (the oracle's quadtree, time state and the
+    fields U, Bi, ff, gg after 20 steps, as a reference run would hand them)
+    continues bit-identical to the oracle for 15 more steps, remeshing
+    included."""
+    kw = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4)
+    o = P.Oracle(**kw).init()
+    o.run(20)
+    inf = o.info()
+    sim = gpu.Simulation(**to_gpu_cfg(kw))   # created, not initialised
+    sim.set_tree(o.get("lp"), o.get("icoord"), o.get("leafs"), inf["nbleafs"], inf["t"], inf["dt"],
+                 inf["dt_next"], inf["count"])
+    for f in ("U", "Bi", "ff", "gg"):
+        sim.upload(f, o.get(f))
+    o.run(35)
+    sim.run(15)
+    a, b = sim.state(), o.state()
+    assert P.compare_states(a, b, 2)[0]
+    assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["Bi"], b["Bi"]) and a["t"] == b["t"]
+    assert sim.info()["steps"] == 35
+    with pytest.raises(gpu.AmrError):   # amr_set_tree takes the place of amr_init
+        sim.set_tree(o.get("lp"), o.get("icoord"), o.get("leafs"), inf["nbleafs"], 0.0, 0.0, 0.0, 0)
