@@ -204,6 +204,9 @@ int amr_profile_read(amr_handle *h, amr_profile *o) {
   return guarded(h, [&](amr::Engine &e) { return e.profile_read(o); });
 }
 
+int amr_criteria_flags(amr_handle *h, uint8_t *iref, uint8_t *icoarse, int32_t cap) {
+  return guarded(h, [&](amr::Engine &e) { return e.api_criteria_flags(iref, icoarse, cap); });
+}
 int amr_criteria(amr_handle *h, double *grad, int32_t cap) {
   return guarded(h, [&](amr::Engine &e) { return e.api_criteria(grad, cap); });
 }

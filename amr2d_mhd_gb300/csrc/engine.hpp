@@ -84,6 +84,7 @@ class Engine {
   int api_cfl_dt(double *lambda_min);
   int api_admesh();
   int api_criteria(double *grad, int32_t cap);
+  int api_criteria_flags(uint8_t *iref, uint8_t *icoarse, int32_t cap);
   int api_set_tree(int q, int32_t last_active, int32_t nb_leafs, const int32_t *lp, const int32_t *icoord,
                    const uint8_t *leafs, double t, double dt, double dtn, int64_t steps);
   // host <-> device state

@@ -330,6 +330,26 @@ int Engine::api_criteria(double *grad, int32_t cap) {
   return AMR_OK;
 }
 
+// criteria.cpp:31,43 (markref.cpp:6-18) on the device criterion of each leaf
+int Engine::api_criteria_flags(uint8_t *iref, uint8_t *icoarse, int32_t cap) {
+  if (!iref || !icoarse) return fail(AMR_E_ARG, "null pointer");
+  const Instance &in = inst_[0];
+  std::vector<double> g(static_cast<size_t>(in.tree.lastActive > 0 ? in.tree.lastActive : 1));
+  if (cap < in.tree.lastActive) return fail(AMR_E_ARG, "buffer too small");
+  if (int rc = api_criteria(g.data(), static_cast<int32_t>(g.size()))) return rc;
+  for (int b = 0; b < in.tree.lastActive; b++) {
+    iref[b] = 0;
+    icoarse[b] = 0;
+    if (!in.tree.leafs[b]) continue;
+    if (g[b] >= 0.05) {
+      if (in.tree.lp[b][0] < in.cfg.maxlevs - 1) iref[b] = 1;
+    } else if (g[b] <= 1.0) {
+      icoarse[b] = 1;
+    }
+  }
+  return AMR_OK;
+}
+
 int Engine::api_admesh() {
   double lam;
   if (int rc = api_cfl_dt(&lam)) return rc;

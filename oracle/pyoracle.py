@@ -244,6 +244,15 @@ def criteria_grad(W, ng=2):
     return out
 
 
+def criteria_flags(grad, leafs, level, maxlevs, r_thresh=0.05, c_thresh=1.0):
+    """criteria.cpp:31-43: refine a leaf whose criterion reaches r_thresh below
+    the finest level; coarsen a leaf whose criterion stays below r_thresh and
+    at most c_thresh (before the neighbour rule of critneighup.cpp)."""
+    iref = leafs & (grad >= r_thresh) & (level < maxlevs - 1)
+    icoarse = leafs & (grad < r_thresh) & (grad <= c_thresh)
+    return iref, icoarse
+
+
 def compare_states(a, b, ng=2):
     """Compare two states (dicts as above) on the leaf blocks.
 

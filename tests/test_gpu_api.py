@@ -136,6 +136,10 @@ def test_criteria_matches_oracle(gpu):
     ref = P.criteria_grad(W, 2)
     assert np.array_equal(g[lf], ref[lf])
     assert np.all(g[~lf] == -1.0)
+    iref, ico = sim.criteria_flags()
+    eref, eco = P.criteria_flags(ref, lf, o.get("lp")[:, 0], kw["maxlevs"])
+    assert np.array_equal(iref, eref) and np.array_equal(ico, eco)
+    assert ico.any()   # the ambient region is uniform: its leaves are marked to coarsen
 
 
 @pytest.mark.gpu
