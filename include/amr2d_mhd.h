@@ -168,7 +168,7 @@ int amr_admesh(amr_handle *h);
  * (admesh refines where it is >= 0.05), -1 for blocks that are not leaves;
  * cap >= amr_info.last_active */
 int amr_criteria(amr_handle *h, double *grad, int32_t cap);                               /* admesh.cpp:17 */
-/* the same as criteria.cpp's flags (:31, :43): iref[b] = 1 where a leaf's
+/* criteria.cpp's flags (:31, :43) of instance 0: iref[b] = 1 where a leaf's
  * criterion is >= 0.05 below the finest level, icoarse[b] = 1 where it is
  * below 0.05; 0 elsewhere and for non-leaves (admesh then applies the
  * neighbour rule of critneighup.cpp); cap >= amr_info.last_active */

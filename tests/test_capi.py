@@ -72,3 +72,21 @@ def test_python_config_mirror_matches_the_c_struct():
     assert c.struct_size == ctypes.sizeof(amr.Config)
     assert (c.ct_type, c.diffusion, c.reserved[0], c.reserved[1]) == (2, 1, 0, 0)
     assert ctypes.sizeof(amr.Profile) == 8 * 12   # 12 eight-byte fields of amr_profile
+
+
+def test_every_entry_point_rejects_a_null_handle():
+    """Each call that takes a handle returns AMR_E_ARG for NULL (no crash, no
+    device call); amr_destroy(NULL) is a no-op like free(NULL)."""
+    L = amr.load()
+    handle_first = {"amr_destroy", "amr_set_stream", "amr_last_error"} | {
+        n for n in amr.EXPORTS
+        if n not in ("amr_cfl_dt_static", "amr_config_default", "amr_config_from_input", "amr_config_blast",
+                     "amr_config_kh", "amr_abi_version", "amr_status_string", "amr_create", "amr_create_batch")}
+    assert "amr_criteria_flags" in handle_first and "amr_set_tree" in handle_first
+    for n in sorted(handle_first):
+        fn = getattr(L, n)
+        args = [None] + [0 if t in (ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t, ctypes.c_double) else None
+                         for t in fn.argtypes[1:]]
+        assert fn(*args) == (0 if n == "amr_destroy" else -12), n
+    # the allocation-free CFL reduction checks its pointers before any launch
+    assert L.amr_cfl_dt_static(None, 4, 2, None, 5 / 3, None, None) == -12
