@@ -29,7 +29,7 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "a
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_step_begin", "amr_step_end", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_set_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_criteria_flags", "amr_autotune", "amr_save4py",
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_criteria_flags", "amr_admesh_marked", "amr_autotune", "amr_save4py",
            "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
            "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
 
@@ -117,6 +117,7 @@ def load(build_if_missing: bool = True):
         "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
         "amr_criteria": (ctypes.c_int, [vp, dp, i32]),
         "amr_criteria_flags": (ctypes.c_int, [vp, dp, dp, i32]),
+        "amr_admesh_marked": (ctypes.c_int, [vp, dp, dp, i32]),
         "amr_autotune": (ctypes.c_int, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "amr_save4py": (ctypes.c_int, [vp, i32, i32, ctypes.c_char_p, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "amr_checkpoint_save": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -359,6 +360,16 @@ class Simulation:
         ico = np.zeros(na, np.uint8)
         self._ck(load().amr_criteria_flags(self.h, iref.ctypes.data, ico.ctypes.data, na))
         return iref.astype(bool), ico.astype(bool)
+
+    def admesh_marked(self, iref, icoarse):
+        """admesh with the caller's refine / coarsen marks per block ID
+        (amr_admesh_marked)."""
+        na = self.info()["last_active"]
+        r = np.ascontiguousarray(np.asarray(iref, dtype=bool)[:na], np.uint8)
+        c = np.ascontiguousarray(np.asarray(icoarse, dtype=bool)[:na], np.uint8)
+        if r.size < na or c.size < na:
+            raise ValueError("need a mark per block ID (%d)" % na)
+        self._ck(load().amr_admesh_marked(self.h, r.ctypes.data, c.ctypes.data, na))
 
     def autotune(self, reps=5):
         """Pick the fastest launch schedule on the current state; returns the

@@ -204,6 +204,9 @@ int amr_profile_read(amr_handle *h, amr_profile *o) {
   return guarded(h, [&](amr::Engine &e) { return e.profile_read(o); });
 }
 
+int amr_admesh_marked(amr_handle *h, const uint8_t *iref, const uint8_t *icoarse, int32_t n) {
+  return guarded(h, [&](amr::Engine &e) { return e.api_admesh_marked(iref, icoarse, n); });
+}
 int amr_criteria_flags(amr_handle *h, uint8_t *iref, uint8_t *icoarse, int32_t cap) {
   return guarded(h, [&](amr::Engine &e) { return e.api_criteria_flags(iref, icoarse, cap); });
 }

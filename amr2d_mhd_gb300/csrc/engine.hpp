@@ -85,6 +85,7 @@ class Engine {
   int api_admesh();
   int api_criteria(double *grad, int32_t cap);
   int api_criteria_flags(uint8_t *iref, uint8_t *icoarse, int32_t cap);
+  int api_admesh_marked(const uint8_t *iref, const uint8_t *icoarse, int32_t n);
   int api_set_tree(int q, int32_t last_active, int32_t nb_leafs, const int32_t *lp, const int32_t *icoord,
                    const uint8_t *leafs, double t, double dt, double dtn, int64_t steps);
   // host <-> device state
@@ -133,7 +134,11 @@ class Engine {
   int ct2d(int step);
   int dt_crit(bool want_grad);
   int finish_step();
-  int admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad);
+  struct AdmeshMarks {
+    const uint8_t *ref, *crs;
+  };
+  int admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad,
+                 const AdmeshMarks *marks = nullptr);
   int xfer(Instance &in, int field, double *host, bool to_device);
   void *field_ptr(int field) const;
   int field_nv(int field) const;

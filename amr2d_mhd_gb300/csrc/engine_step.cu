@@ -67,10 +67,12 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
 
 // admesh.cpp:17-102 for the instances in `which`; the criterion comes from the
 // device reduction of the last dt_crit (or, at initialisation, from the IC's
-// primitive state on the host).  The refine / coarsen kernels run while the
+// primitive state on the host), or the caller's marks replace it (`marks`,
+// one instance).  The refine / coarsen kernels run while the
 // host compiles the changed instances' ghost programs; the device error check
 // (U2W("refine") traps) follows, so errors surface before the call returns.
-int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad) {
+int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad,
+                       const AdmeshMarks *marks) {
   const auto t0 = std::chrono::steady_clock::now();
   std::vector<TreeOp> ref, crs;
   // the quadtrees of a batch are independent: admesh them on host threads,
@@ -83,6 +85,10 @@ int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vec
   parallel_items(pool_, which.size(), host_threads(blocks), [&](size_t, size_t w) {
     Instance &in = inst_[which[w]];
     if (in.cfg.maxlevs <= 1) return;
+    if (marks) {
+      ok[w] = in.tree.admesh_marked(marks->ref, marks->crs, plans[w], errs[w]) ? 1 : 0;
+      return;
+    }
     std::vector<double> grad(in.tree.lastActive, 0.0);
     if (host_grad) {
       grad = (*host_grad)[which[w]];
@@ -348,6 +354,16 @@ int Engine::api_criteria_flags(uint8_t *iref, uint8_t *icoarse, int32_t cap) {
     }
   }
   return AMR_OK;
+}
+
+// admesh.cpp:17-102 on instance 0 with the caller's refine / coarsen marks
+// (per block ID) in place of criteria.cpp's
+int Engine::api_admesh_marked(const uint8_t *iref, const uint8_t *icoarse, int32_t n) {
+  if (!initialised_) return fail(AMR_E_STATE, "amr_init has not been called");
+  if (!iref || !icoarse) return fail(AMR_E_ARG, "null pointer");
+  if (n < inst_[0].tree.lastActive) return fail(AMR_E_ARG, "fewer marks than last_active blocks");
+  const AdmeshMarks m{iref, icoarse};
+  return admesh_all({0}, nullptr, &m);
 }
 
 int Engine::api_admesh() {

@@ -139,8 +139,6 @@ void Tree::updatelpdown(int dad, const int *s) {
 
 bool Tree::admesh(const std::vector<double> &grad, AdmeshPlan &plan, std::string &err) {
   const int maxlevs = shape_.maxlevs;
-  plan.refine.clear();
-  plan.coarsen.clear();
   // markref.cpp:6-18 + criteria.cpp:31,43 (thresholds 0.05 / 1.0)
   for (int nb = 0; nb < lastActive; nb++) { iref[nb] = 0; icoarse[nb] = 0; }
   for (int nb = 0; nb < lastActive; nb++) {
@@ -152,6 +150,29 @@ bool Tree::admesh(const std::vector<double> &grad, AdmeshPlan &plan, std::string
       icoarse[nb] = 1;
     }
   }
+  return apply_marks(plan, err);
+}
+
+bool Tree::admesh_marked(const uint8_t *mark_ref, const uint8_t *mark_crs, AdmeshPlan &plan, std::string &err) {
+  const int maxlevs = shape_.maxlevs;
+  // the marks as criteria.cpp:31-43 leaves them: leaves only, refinement
+  // below the finest level, a refine mark cancelling a coarsen mark
+  for (int nb = 0; nb < lastActive; nb++) { iref[nb] = 0; icoarse[nb] = 0; }
+  for (int nb = 0; nb < lastActive; nb++) {
+    if (!leafs[nb] || lp[nb][0] < 0) continue;
+    if (mark_ref[nb]) {
+      if (lp[nb][0] < maxlevs - 1) iref[nb] = 1;
+    } else if (mark_crs[nb]) {
+      icoarse[nb] = 1;
+    }
+  }
+  return apply_marks(plan, err);
+}
+
+bool Tree::apply_marks(AdmeshPlan &plan, std::string &err) {
+  const int maxlevs = shape_.maxlevs;
+  plan.refine.clear();
+  plan.coarsen.clear();
   // critneighup.cpp:6-34: keep neighbours within one level
   for (int nl = maxlevs - 1; nl >= 0; nl--)
     for (int nb = 0; nb < lastActive; nb++)

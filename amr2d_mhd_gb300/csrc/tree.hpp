@@ -50,6 +50,11 @@ class Tree {
   // Applies refine / coarsen to the tree and lists them in `plan`.
   // Returns false (with `err`) when the block budget is exceeded.
   bool admesh(const std::vector<double> &grad, AdmeshPlan &plan, std::string &err);
+  // admesh.cpp:17-102 with the caller's marks in place of criteria.cpp's:
+  // mark_ref[nb] / mark_crs[nb] are read for leaves only; a refine mark on
+  // the finest level is dropped and cancels a coarsen mark, as in
+  // criteria.cpp:31-43.  The neighbour rules and the operations are admesh's.
+  bool admesh_marked(const uint8_t *mark_ref, const uint8_t *mark_crs, AdmeshPlan &plan, std::string &err);
 
   std::vector<std::array<int, 8>> lp;      // level, father, first son, sibling, L, R, D, U
   std::vector<std::array<int, 2>> icoord;  // block origin in cells of its own level
@@ -59,6 +64,8 @@ class Tree {
   uint64_t version = 0;  // bumped whenever the tree changes
 
  private:
+  // critneighup / refine / critneighdown / coarsen on iref and icoarse
+  bool apply_marks(AdmeshPlan &plan, std::string &err);
   void updatelpup(int nb, const int *s);
   void updatelpdown(int dad, const int *s);
   TreeShape shape_;

@@ -173,6 +173,15 @@ int amr_criteria(amr_handle *h, double *grad, int32_t cap);                     
  * below 0.05; 0 elsewhere and for non-leaves (admesh then applies the
  * neighbour rule of critneighup.cpp); cap >= amr_info.last_active */
 int amr_criteria_flags(amr_handle *h, uint8_t *iref, uint8_t *icoarse, int32_t cap);
+/* admesh.cpp:17-102 on instance 0 with the caller's marks in place of
+ * criteria.cpp's (the prolongation / restriction of chosen blocks): for each
+ * leaf b, iref[b] != 0 refines it (dropped on the finest level), else
+ * icoarse[b] != 0 marks it for coarsening; entries of non-leaves are
+ * ignored.  The neighbour rules (critneighup.cpp, critneighdown.cpp), the
+ * four-sibling rule and the refine / coarsen operators (refine.cpp,
+ * refineBi_CT.cpp, coarsen.cpp, coarsenBi_CT.cpp) are admesh's, so marks
+ * equal to amr_criteria_flags give amr_admesh's result.  n >= last_active. */
+int amr_admesh_marked(amr_handle *h, const uint8_t *iref, const uint8_t *icoarse, int32_t n);
 
 /* ---- handing over a run (extension: no counterpart in the reference) -----
  * Instance `instance` of a created handle takes the quadtree and time state

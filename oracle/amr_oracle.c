@@ -1496,13 +1496,24 @@ static void criteria(oracle *o, int nb) {
   if (grad <= cT) o->icoarse[nb] = 1;
 }
 
-/* admesh.cpp:17-102 with markref.cpp, critneighup.cpp, critneighdown.cpp */
-static int admesh(oracle *o) {
+/* admesh.cpp:17-102 with markref.cpp, critneighup.cpp, critneighdown.cpp;
+ * with mref / mcrs non-NULL the caller's marks take criteria's place, set as
+ * criteria.cpp:31-43 sets them (leaves only, no refinement on the finest
+ * level, a refine mark cancelling a coarsen mark) */
+static int admesh_with(oracle *o, const unsigned char *mref, const unsigned char *mcrs) {
   int (*lp)[8] = o->lp;
   int maxlevs = o->c.maxlevs;
   for (int nb = 0; nb < o->lastActive; nb++) { o->iref[nb] = 0; o->icoarse[nb] = 0; }
-  for (int nb = 0; nb < o->lastActive; nb++)
-    if (o->leafs[nb] && lp[nb][0] >= 0) criteria(o, nb);
+  for (int nb = 0; nb < o->lastActive; nb++) {
+    if (!o->leafs[nb] || lp[nb][0] < 0) continue;
+    if (!mref) {
+      criteria(o, nb);
+    } else if (mref[nb]) {
+      if (lp[nb][0] < maxlevs - 1) o->iref[nb] = 1;
+    } else if (mcrs[nb]) {
+      o->icoarse[nb] = 1;
+    }
+  }
   for (int nl = maxlevs - 1; nl >= 0; nl--)        /* critneighup.cpp:6-34 */
     for (int nb = 0; nb < o->lastActive; nb++)
       if (o->iref[nb] && lp[nb][0] == nl)
@@ -1547,6 +1558,8 @@ static int admesh(oracle *o) {
       }
   return 0;
 }
+
+static int admesh(oracle *o) { return admesh_with(o, NULL, NULL); }
 
 /* ------------------------------------------------------------ IC2Dtype.cpp */
 static void set_w(oracle *o, int nb, int i, int j, const double *w) {
@@ -1864,6 +1877,10 @@ const char *oracle_error(const oracle *o) { return o->err_set ? o->err : ""; }
  * (boundaryfc.cpp), 2 = edge (boundaryec.cpp) */
 void oracle_set_remesh(oracle *o, int on) { o->no_remesh = !on; }
 int oracle_admesh(oracle *o) { return admesh(o); }
+int oracle_admesh_marked(oracle *o, const unsigned char *iref, const unsigned char *icoarse) {
+  if (!iref || !icoarse) return fail(o, "null marks");
+  return admesh_with(o, iref, icoarse);
+}
 
 int oracle_fill(oracle *o, double *field, int nv, int kind) {
   locate_bounds(o);

@@ -74,6 +74,8 @@ int oracle_set(oracle *o, int what, const double *src);
 /* test hooks: skip the remesh at the end of oracle_step; run admesh alone */
 void oracle_set_remesh(oracle *o, int on);
 int oracle_admesh(oracle *o);
+/* admesh with the caller's marks per block ID in place of criteria's */
+int oracle_admesh_marked(oracle *o, const unsigned char *iref, const unsigned char *icoarse);
 
 /* the sequential ghost fill of the current tree applied to `field` */
 int oracle_fill(oracle *o, double *field, int nv, int kind);

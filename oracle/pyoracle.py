@@ -79,6 +79,7 @@ def lib():
         L.oracle_error.argtypes = [ctypes.c_void_p]
         L.oracle_set_remesh.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.oracle_admesh.argtypes = [ctypes.c_void_p]
+        L.oracle_admesh_marked.argtypes = [ctypes.c_void_p] * 3
         L.oracle_fill.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.oracle_slopelimiter.restype = ctypes.c_double
         L.oracle_slopelimiter.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
@@ -174,6 +175,14 @@ class Oracle:
 
     def admesh(self):
         self._check(lib().oracle_admesh(self.h))
+
+    def admesh_marked(self, iref, icoarse):
+        """admesh with the caller's marks per block ID (criteria's place)."""
+        n = self.info()["lastActive"]
+        r = np.ascontiguousarray(np.asarray(iref, bool)[:n], np.uint8)
+        c = np.ascontiguousarray(np.asarray(icoarse, bool)[:n], np.uint8)
+        assert r.size == n and c.size == n
+        self._check(lib().oracle_admesh_marked(self.h, r.ctypes.data, c.ctypes.data))
 
     def fill(self, field, kind):
         """Sequential ghost fill (kind 0 cell, 1 face, 2 edge) of a copy of `field`."""

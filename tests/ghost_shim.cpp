@@ -70,11 +70,13 @@ extern "C" int ghost_shim_apply(int last_active, const int *lp, const int *icoor
   return 0;
 }
 
-// the product's Tree::admesh on a given tree and per-block criterion; writes
-// the new tree back and returns the number of refine and coarsen operations
+// the product's Tree::admesh on a given tree and per-block criterion (or,
+// with grad NULL, Tree::admesh_marked on the marks mref / mcrs); writes the
+// new tree back and returns the number of refine and coarsen operations
 extern "C" int tree_shim_admesh(int *last_active, int *lp, int *icoord, unsigned char *leafs, int *nbleafs,
                                 int maxlevs, int nrx, int nry, int periodic, int ng, const double *grad,
-                                int cap, int *n_ref, int *n_crs) {
+                                int cap, int *n_ref, int *n_crs, const unsigned char *mref,
+                                const unsigned char *mcrs) {
   using namespace amr;
   TreeShape s{16, 16, ng, maxlevs, nrx, nry, periodic != 0};
   Tree t(s);
@@ -85,10 +87,14 @@ extern "C" int tree_shim_admesh(int *last_active, int *lp, int *icoord, unsigned
     t.icoord[b] = {icoord[2 * b], icoord[2 * b + 1]};
     t.leafs[b] = leafs[b];
   }
-  std::vector<double> g(grad, grad + t.lastActive);
   AdmeshPlan plan;
   std::string err;
-  if (!t.admesh(g, plan, err)) return -1;
+  if (grad) {
+    std::vector<double> g(grad, grad + t.lastActive);
+    if (!t.admesh(g, plan, err)) return -1;
+  } else if (!t.admesh_marked(mref, mcrs, plan, err)) {
+    return -1;
+  }
   if (t.lastActive > cap) return -2;
   *last_active = t.lastActive;
   *nbleafs = t.nbleafs;

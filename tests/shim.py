@@ -28,8 +28,8 @@ def lib():
         L = ctypes.CDLL(OUT)
         L.ghost_shim_apply.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 7 + \
             [ctypes.c_void_p] * 3
-        L.tree_shim_admesh.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int,
-                                                                                 ctypes.c_void_p, ctypes.c_void_p]
+        L.tree_shim_admesh.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int] + \
+            [ctypes.c_void_p] * 4
         L.host_pool_shim.argtypes = [ctypes.c_int] * 3
         _lib = L
     return _lib
@@ -48,7 +48,9 @@ def ghost_apply(st, kind, nv, field, maxlevs, ng=2, nroots=(2, 2), periodic=Fals
     return a, no.value, ns.value
 
 
-def admesh(st, grad, maxlevs, ng=2, nroots=(2, 2), periodic=False, cap=100000):
+def admesh(st, grad, maxlevs, ng=2, nroots=(2, 2), periodic=False, cap=100000, marks=None):
+    """Tree::admesh on the criterion `grad`, or Tree::admesh_marked on
+    marks = (iref, icoarse) when grad is None."""
     na = ctypes.c_int(st["lastActive"])
     nbl = ctypes.c_int(st["nbleafs"])
     lp = np.zeros((cap, 8), np.int32)
@@ -56,11 +58,17 @@ def admesh(st, grad, maxlevs, ng=2, nroots=(2, 2), periodic=False, cap=100000):
     lf = np.zeros(cap, np.uint8)
     n0 = st["lastActive"]
     lp[:n0], ic[:n0], lf[:n0] = st["lp"], st["icoord"], st["leafs"]
-    g = np.ascontiguousarray(grad, np.float64)
+    g = None if grad is None else np.ascontiguousarray(grad, np.float64)
+    mr = mc = None
+    if marks is not None:
+        mr = np.ascontiguousarray(marks[0], np.uint8)
+        mc = np.ascontiguousarray(marks[1], np.uint8)
+        assert mr.size >= n0 and mc.size >= n0
     nr, nc = ctypes.c_int(), ctypes.c_int()
     rc = lib().tree_shim_admesh(ctypes.byref(na), lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, ctypes.byref(nbl),
-                                maxlevs, nroots[0], nroots[1], int(periodic), ng, g.ctypes.data, cap,
-                                ctypes.byref(nr), ctypes.byref(nc))
+                                maxlevs, nroots[0], nroots[1], int(periodic), ng,
+                                None if g is None else g.ctypes.data, cap, ctypes.byref(nr), ctypes.byref(nc),
+                                None if mr is None else mr.ctypes.data, None if mc is None else mc.ctypes.data)
     assert rc == 0, rc
     n = na.value
     return dict(lastActive=n, nbleafs=nbl.value, lp=lp[:n], icoord=ic[:n], leafs=lf[:n].astype(bool)), nr.value, nc.value

@@ -165,3 +165,33 @@ def test_set_tree_continues_a_run_bit_for_bit(gpu):
     assert sim.info()["steps"] == 35
     with pytest.raises(gpu.AmrError):   # amr_set_tree takes the place of amr_init
         sim.set_tree(o.get("lp"), o.get("icoord"), o.get("leafs"), inf["nbleafs"], 0.0, 0.0, 0.0, 0)
+
+
+@pytest.mark.gpu
+def test_admesh_marked_matches_oracle(gpu):
+    """amr_admesh_marked with arbitrary marks (the caller choosing the blocks
+    to prolong and restrict) gives the oracle's tree and fields bit for bit
+    after each remesh, and the run continues bit-identical."""
+    kw = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4)
+    sim = gpu.Simulation(**to_gpu_cfg(kw)).init()
+    o = P.Oracle(**kw).init()
+    rng = np.random.default_rng(3)
+    changed = 0
+    for k in range(4):
+        sim.run(5)
+        o.run(5 * (k + 1))
+        n = o.info()["lastActive"]
+        leaves = o.get("leafs").copy()
+        iref, ico = rng.random(n) < 0.1, rng.random(n) < 0.7
+        sim.admesh_marked(iref, ico)
+        o.admesh_marked(iref, ico)
+        a, b = sim.state(), o.state()
+        changed += int(a["lastActive"] != n or not np.array_equal(a["leafs"][:n], leaves))
+        assert P.compare_states(a, b, 2)[0], k
+        assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["Bi"], b["Bi"]), k
+    assert changed >= 3
+    sim.run(10)
+    o.run(30)
+    a, b = sim.state(), o.state()
+    assert P.compare_states(a, b, 2)[0]
+    assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["Bi"], b["Bi"]) and a["t"] == b["t"]

@@ -58,6 +58,125 @@ def test_admesh_matches_oracle(ic, flux, L, steps):
     assert changes > 0
 
 
+def _leaf_rects(st, L):
+    """Leaves as [level, x0, y0, size] in cells of the finest level."""
+    lf = np.flatnonzero(st["leafs"])
+    lev = st["lp"][lf, 0]
+    scale = 2 ** (L - 1 - lev)
+    return lev, st["icoord"][lf, 0] * scale, st["icoord"][lf, 1] * scale, 16 * scale
+
+
+def _max_level_jump(st, L):
+    """Largest level difference between two leaves sharing an edge."""
+    lev, x0, y0, sz = _leaf_rects(st, L)
+    x1, y1 = x0 + sz, y0 + sz
+    ov_y = (np.minimum(y1[:, None], y1[None]) - np.maximum(y0[:, None], y0[None])) > 0
+    ov_x = (np.minimum(x1[:, None], x1[None]) - np.maximum(x0[:, None], x0[None])) > 0
+    touch = ((x1[:, None] == x0[None]) & ov_y) | ((y1[:, None] == y0[None]) & ov_x)
+    return int(np.abs(lev[:, None] - lev[None])[touch].max())
+
+
+def test_admesh_marked_with_criteria_marks_is_admesh():
+    """Tree::admesh_marked given criteria.cpp's flags gives Tree::admesh's
+    tree, step after step of a rotor run."""
+    L = 5
+    o = P.Oracle(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=L).init()
+    o.set_remesh(False)
+    changes = 0
+    for _ in range(30):
+        o.step()
+        st = o.state()
+        grad = P.criteria_grad(o.get("W"))
+        marks = P.criteria_flags(grad, st["leafs"], st["lp"][:, 0], L)
+        a, nr, nc = admesh(st, grad, L)
+        b, mr, mc = admesh(st, None, L, marks=marks)
+        assert (nr, nc) == (mr, mc)
+        for k in ("lastActive", "nbleafs"):
+            assert a[k] == b[k]
+        for k in ("leafs", "lp", "icoord"):
+            assert np.array_equal(a[k], b[k])
+        o.admesh()
+        changes += nr + nc
+    assert changes > 0
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_admesh_marked_random_marks_keep_the_tree_balanced(seed):
+    """Arbitrary marks: the neighbour rules keep leaves that share an edge
+    within one level; refining adds three leaves, coarsening removes three,
+    marks on the finest level or on non-leaves change nothing, and coarsening
+    needs all four siblings marked."""
+    L = 5
+    o = P.Oracle(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=L).init()
+    st = o.state()
+    rng = np.random.default_rng(seed)
+    total = np.zeros(2, int)
+    for it in range(14):
+        n = st["lastActive"]
+        iref = rng.random(n) < (0.08 if it < 9 else 0.0)   # grow, then mostly coarsen
+        ico = rng.random(n) < (0.6 if it < 9 else 0.95)
+        got, nr, nc = admesh(st, None, L, marks=(iref, ico))
+        total += (nr, nc)
+        assert got["leafs"].sum() == st["leafs"].sum() + 3 * nr - 3 * nc
+        assert got["nbleafs"] == st["nbleafs"] + 4 * nr - 3 * nc
+        assert _max_level_jump(got, L) <= 1
+        # every coarsened dad had four leaf sons marked for coarsening (a
+        # block that turns leaf because its father was refined, son-ID
+        # reuse, is not a coarsened dad)
+        m = got["lastActive"]
+        for d in np.flatnonzero(got["leafs"][:n] & ~st["leafs"][:n]):
+            father = st["lp"][d, 1]
+            if father >= 0 and st["leafs"][father]:
+                continue
+            s0 = st["lp"][d, 2]
+            sons = [s0, st["lp"][s0, 5], st["lp"][s0, 7], st["lp"][st["lp"][s0, 7], 5]]
+            assert all(st["leafs"][q] and ico[q] and not iref[q] for q in sons)
+        assert m >= n
+        st = got
+    assert total[0] > 20 and total[1] > 20, total
+    # marks on the finest level (refine) and on non-leaves change nothing
+    n = st["lastActive"]
+    fine = st["leafs"] & (st["lp"][:, 0] == L - 1)
+    same, nr, nc = admesh(st, None, L, marks=(fine | ~st["leafs"], ~st["leafs"]))
+    assert (nr, nc) == (0, 0)
+    assert np.array_equal(same["lp"], st["lp"]) and same["lastActive"] == n
+
+
+def test_admesh_marked_matches_oracle_on_random_marks():
+    """The product's Tree::admesh_marked and the oracle's marked admesh give
+    the same tree for the same arbitrary marks; the oracle's marked admesh
+    with criteria.cpp's flags is its own admesh (tree and fields)."""
+    L = 5
+    o = P.Oracle(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=L).init()
+    o.set_remesh(False)
+    rng = np.random.default_rng(7)
+    for it in range(10):
+        o.step()
+        st = o.state()
+        n = st["lastActive"]
+        iref, ico = rng.random(n) < 0.06, rng.random(n) < 0.7
+        got, _, _ = admesh(st, None, L, marks=(iref, ico))
+        o.admesh_marked(iref, ico)
+        ref = o.state()
+        assert got["lastActive"] == ref["lastActive"] and got["nbleafs"] == ref["nbleafs"]
+        for k in ("leafs", "lp", "icoord"):
+            assert np.array_equal(got[k], ref[k]), (it, k)
+    a = P.Oracle(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=L).init()
+    b = P.Oracle(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=L).init()
+    for x in (a, b):
+        x.set_remesh(False)
+        for _ in range(6):
+            x.step()
+    st = a.state()
+    marks = P.criteria_flags(P.criteria_grad(a.get("W")), st["leafs"], st["lp"][:, 0], L)
+    a.admesh()
+    b.admesh_marked(*marks)
+    sa, sb = a.state(), b.state()
+    assert sa["lastActive"] > st["lastActive"]
+    for k in ("leafs", "lp", "icoord", "U", "Bi"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
 @pytest.mark.parametrize("threads", [1, 2, 8])
 def test_host_pool_parallel_loops(threads):
     """The engine's persistent host threads (remesh, compile and layout loops
