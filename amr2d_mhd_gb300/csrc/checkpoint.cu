@@ -66,9 +66,17 @@ int Engine::checkpoint_save(const char *path) {
 }
 
 // Restores a checkpoint into a handle created with the same configurations
-// and not yet initialised; the next amr_step continues bit for bit.
+// and not yet initialised; the next amr_step continues bit for bit.  A load
+// that fails leaves every instance with a fresh tree, as amr_create made it.
 int Engine::checkpoint_load(const char *path) {
   if (initialised_) return fail(AMR_E_STATE, "checkpoints load into a handle before amr_init");
+  const int rc = checkpoint_read(path);
+  if (rc != AMR_OK)
+    for (Instance &in : inst_) in.tree = Tree(in.tree.shape());
+  return rc;
+}
+
+int Engine::checkpoint_read(const char *path) {
   if (!path) return fail(AMR_E_ARG, "no path");
   std::ifstream f(path, std::ios::binary);
   if (!f) return fail(AMR_E_ARG, std::string("cannot read ") + path);
@@ -98,6 +106,8 @@ int Engine::checkpoint_load(const char *path) {
         !get(f, t.icoord.data(), static_cast<size_t>(t.lastActive)) || !get(f, t.leafs.data(), mb) ||
         !get(f, t.iref.data(), mb) || !get(f, t.icoarse.data(), mb))
       return fail(AMR_E_ARG, "truncated checkpoint");
+    std::string err;
+    if (!t.check(err)) return fail(AMR_E_ARG, "corrupt checkpoint: " + err);
     in.t = td[0];
     in.dt = td[1];
     in.dtn = td[2];

@@ -140,6 +140,7 @@ class Engine {
   int admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad,
                  const AdmeshMarks *marks = nullptr);
   int xfer(Instance &in, int field, double *host, bool to_device);
+  int checkpoint_read(const char *path);   // checkpoint_load's body
   void *field_ptr(int field) const;
   int field_nv(int field) const;
   bool field_f32(int field) const;

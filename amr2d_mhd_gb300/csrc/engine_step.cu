@@ -419,21 +419,23 @@ int Engine::api_set_tree(int q, int32_t na, int32_t nbl, const int32_t *lp, cons
   if (q < 0 || q >= static_cast<int>(inst_.size()) || !lp || !icoord || !leafs)
     return fail(AMR_E_ARG, "bad instance or pointer");
   Instance &in = inst_[q];
-  Tree &tr = in.tree;
-  if (na < 1 || na > tr.maxblocks()) return fail(AMR_E_MAXBLOCKS, "last_active outside [1, maxblocks]");
-  for (int b = 0; b < tr.maxblocks(); b++) {
-    tr.leafs[b] = b < na ? (leafs[b] ? 1 : 0) : 0;
-    tr.iref[b] = 0;
-    tr.icoarse[b] = 0;
-  }
+  if (na < 1 || na > in.tree.maxblocks()) return fail(AMR_E_MAXBLOCKS, "last_active outside [1, maxblocks]");
+  // built in a fresh tree (IDs from na on as a new tree has them) and checked
+  // before it replaces the instance's: its IDs index slots, ghost programs
+  // and refine / coarsen operations
+  Tree tr(in.tree.shape());
   for (int b = 0; b < na; b++) {
     for (int k = 0; k < 8; k++) tr.lp[b][k] = lp[8 * b + k];
     tr.icoord[b] = {icoord[2 * b], icoord[2 * b + 1]};
+    tr.leafs[b] = leafs[b] ? 1 : 0;
     if (tr.lp[b][0] < 0 || tr.lp[b][0] >= in.cfg.maxlevs) return fail(AMR_E_CONFIG, "block level outside maxlevs");
   }
   tr.lastActive = na;
+  std::string err;
+  if (!tr.check(err)) return fail(AMR_E_ARG, "amr_set_tree: " + err);
   tr.nbleafs = nbl;
-  tr.version++;
+  tr.version = in.tree.version + 1;
+  in.tree = std::move(tr);
   in.t = t;
   in.dt = dt;
   in.dtn = dtn;

@@ -49,6 +49,76 @@ void Tree::basegrid() {
   version++;
 }
 
+bool Tree::check(std::string &err) const {
+  const int na = lastActive, nroots = shape_.nrx * shape_.nry;
+  auto bad = [&](int b, const char *what) {
+    err = "block " + std::to_string(b) + ": " + what;
+    return false;
+  };
+  if (na < nroots || na > maxblocks_) {
+    err = "last_active outside [nroots, maxblocks]";
+    return false;
+  }
+  // index ranges (basegrid.cpp: roots are IDs 0..nroots-1 with father 0;
+  // admesh.cpp:33-41: sons come as four consecutive IDs after the roots)
+  for (int b = 0; b < na; b++) {
+    const auto &l = lp[b];
+    if (l[0] < 0 || l[0] >= shape_.maxlevs) return bad(b, "level outside [0, maxlevs)");
+    if ((b < nroots) != (l[0] == 0)) return bad(b, "the roots are the first nrx * nry IDs, at level 0");
+    if (l[1] < 0 || l[1] >= na) return bad(b, "father ID out of range");
+    if (l[2] != 0 && (l[2] < nroots || l[2] + 3 >= na)) return bad(b, "first-son ID out of range");
+    if (l[3] < 0 || l[3] > 3) return bad(b, "sibling number outside 0..3");
+    for (int c = 4; c < 8; c++)
+      if (l[c] < -1 || l[c] >= na) return bad(b, "neighbour ID out of range");
+  }
+  // father / son relations and the links inside each group of four sons
+  // (updatelpup.cpp), which later remeshes follow
+  for (int b = 0; b < na; b++) {
+    const auto &l = lp[b];
+    if (l[0] > 0) {
+      const int f = l[1];
+      if (lp[f][0] != l[0] - 1 || lp[f][2] + l[3] != b) return bad(b, "not the son its father lists");
+      if (leafs[b] && leafs[f]) return bad(b, "a leaf whose father is a leaf");
+    }
+    if (l[2] != 0) {
+      const int s = l[2];
+      for (int q = 0; q < 4; q++)
+        if (lp[s + q][0] != l[0] + 1 || lp[s + q][1] != b || lp[s + q][3] != q)
+          return bad(b, "its sons do not list it as their father");
+      if (lp[s][5] != s + 1 || lp[s][7] != s + 2 || lp[s + 1][4] != s || lp[s + 1][7] != s + 3 ||
+          lp[s + 2][5] != s + 3 || lp[s + 2][6] != s || lp[s + 3][4] != s + 2 || lp[s + 3][6] != s + 1)
+        return bad(b, "broken links between its sons");
+    }
+  }
+  // the active tree (leaves and their ancestors): neighbours are active, on
+  // the same level or, for a leaf, a leaf one level coarser; a leaf's
+  // same-level neighbour that is refined has leaves along the shared edge
+  std::vector<uint8_t> active(static_cast<size_t>(na), 0);
+  for (int b = 0; b < na; b++)
+    if (leafs[b])
+      for (int a = b, depth = 0; depth < shape_.maxlevs && !active[a]; depth++) {
+        active[a] = 1;
+        if (lp[a][0] == 0) break;
+        a = lp[a][1];
+      }
+  static constexpr int kFacing[4][2] = {{1, 3}, {0, 2}, {2, 3}, {0, 1}};  // sons of the L, R, D, U neighbour
+  for (int b = 0; b < na; b++) {
+    if (!active[b]) continue;
+    if (!leafs[b] && lp[b][2] == 0) return bad(b, "a refined block without sons");
+    for (int side = 0; side < 4; side++) {
+      const int n = lp[b][kNbCol[side]];
+      if (n == -1) continue;
+      if (!active[n]) return bad(b, "a neighbour outside the active tree");
+      if (lp[n][0] == lp[b][0] - 1 && leafs[b] && leafs[n]) continue;
+      if (lp[n][0] != lp[b][0]) return bad(b, "a neighbour more than one level coarser, or finer");
+      if (leafs[b] && !leafs[n])
+        for (int k = 0; k < 2; k++)
+          if (!leafs[lp[n][2] + kFacing[side][k]]) return bad(b, "neighbours two levels apart");
+    }
+  }
+  return true;
+}
+
 std::vector<int> Tree::leaves() const {
   std::vector<int> out;
   for (int nb = 0; nb < lastActive; nb++)

@@ -44,6 +44,11 @@ class Tree {
   // locate_bounds.cpp:35-208
   void locate_bounds(std::vector<Bound> &out) const;
   std::vector<int> leaves() const;
+  // The structure every tree admesh builds: IDs in range, father / son and
+  // sibling links consistent, the active tree 2:1 balanced.  A tree handed
+  // in from outside must pass before its IDs reach ghost programs or
+  // refine / coarsen operations.  Returns false with `err` otherwise.
+  bool check(std::string &err) const;
 
   // admesh.cpp:17-102.  grad[nb] is, for each leaf, the largest relative
   // jump of criteria.cpp:11-29 over the block (only leaves are read).

@@ -191,7 +191,10 @@ int amr_admesh_marked(amr_handle *h, const uint8_t *iref, const uint8_t *icoarse
  * and dt_next as amr_get_info reports them, and the step count.  Call it for
  * every instance instead of amr_init; then amr_upload U and Bi (and ff / gg,
  * whose low ghost face the next residual reads as the last stage left it,
- * main.cpp:150, for a bit-identical continuation) before stepping. */
+ * main.cpp:150, for a bit-identical continuation) before stepping.  The tree
+ * must have the structure admesh builds (IDs in range, father / son and
+ * sibling links consistent, leaves sharing an edge at most one level apart);
+ * anything else returns AMR_E_ARG and leaves the instance as it was. */
 int amr_set_tree(amr_handle *h, int32_t instance, int32_t last_active, int32_t nb_leafs, const int32_t *lp,
                  const int32_t *icoord, const uint8_t *leafs, double t, double dt, double dt_next, int64_t steps);
 

@@ -2,6 +2,7 @@
 // (amr2d_mhd_gb300/csrc/ghost_compile.cpp) on a given quadtree and applies the
 // compiled gathers on the CPU the way k_ghost_snap / k_ghost_apply do, so the
 // compiler can be checked against the oracle's sequential fill without a GPU.
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -107,6 +108,25 @@ extern "C" int tree_shim_admesh(int *last_active, int *lp, int *icoord, unsigned
   *n_ref = static_cast<int>(plan.refine.size());
   *n_crs = static_cast<int>(plan.coarsen.size());
   return 0;
+}
+
+// Tree::check on a given tree: 0 when it passes, 1 (message in err) when not
+extern "C" int tree_shim_check(int last_active, const int *lp, const int *icoord, const unsigned char *leafs,
+                               int maxlevs, int nrx, int nry, int periodic, int ng, char *err, int errlen) {
+  using namespace amr;
+  TreeShape s{16, 16, ng, maxlevs, nrx, nry, periodic != 0};
+  Tree t(s);
+  if (last_active > t.maxblocks()) return 2;
+  t.lastActive = last_active;
+  for (int b = 0; b < last_active; b++) {
+    for (int q = 0; q < 8; q++) t.lp[b][q] = lp[8 * b + q];
+    t.icoord[b] = {icoord[2 * b], icoord[2 * b + 1]};
+    t.leafs[b] = leafs[b];
+  }
+  std::string e;
+  if (t.check(e)) return 0;
+  std::snprintf(err, static_cast<size_t>(errlen), "%s", e.c_str());
+  return 1;
 }
 
 // The engine's host thread pool: `rounds` parallel loops of n items on up to

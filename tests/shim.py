@@ -31,6 +31,8 @@ def lib():
         L.tree_shim_admesh.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int] + \
             [ctypes.c_void_p] * 4
         L.host_pool_shim.argtypes = [ctypes.c_int] * 3
+        L.tree_shim_check.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 5 + \
+            [ctypes.c_char_p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -72,6 +74,18 @@ def admesh(st, grad, maxlevs, ng=2, nroots=(2, 2), periodic=False, cap=100000, m
     assert rc == 0, rc
     n = na.value
     return dict(lastActive=n, nbleafs=nbl.value, lp=lp[:n], icoord=ic[:n], leafs=lf[:n].astype(bool)), nr.value, nc.value
+
+
+def tree_check(st, maxlevs, ng=2, nroots=(2, 2), periodic=False):
+    """Tree::check: None when the tree passes, else the message."""
+    lp = np.ascontiguousarray(st["lp"], np.int32)
+    ic = np.ascontiguousarray(st["icoord"], np.int32)
+    lf = np.ascontiguousarray(np.asarray(st["leafs"]).astype(np.uint8))
+    buf = ctypes.create_string_buffer(256)
+    rc = lib().tree_shim_check(st["lastActive"], lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, maxlevs,
+                               nroots[0], nroots[1], int(periodic), ng, buf, 256)
+    assert rc in (0, 1), rc
+    return None if rc == 0 else buf.value.decode()
 
 
 def host_pool(rounds, n, threads):

@@ -195,3 +195,30 @@ def test_admesh_marked_matches_oracle(gpu):
     a, b = sim.state(), o.state()
     assert P.compare_states(a, b, 2)[0]
     assert np.array_equal(a["U"], b["U"]) and np.array_equal(a["Bi"], b["Bi"]) and a["t"] == b["t"]
+
+
+@pytest.mark.gpu
+def test_set_tree_refuses_a_broken_tree(gpu):
+    """A handed tree whose neighbour link leaves the ID range is refused on
+    the host (AMR_E_ARG) before any ID reaches the device; the instance then
+    takes the intact tree."""
+    kw = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4)
+    o = P.Oracle(**kw).init()
+    o.run(10)
+    inf = o.info()
+    lp = o.get("lp").copy()
+    leaf = int(np.flatnonzero(o.get("leafs"))[-1])
+    lp[leaf, 5] = inf["lastActive"] + 100
+    sim = gpu.Simulation(**to_gpu_cfg(kw))
+    with pytest.raises(gpu.AmrError) as e:
+        sim.set_tree(lp, o.get("icoord"), o.get("leafs"), inf["nbleafs"], inf["t"], inf["dt"], inf["dt_next"],
+                     inf["count"])
+    assert e.value.code == -12
+    sim.set_tree(o.get("lp"), o.get("icoord"), o.get("leafs"), inf["nbleafs"], inf["t"], inf["dt"],
+                 inf["dt_next"], inf["count"])
+    for f in ("U", "Bi", "ff", "gg"):
+        sim.upload(f, o.get(f))
+    o.run(12)
+    sim.run(2)
+    a, b = sim.state(), o.state()
+    assert P.compare_states(a, b, 2)[0] and np.array_equal(a["U"], b["U"])

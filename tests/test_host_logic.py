@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as P
-from shim import admesh, ghost_apply, host_pool
+from shim import admesh, ghost_apply, host_pool, tree_check
 
 GHOST_CASES = [("BWx", "MC", 4, 2, 3), ("rotor", "MC", 5, 2, 30), ("BWx", "WENO5", 3, 4, 10),
                ("rotor", "WENO5", 3, 4, 25)]
@@ -117,6 +117,7 @@ def test_admesh_marked_random_marks_keep_the_tree_balanced(seed):
         ico = rng.random(n) < (0.6 if it < 9 else 0.95)
         got, nr, nc = admesh(st, None, L, marks=(iref, ico))
         total += (nr, nc)
+        assert tree_check(got, L) is None, (it, tree_check(got, L))
         assert got["leafs"].sum() == st["leafs"].sum() + 3 * nr - 3 * nc
         assert got["nbleafs"] == st["nbleafs"] + 4 * nr - 3 * nc
         assert _max_level_jump(got, L) <= 1
@@ -175,6 +176,84 @@ def test_admesh_marked_matches_oracle_on_random_marks():
     assert sa["lastActive"] > st["lastActive"]
     for k in ("leafs", "lp", "icoord", "U", "Bi"):
         assert np.array_equal(sa[k], sb[k]), k
+
+
+TREE_RUNS = [(dict(ic="rotor", flux="HLLD", maxlevs=4), 60, (2, 2), False),
+             (dict(ic="rotor", flux="RUSA", maxlevs=5), 120, (2, 2), False),
+             (dict(ic="BWx", flux="RUSA", maxlevs=4), 120, (2, 2), False),
+             (dict(ic="OT", flux="RUSA", maxlevs=3, nroots=(4, 4), periodic=True, geom_ref=False,
+                   lenx=2 * np.pi, leny=2 * np.pi), 40, (4, 4), True)]
+
+
+@pytest.mark.parametrize("kw,steps,nroots,periodic", TREE_RUNS)
+def test_tree_check_accepts_every_tree_admesh_builds(kw, steps, nroots, periodic):
+    """Tree::check (run on trees handed in by amr_set_tree) passes every
+    tree of these runs, step by step, refinement and coarsening included."""
+    o = P.Oracle(limiter="MC", cfl=0.4, **kw).init()
+    L = kw["maxlevs"]
+    seen = set()
+    for k in range(steps + 1):
+        st = o.state()
+        assert tree_check(st, L, 2, nroots, periodic) is None, (k, tree_check(st, L, 2, nroots, periodic))
+        seen.add(st["lastActive"])
+        o.step()
+    assert len(seen) > 1
+
+
+def test_tree_check_accepts_blast_and_kh_trees():
+    """The seeded blast instances (uneven levels, as checkpointed in a batch)
+    and the single-level periodic KH problem pass Tree::check step by step."""
+    import amr2d_mhd_gb300 as amr
+    cfgs = [amr.blast_config(3, i) for i in range(3)] + [amr.kh_config(42)]
+    for c in cfgs:
+        c.maxlevs = min(c.maxlevs, 4)
+        kw = dict(ic=c.ic.decode(), limiter=c.limiter.decode(), flux=c.flux.decode(), cfl=c.cfl,
+                  maxlevs=c.maxlevs, nghosts=c.nghosts, nroots=(c.nroots_x, c.nroots_y),
+                  periodic=bool(c.periodic), geom_ref=c.geometry == 0, gamma=c.gamma, tend=c.t_end,
+                  ic_param=list(c.ic_param), nthreads=4, dt_fixed=c.dt_fixed)
+        o = P.Oracle(**kw).init()
+        for k in range(26):
+            msg = tree_check(o.state(), c.maxlevs, c.nghosts, (c.nroots_x, c.nroots_y), bool(c.periodic))
+            assert msg is None, (c.ic, k, msg)
+            o.step()
+
+
+def test_tree_check_rejects_broken_trees():
+    """IDs out of range, broken father / son or sibling links, neighbours
+    outside the active tree and unbalanced neighbours are all refused."""
+    L = 5
+    o = P.Oracle(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=L).init()
+    o.run(40)
+    st = o.state()
+    assert tree_check(st, L) is None
+    lp, lf = st["lp"], st["leafs"]
+    n = st["lastActive"]
+    leaf = int(np.flatnonzero(lf & (lp[:, 0] >= 2))[0])
+    dad = int(np.flatnonzero(~lf[:n] & (lp[:n, 2] != 0) & (lp[:n, 0] >= 1))[0])
+
+    def broken(edit):
+        bad = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
+        edit(bad)
+        return tree_check(bad, L)
+
+    def setlp(b, c, v):
+        return lambda t: t["lp"].__setitem__((b, c), v)
+
+    assert "neighbour ID" in broken(setlp(leaf, 5, n))
+    assert "neighbour ID" in broken(setlp(leaf, 4, -2))
+    assert "father ID" in broken(setlp(leaf, 1, n + 7))
+    assert "first-son ID" in broken(setlp(dad, 2, n - 2))
+    assert "level" in broken(setlp(leaf, 0, L))
+    assert "sibling number" in broken(setlp(leaf, 3, 4))
+    assert "father" in broken(setlp(leaf, 3, (lp[leaf, 3] + 1) % 4))
+    s0 = lp[dad, 2]
+    assert "links between its sons" in broken(setlp(s0, 5, s0 + 2))
+    assert "roots" in broken(setlp(0, 0, 1))
+    assert "a leaf whose father is a leaf" in broken(lambda t: t["leafs"].__setitem__(lp[leaf, 1], True))
+    # a neighbour pointer to a block two levels coarser
+    coarse = int(np.flatnonzero(lp[:n, 0] == lp[leaf, 0] - 2)[0])
+    assert broken(setlp(leaf, 4, coarse)) is not None
+    assert "last_active" in broken(lambda t: t.__setitem__("lastActive", 3))
 
 
 @pytest.mark.parametrize("threads", [1, 2, 8])
