@@ -26,6 +26,32 @@ def test_ghost_program_matches_sequential_fill(ic, lim, L, ng, steps):
         assert np.array_equal(ref, got), (kind, nv, int((ref != got).sum()))
 
 
+@pytest.mark.parametrize("seed,periodic", [(11, False), (12, False), (13, True)])
+def test_ghost_program_on_random_mark_trees(seed, periodic):
+    """The compiled ghost fills equal the oracle's sequential fills on trees
+    remeshed by random marks (coarse / fine layouts no run of the
+    reference's criterion produces), every fill kind."""
+    kw = dict(ic="rotor", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=5)
+    nroots = (2, 2)
+    if periodic:
+        kw = dict(ic="OT", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=4, nroots=(3, 3), periodic=True,
+                  geom_ref=False, lenx=2 * np.pi, leny=2 * np.pi)
+        nroots = (3, 3)
+    L = kw["maxlevs"]
+    o = P.Oracle(**kw).init()
+    o.set_remesh(False)
+    rng = np.random.default_rng(seed)
+    for it in range(8):
+        n = o.info()["lastActive"]
+        o.admesh_marked(rng.random(n) < 0.15, rng.random(n) < 0.5)
+        st = o.state()
+        assert tree_check(st, L, 2, nroots, periodic) is None
+        for kind, nv in [(0, 8), (1, 2), (2, 1)]:
+            f = rng.standard_normal((st["lastActive"], nv, 20, 20))
+            got, _, _ = ghost_apply(st, kind, nv, f, L, 2, nroots, periodic)
+            assert np.array_equal(o.fill(f, kind), got), (it, kind)
+
+
 def test_ghost_program_periodic_16_roots():
     o = P.Oracle(ic="OT", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=3, nroots=(4, 4), periodic=True,
                  geom_ref=False, lenx=2 * np.pi, leny=2 * np.pi).init()
