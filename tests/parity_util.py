@@ -36,3 +36,12 @@ def to_gpu_cfg(c):
                 t_end=c.get("tend", 0.0), ic_param=c.get("ic_param"),
                 precision=c.get("precision", "fp64"), lenx=c.get("lenx", 1.0), leny=c.get("leny", 1.0),
                 ct_type=c.get("ct_type", 1), diffusion=c.get("diffusion", False))
+
+
+def oracle_kw(c, nthreads=8):
+    """Oracle keyword arguments for a library configuration (amr_config)."""
+    return dict(ic=c.ic.decode(), limiter=c.limiter.decode(), flux=c.flux.decode(), cfl=c.cfl,
+                maxlevs=c.maxlevs, nghosts=c.nghosts, nroots=(c.nroots_x, c.nroots_y),
+                periodic=bool(c.periodic), geom_ref=c.geometry == 0, gamma=c.gamma, tend=c.t_end,
+                ic_param=list(c.ic_param), nthreads=nthreads, dt_fixed=c.dt_fixed, ct_type=c.ct_type or 1,
+                diffusion=bool(c.diffusion))

@@ -5,14 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as P
-
-
-def oracle_kw(c, nthreads=8):
-    return dict(ic=c.ic.decode(), limiter=c.limiter.decode(), flux=c.flux.decode(), cfl=c.cfl,
-                maxlevs=c.maxlevs, nghosts=c.nghosts, nroots=(c.nroots_x, c.nroots_y),
-                periodic=bool(c.periodic), geom_ref=c.geometry == 0, gamma=c.gamma, tend=c.t_end,
-                ic_param=list(c.ic_param), nthreads=nthreads, dt_fixed=c.dt_fixed, ct_type=c.ct_type or 1,
-                diffusion=bool(c.diffusion))
+from parity_util import oracle_kw
 
 
 def blast_batch(gpu, seed, n, cap_levels, precision="fp64", t_end=None):

@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as P
+from parity_util import oracle_kw
 from shim import admesh, ghost_apply, host_pool, tree_check
 
 GHOST_CASES = [("BWx", "MC", 4, 2, 3), ("rotor", "MC", 5, 2, 30), ("BWx", "WENO5", 3, 4, 10),
@@ -233,11 +234,7 @@ def test_tree_check_accepts_blast_and_kh_trees():
     cfgs = [amr.blast_config(3, i) for i in range(3)] + [amr.kh_config(42)]
     for c in cfgs:
         c.maxlevs = min(c.maxlevs, 4)
-        kw = dict(ic=c.ic.decode(), limiter=c.limiter.decode(), flux=c.flux.decode(), cfl=c.cfl,
-                  maxlevs=c.maxlevs, nghosts=c.nghosts, nroots=(c.nroots_x, c.nroots_y),
-                  periodic=bool(c.periodic), geom_ref=c.geometry == 0, gamma=c.gamma, tend=c.t_end,
-                  ic_param=list(c.ic_param), nthreads=4, dt_fixed=c.dt_fixed)
-        o = P.Oracle(**kw).init()
+        o = P.Oracle(**oracle_kw(c, 4)).init()
         for k in range(26):
             msg = tree_check(o.state(), c.maxlevs, c.nghosts, (c.nroots_x, c.nroots_y), bool(c.periodic))
             assert msg is None, (c.ic, k, msg)

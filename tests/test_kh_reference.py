@@ -7,7 +7,7 @@ import torch
 import amr2d_mhd_gb300 as amr
 import kh_reference as K
 from oracle import pyoracle as P
-from test_gpu_batch import oracle_kw
+from parity_util import oracle_kw
 
 
 def test_torch_kh_step_matches_oracle():
