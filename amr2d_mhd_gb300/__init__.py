@@ -29,7 +29,7 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "a
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_step_begin", "amr_step_end", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_set_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_criteria_flags", "amr_admesh_marked", "amr_autotune", "amr_save4py",
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_criteria_flags", "amr_admesh_marked", "amr_set_remesh", "amr_autotune", "amr_save4py",
            "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
            "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
 
@@ -113,6 +113,7 @@ def load(build_if_missing: bool = True):
         "amr_download": (ctypes.c_int, [vp, i32, i32, dp, i64]),
         "amr_upload": (ctypes.c_int, [vp, i32, i32, dp, i64]),
         "amr_profile_enable": (ctypes.c_int, [vp, i32]),
+        "amr_set_remesh": (ctypes.c_int, [vp, i32]),
         "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
         "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
         "amr_criteria": (ctypes.c_int, [vp, dp, i32]),
@@ -149,7 +150,12 @@ def make_config(ic="rotor", limiter="MC", flux="RUSA", cfl=0.5, maxlevs=5, nghos
             raise AmrError(rc, "cannot read %s" % input_txt)
     else:
         c.nx, c.ny, c.lenx, c.leny, c.cfl = nx, ny, lenx, leny, cfl
-        c.ic, c.limiter, c.flux = ic.encode(), limiter.encode(), flux.encode()
+        # zero-padded, as the C side writes names (configurations are
+        # compared byte for byte, e.g. by amr_checkpoint_load); a ctypes
+        # char-array field assignment stops at the first NUL
+        for field, name in (("ic", ic), ("limiter", limiter), ("flux", flux)):
+            ctypes.memset(ctypes.addressof(c) + getattr(Config, field).offset, 0, 16)
+            setattr(c, field, name.encode()[:15])
     c.maxlevs, c.nghosts = maxlevs, nghosts
     c.nroots_x, c.nroots_y = nroots
     c.periodic, c.geometry = int(periodic), int(geometry)
@@ -273,6 +279,11 @@ class Simulation:
 
     def admesh(self):
         self._ck(load().amr_admesh(self.h))
+
+    def set_remesh(self, on):
+        """on=False: step() stops before main.cpp's closing admesh; call
+        admesh() after acting on the state (amr_set_remesh)."""
+        self._ck(load().amr_set_remesh(self.h, int(bool(on))))
 
     # state exchange
     def tree(self, instance=0):

@@ -1,4 +1,5 @@
-"""Build of the sm_103a library libamr2d_mhd.so (in-tree, amr2d_mhd_gb300/_build/).
+"""Build of the sm_103a library libamr2d_mhd.so and of the host program
+amr2d_mhd that drives it (in-tree, amr2d_mhd_gb300/_build/).
 
 Every translation unit compiles in parallel with nvcc for sm_103a only.  Every
 translation unit but the FP32 stage kernels (stage_f32_*.cu) is compiled with
@@ -17,6 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libamr2d_mhd.so")
+HOST = os.path.join(HERE, "host")
+DRIVER = os.path.join(BUILD, "amr2d_mhd")   # the reference program's main() on the library
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -42,14 +45,33 @@ def _flags(src: str):
 
 def _stamp() -> float:
     t = 0.0
-    for f in os.listdir(CSRC):
-        t = max(t, os.path.getmtime(os.path.join(CSRC, f)))
+    for d in (CSRC, HOST):
+        for f in os.listdir(d):
+            t = max(t, os.path.getmtime(os.path.join(d, f)))
     t = max(t, os.path.getmtime(os.path.join(HERE, "..", "include", "amr2d_mhd.h")))
     return max(t, os.path.getmtime(__file__))
 
 
+def build_driver() -> str:
+    """amr2d_mhd, the host program that reads input.txt and drives the
+    library through its C ABI only (linked with an $ORIGIN run path)."""
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
+    src = os.path.join(HOST, "amr2d_main.cpp")
+    tmp = DRIVER + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(HERE, "..", "include"), src, "-L" + BUILD,
+           "-lamr2d_mhd", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _stamp():
+    stamp = _stamp()
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= stamp:
+        if not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < stamp:
+            build_driver()
         return LIB
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
@@ -74,6 +96,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
 
 

@@ -1,7 +1,7 @@
 // Discrete adjoint of the frozen-mesh time step.  The forward step is
 // recomputed from its checkpoint with a tape of the values the transposed
 // kernels need, then the transposed step runs in reverse order of
-// main.cpp:241-315.  No counterpart in the reference.
+// main.cpp:128-202.  No counterpart in the reference.
 #include <cstring>
 
 #include "adjoint_kernels.cuh"
@@ -140,7 +140,7 @@ int Engine::ct2d_taped(int step) {
   return AMR_OK;
 }
 
-// main.cpp:242-315 from the restored checkpoint, keeping the tape
+// main.cpp:129-202 from the restored checkpoint, keeping the tape
 int Engine::adjoint_recompute() {
   const size_t cell = sizeof(double) * 8 * nn_ * used_slots_, face = sizeof(double) * 2 * nn_ * used_slots_;
   const bool split = split_;

@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(128) k_faces_adj(StageAdjArgs a) {
 // Per cell: the primitive-state adjoint gathered from the (up to 8) faces
 // whose reconstruction read the cell, the transpose of U2W
 // (meshblock.cpp:119-145) added to aIn, and the RK combine
-// (main.cpp:260-270 / 292-302) transposed (aIn += s aOut; aOut -> the old
+// (main.cpp:147-157 / 179-189) transposed (aIn += s aOut; aOut -> the old
 // state's adjoint).  Face m+1/2 (m in [LO, HI]) gives cell m-1+q its C[q].
 template <int NG>
 __global__ void __launch_bounds__(256) k_cells_adj(StageAdjArgs a) {

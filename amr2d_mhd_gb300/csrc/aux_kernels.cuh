@@ -133,7 +133,7 @@ struct CtArgs {
 // then the corner EMF weighting the two flux averages by psi, which stays 1/2
 // unless the corner sits at a strong pressure jump (beta = 0.5) in a strongly
 // compressive flow (delta = 0.1).  Two terms of the divergence divide rho*v
-// by itself (:53), as the reference does.  Arithmetic in the storage type S
+// by itself (:52), as the reference does.  Arithmetic in the storage type S
 // (FP64 on the FP64 path, in the reference's order).
 template <int NG, typename S>
 __device__ __forceinline__ void ct_emf_upwind(const CtArgs &a, const LeafTask &t, S *sp, S *sC) {
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(128) k_diffuse(CtArgs a) {
   }
 }
 
-// --------------------------------------------- dt (main.cpp:322-343) and
+// --------------------------------------------- dt (main.cpp:209-230) and
 // refinement criterion (criteria.cpp:6-44) of every leaf: one CTA per leaf,
 // one thread per interior cell, reading the primitive state that k_prim wrote
 // for U (FP64 for the FP64 path; the FP32 path computes the cell values in
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
 #pragma unroll
   for (int k = 0; k < 8; k++) w[k] = W[k * NN + c];
   // wavespeeds (misc.cpp:71-79) for norm 5 and 6; ca and a are the same
-  // values in both calls.  lambda1 takes |rho| (main.cpp:335), lambda2 |u|.
+  // values in both calls.  lambda1 takes |rho| (main.cpp:222), lambda2 |u|.
   const T ca = sqrt((w[5] * w[5] + w[6] * w[6] + w[7] * w[7]) / w[0]);
   const T as = sqrt(g * w[4] / w[0]);
   T cf[2];
@@ -590,7 +590,7 @@ __global__ void k_coarsen(TreeOpArgs a) {
   constexpr int N = G::N, NN = G::NN;
   const TreeOp op = a.ops[blockIdx.x];
   coarsen_field<NG, S, false>(static_cast<S *>(a.U), 8, op.son, op.dad);
-  // coarsen.cpp:310 U2W("coarsen") pressure trap on the dad
+  // coarsen.cpp:151 U2W("coarsen") pressure trap on the dad
   const S *D = static_cast<const S *>(a.U) + static_cast<size_t>(op.dad) * 8 * NN;
   for (int c = threadIdx.x; c < NN; c += blockDim.x) {
     S u[8], w[8];

@@ -82,7 +82,7 @@ void amr_config_default(amr_config *c) {
   c->precision = AMR_FP64;
 }
 
-// main.cpp:156-177
+// main.cpp:43-64
 int amr_config_from_input(const char *path, amr_config *c) {
   if (!path || !c) return AMR_E_ARG;
   std::ifstream f(path);
@@ -197,6 +197,9 @@ int amr_upload(amr_handle *h, int32_t q, int32_t f, const double *s, int64_t n) 
   return guarded(h, [&](amr::Engine &e) { return e.upload(q, f, s, n); });
 }
 
+int amr_set_remesh(amr_handle *h, int32_t on) {
+  return guarded(h, [&](amr::Engine &e) { return e.set_remesh(on != 0); });
+}
 int amr_profile_enable(amr_handle *h, int32_t on) {
   return guarded(h, [&](amr::Engine &e) { return e.profile_enable(on != 0); });
 }

@@ -1,4 +1,4 @@
-// amr_cfl_dt_static: the CFL reduction (main.cpp:322-343) for callers that may
+// amr_cfl_dt_static: the CFL reduction (main.cpp:209-230) for callers that may
 // not allocate device memory.
 //
 // Some hosts cannot call cudaMalloc at the point where they need the time step:
@@ -23,8 +23,8 @@ constexpr int kCflStaticMaxBlocks = 1 << 16;
 // per-block min(dx,dy)/lambda_b of the last call; shared by every call
 static __device__ __align__(256) double g_cfl_scratch[kCflStaticMaxBlocks];
 
-// main.cpp:324-341 for one block of the dense array: lambda1 takes |rho| +
-// c_f,x (W[..][0], main.cpp:335) and lambda2 |u| + c_f,y (:337) over the
+// main.cpp:211-228 for one block of the dense array: lambda1 takes |rho| +
+// c_f,x (W[..][0], main.cpp:222) and lambda2 |u| + c_f,y (:224) over the
 // interior cells
 template <int NG>
 __global__ void __launch_bounds__(256) k_cfl_static_blocks(const double *U, const double *dxdy, double gamma,
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256) k_cfl_static_blocks(const double *U, cons
   }
 }
 
-// lambda = min(1e6, min over blocks) (main.cpp:322,341); a NaN block value
+// lambda = min(1e6, min over blocks) (main.cpp:209,228); a NaN block value
 // makes the result NaN, which the caller's invalid-dt check catches
 __global__ void k_cfl_static_min(const double *scratch, int n, double *out) {
   __shared__ double red[32];

@@ -718,7 +718,7 @@ int Engine::dt_crit(bool want_grad) {
   return AMR_OK;
 }
 
-// main.cpp:242-315: ghost fills, stage 1 with CT, stage 2 with CT
+// main.cpp:129-202: ghost fills, stage 1 with CT, stage 2 with CT
 int Engine::enqueue_stage_sequence() {
   int rc;
   if ((rc = fill({{FILL_CC, AMR_FIELD_U}, {FILL_FC, AMR_FIELD_BI}}))) return rc;

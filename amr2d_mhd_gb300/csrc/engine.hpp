@@ -1,6 +1,6 @@
 // The engine behind the C ABI: a pool of block slots resident on one GPU, the
 // host quadtree of every instance, the compiled ghost fills, and the driver of
-// one time step in the order of main.cpp:241-360.
+// one time step in the order of main.cpp:128-247.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -94,6 +94,11 @@ class Engine {
   int upload(int inst, int field, const double *src, int64_t count);
 
   int profile_enable(bool on);
+  // off: a step ends after the dt reduction, without main.cpp:246's admesh
+  int set_remesh(bool on) {
+    remesh_ = on;
+    return 0;
+  }
   int profile_read(amr_profile *out);
 
   // Times candidate launch schedules (fused or split stage, threads per CTA
@@ -190,6 +195,7 @@ class Engine {
 
   // measurement
   bool prof_on_ = false;
+  bool remesh_ = true;
   amr_profile prof_{};
   std::vector<cudaEvent_t> ev_;     // start/stop pairs of this step's stage launches
   int ev_used_ = 0;

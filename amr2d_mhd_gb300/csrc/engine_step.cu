@@ -137,7 +137,7 @@ int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vec
   return check_device_error();  // also keeps `all` alive until the copy is done
 }
 
-// basegrid + IC2Dtype + W2U + initial admesh (main.cpp:210-229)
+// basegrid + IC2Dtype + W2U + initial admesh (main.cpp:97-116)
 int Engine::init() {
   if (initialised_) return fail(AMR_E_STATE, "amr_init called twice");
   if (poisoned_) return fail(AMR_E_STATE, "engine stopped by an earlier error");
@@ -160,7 +160,7 @@ int Engine::init() {
     if (int rc = xfer(in, AMR_FIELD_U, U.data(), true)) return rc;
     if (int rc = xfer(in, AMR_FIELD_BI, B.data(), true)) return rc;
     in.t = 0.0;
-    in.dt = 0.0;  // dom.dt is read before its first assignment (main.cpp:267 vs :344)
+    in.dt = 0.0;  // dom.dt is read before its first assignment (main.cpp:154 vs :231)
     in.dtn = 0.0;
     if (in.cfg.dt_fixed > 0) in.dt = in.dtn = in.cfg.dt_fixed;
     in.count = 0;
@@ -180,7 +180,7 @@ int Engine::finish_step() {
   const double *hl = h_lambda_.as<double>();
   for (int a : active_) {
     Instance &in = inst_[a];
-    double lambda = 1.E6;  // main.cpp:322, 341
+    double lambda = 1.E6;  // main.cpp:209, 228
     for (int t = in.task_begin; t < in.task_end; t++) {
       const double v = (tasks_[t].dx < tasks_[t].dy ? tasks_[t].dx : tasks_[t].dy) / hl[t];
       lambda = v < lambda ? v : lambda;
@@ -191,15 +191,16 @@ int Engine::finish_step() {
       in.t = in.t + in.cfg.dt_fixed;
       continue;
     }
-    in.t = in.t + in.dtn;  // main.cpp:344-347
+    in.t = in.t + in.dtn;  // main.cpp:231-234
     in.dt = in.dtn;
     in.dtn = in.cfl * lambda;
     if (in.dtn < 0 || std::isnan(in.dtn)) return fail(AMR_E_DT, "invalid dt produced");
   }
+  if (!remesh_) return AMR_OK;
   return admesh_all(active_, nullptr);
 }
 
-// one iteration of main.cpp:241-360 for every instance with t <= t_end
+// one iteration of main.cpp:128-247 for every instance with t <= t_end
 int Engine::step() {
   if (int rc = step_begin()) return rc;
   return step_end();

@@ -1,6 +1,6 @@
 // Fused RK stage of one leaf block: MUSCL2D.cpp:13-121 (cons2prim,
 // reconstruction, CT normal-B override, Riemann fluxes) followed by the
-// residual and RK2ndv1 update of main.cpp:260-270 / 292-302.
+// residual and RK2ndv1 update of main.cpp:147-157 / 179-189.
 //
 // One CTA per leaf block.  Shared memory holds the primitive state of the
 // whole block (with ghosts) and the x / y face fluxes that the residual

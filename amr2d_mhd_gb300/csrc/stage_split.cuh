@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(128, MINB) k_faces_persist(SplitArgs a) {
 }
 
 // residual on [LO, HI]^2 (zero elsewhere) and the RK stage on every cell
-// (main.cpp:260-270 / 292-302)
+// (main.cpp:147-157 / 179-189)
 template <int NG, typename S>
 __global__ void __launch_bounds__(512) k_resid(SplitArgs a) {
   pdl_wait();

@@ -11,7 +11,7 @@ constexpr int kBoxCode[4] = {-1, -2, -3, -4};
 constexpr int kSameCode[4] = {1, 4, 7, 10};
 constexpr int kFineCode[4] = {2, 5, 8, 11};
 // first son of the finer neighbour that touches side s, and the step to the
-// second one (locate_bounds.cpp:268-274, 308-309, 343-345, 379-380)
+// second one (locate_bounds.cpp:83-89, 123-124, 158-160, 194-195)
 constexpr int kFineFirst[4] = {1, 0, 2, 0};
 constexpr int kFineStep[4] = {2, 2, 1, 1};
 }  // namespace

@@ -4,7 +4,7 @@
  * spaceauk/AMR2D_MHD).
  *
  * The reference has no library API: its seam is the set of free functions
- * main() calls on a `meshblock&` (main.cpp:241-360).  Each entry point below
+ * main() calls on a `meshblock&` (main.cpp:128-247).  Each entry point below
  * names the reference function it replaces.  Conventions:
  *   - plain C types only; an opaque handle owns one or more AMR problems
  *     ("instances"); all cell- and face-centred data stay resident on one GPU;
@@ -34,14 +34,14 @@ typedef enum amr_status {
   AMR_E_MAXBLOCKS = -4,   /* admesh.cpp:42-45 "nblocks exceeded max limit" */
   AMR_E_PRESSURE = -5,    /* meshblock.cpp:136-142 / 164-170 zero or negative pressure */
   AMR_E_NAN = -6,         /* celledges.cpp:17-21, MUSCL2D.cpp:79-85, meshblock.cpp:171-176 */
-  AMR_E_DT = -7,          /* main.cpp:348-351 invalid dt */
+  AMR_E_DT = -7,          /* main.cpp:235-238 invalid dt */
   AMR_E_HLLC = -8,        /* riemannS.cpp:269-276 */
   AMR_E_STATE = -9,       /* call out of order (e.g. amr_step before amr_init) */
   AMR_E_TIMEOUT = -10,    /* a bounded device wait gave up */
   AMR_E_UNSUPPORTED = -11,/* ROE with a magnetic field (riemannS.cpp:39-40), block size != 16 */
   AMR_E_ARG = -12,        /* bad pointer, size or index */
   AMR_E_TOO_LARGE = -13,  /* more blocks than a fixed-size scratch array holds */
-  AMR_E_CT = -14          /* CT2D.cpp:67 "Incorrect psi produced" (ct_type 2) */
+  AMR_E_CT = -14          /* CT2D.cpp:68 "Incorrect psi produced" (ct_type 2) */
 } amr_status;
 
 typedef enum amr_precision {
@@ -60,7 +60,7 @@ typedef enum amr_field {
   AMR_FIELD_W = 7         /* primitive state, computed from U on download */
 } amr_field;
 
-/* One AMR problem.  The first block of fields is input.txt (main.cpp:156-177);
+/* One AMR problem.  The first block of fields is input.txt (main.cpp:43-64);
  * the second block holds the reference's compile-time constants (defs.hpp)
  * and the extensions, each defaulting to the reference's value. */
 typedef struct amr_config {
@@ -83,7 +83,7 @@ typedef struct amr_config {
   int32_t precision;      /* amr_precision */
   int32_t reserved0;
   double dt_fixed;        /* extension: > 0 = every step uses this dt (no CFL
-                             reduction, no lag); 0 = main.cpp:322-347 */
+                             reduction, no lag); 0 = main.cpp:209-234 */
   int32_t ct_type;        /* defs.hpp:34 CTtype: 0 or 1 = basic EMF average, 2 = the
                              upwind-switched EMF of CT2D.cpp:28-75 */
   int32_t diffusion;      /* defs.hpp:35 diffusion: 1 = diffusivity.cpp after stage 2
@@ -92,16 +92,16 @@ typedef struct amr_config {
 } amr_config;
 
 typedef struct amr_info {
-  double t;               /* simulated time (main.cpp:344) */
+  double t;               /* simulated time (main.cpp:231) */
   double dt;              /* dt used by the last step (dom.dt) */
-  double dt_next;         /* dt the next-but-one step will use (main.cpp:347) */
+  double dt_next;         /* dt the next-but-one step will use (main.cpp:234) */
   double t_end;
   double gamma;
-  int64_t steps;          /* completed steps (main.cpp:346 count) */
+  int64_t steps;          /* completed steps (main.cpp:233 count) */
   int32_t last_active;    /* block IDs in use (dom.lastActive) */
   int32_t n_leaves;       /* leaf blocks (count of dom.leafs) */
   int32_t nb_leafs;       /* the reference's own counter dom.nbleafs (updatelpup.cpp:109) */
-  int32_t done;           /* 1 once t > t_end (main.cpp:241) */
+  int32_t done;           /* 1 once t > t_end (main.cpp:128) */
   int32_t n_instances;
   int32_t nx_tot, ny_tot; /* block size with ghosts */
   int64_t cell_updates;   /* sum over completed steps of leaf interior cells */
@@ -111,7 +111,7 @@ typedef struct amr_handle amr_handle;
 
 /* ---- configuration ----------------------------------------------------- */
 /* Defaults = the reference's constants; then parse an input.txt
- * (main.cpp:156-177: "nx ny nvar / lenx leny / CFL / IC limiter fluxMth"). */
+ * (main.cpp:43-64: "nx ny nvar / lenx leny / CFL / IC limiter fluxMth"). */
 void amr_config_default(amr_config *cfg);
 int amr_config_from_input(const char *path, amr_config *cfg);
 /* Seeded extension problems (no counterpart in the reference, which has
@@ -138,9 +138,9 @@ int amr_set_stream(amr_handle *h, void *cuda_stream);
 int amr_last_error(const amr_handle *h, char *buf, size_t len);
 
 /* ---- the time loop --------------------------------------------------------- */
-/* basegrid + IC2Dtype + W2U + initial admesh (main.cpp:210-229) */
+/* basegrid + IC2Dtype + W2U + initial admesh (main.cpp:97-116) */
 int amr_init(amr_handle *h);
-/* one iteration of main.cpp:241-360: ghost fills, two MUSCL2D + RK stages
+/* one iteration of main.cpp:128-247: ghost fills, two MUSCL2D + RK stages
  * with CT2D, the CFL dt reduction and admesh.  Instances that are done are
  * skipped. */
 int amr_step(amr_handle *h);
@@ -159,10 +159,17 @@ int amr_get_info(amr_handle *h, int32_t instance, amr_info *info);
 /* ---- reference-function entry points (single instance) -------------------- */
 int amr_locate_bounds(amr_handle *h);                        /* locate_bounds.cpp:35 */
 int amr_boundary(amr_handle *h, int32_t field);              /* boundary/boundaryfc/boundaryec */
-int amr_muscl2d_rk(amr_handle *h, int32_t step);             /* MUSCL2D + main.cpp:257-272 / 289-308 */
+int amr_muscl2d_rk(amr_handle *h, int32_t step);             /* MUSCL2D + main.cpp:144-159 / 176-195 */
 int amr_ct2d(amr_handle *h, int32_t step);                   /* CT2D.cpp:11 with its ghost fills */
-int amr_cfl_dt(amr_handle *h, double *lambda_min);           /* main.cpp:322-343 */
+int amr_cfl_dt(amr_handle *h, double *lambda_min);           /* main.cpp:209-230 */
 int amr_admesh(amr_handle *h);
+/* on = 0: amr_step ends after the dt reduction (main.cpp:209-238) without the
+ * closing admesh (main.cpp:246), so that the caller can act in between, as
+ * main.cpp:240-243 saves the state there, and then call amr_admesh, which
+ * remeshes on the same criterion the step would have used.  on = 1 (the
+ * default) restores the closing admesh.  amr_init's initial admesh is not
+ * affected. */
+int amr_set_remesh(amr_handle *h, int32_t on);
 /* criteria.cpp:6-44 on the current state of instance 0: grad[b] = the
  * largest relative jump of p, rho, Bx, By over the interior of leaf block b
  * (admesh refines where it is >= 0.05), -1 for blocks that are not leaves;
@@ -208,7 +215,7 @@ int amr_download(amr_handle *h, int32_t instance, int32_t field, double *dst, in
 int amr_upload(amr_handle *h, int32_t instance, int32_t field, const double *src, int64_t count);
 
 /* ---- measurement (no counterpart in the reference, which only has coarse
- * OpenMP wall-clock timers, main.cpp:237-369) ------------------------------ */
+ * OpenMP wall-clock timers, main.cpp:124-256) ------------------------------ */
 typedef struct amr_profile {
   int64_t launches;        /* kernels launched since the last enable/reset */
   int64_t stage_launches;  /* RK stages issued */
@@ -278,7 +285,7 @@ int amr_adjoint_recorded(amr_handle *h, int32_t *steps);
 /* ---- allocation-free CFL reduction (no counterpart in the reference) ------
  * For callers that may not allocate device memory (inside a captured CUDA
  * graph, in allocator-free real-time loops, or in frameworks that own every
- * device allocation).  Same arithmetic as amr_cfl_dt (main.cpp:322-341) on the
+ * device allocation).  Same arithmetic as amr_cfl_dt (main.cpp:209-228) on the
  * caller's device arrays:
  *   U          [nblocks][8][16+2g][16+2g] float64 conserved state (leaf blocks)
  *   dxdy       [nblocks][2] float64 cell sizes (dx, dy) of each block

@@ -594,7 +594,7 @@ static void weno5(oracle *o, int nb, int diry, scr_t *s) {
 
 /* ------------------------------------------------------------ MUSCL2D.cpp */
 /* MUSCL2D.cpp:13-121 followed by the residual / RK2ndv1 loop of
- * main.cpp:260-270 (step 1) or main.cpp:292-302 (step 2). */
+ * main.cpp:147-157 (step 1) or main.cpp:179-189 (step 2). */
 static int muscl_rk(oracle *o, int nb, int step) {
   scr_t s = thread_scratch(o);
   if (cons2prim(o, step == 1 ? o->U : o->Us, nb, step == 2)) return -1;
@@ -1097,8 +1097,8 @@ static void diffuse(oracle *o, double *U, int nb) {
  * EMF weighting the two flux averages by psi, which leaves 1/2 unless the
  * corner sits at a strong pressure jump (switch 1, beta = 0.5) in a strongly
  * compressive flow (switch 2, delta = 0.1).  The divergence term divides
- * rho*v by itself at two of its corners (:53), as the reference does.
- * Returns 1 on the reference's "Incorrect psi produced" (:67). */
+ * rho*v by itself at two of its corners (:52), as the reference does.
+ * Returns 1 on the reference's "Incorrect psi produced" (:68). */
 static int emf_upwind(oracle *o, const double *q, int nb) {
   const int nx = o->nx, ny = o->ny;
   const double g = o->gamma;
@@ -1333,10 +1333,8 @@ static void coarsen_field(oracle *o, double *Q, int nv, int face, int dad, const
       }
     }
   /* ghost cells: the cell and face versions differ in where the low-side
-   * pairs start (coarsen.cpp:197-199 vs coarsenBi_CT.cpp:38-41) and in the
-   * clamp at the array edge (coarsen.cpp:214 vs coarsenBi_CT.cpp:54). */
-  const int lo = face ? 1 : 1;  /* both start the low-side pair at (b-2*i)-1 */
-  (void)lo;
+   * pairs start (coarsen.cpp:38-41 vs coarsenBi_CT.cpp:38-41) and in the
+   * clamp at the array edge (coarsen.cpp:55 vs coarsenBi_CT.cpp:54). */
   /* Left */
   for (int k = 0; k < nv; k++)
     for (int i = 0; i < ng / 2; i++)
@@ -1741,7 +1739,7 @@ int oracle_init(oracle *o) {
     if (ic2dtype(o, nb)) return -1;
     prim2cons(o, nb);
   }
-  /* main.cpp:212-214 W2U again, then the initial remesh (main.cpp:223) */
+  /* main.cpp:99-101 W2U again, then the initial remesh (main.cpp:110) */
   for (int nb = 0; nb < o->lastActive; nb++) if (o->leafs[nb]) prim2cons(o, nb);
   o->dt = 0.0;   /* dom.dt is read before its first assignment in the reference */
   o->dtn = 0.0;
@@ -1755,7 +1753,7 @@ int oracle_init(oracle *o) {
 
 int oracle_done(const oracle *o) { return !(o->t <= o->tEnd); }
 
-/* main.cpp:241-360 */
+/* main.cpp:128-247 */
 int oracle_step(oracle *o) {
   if (!o->initialised) return fail(o, "oracle_init not called");
   if (o->err_set) return -1;
@@ -1786,7 +1784,7 @@ int oracle_step(oracle *o) {
   fill_fc(o, o->gg, 8);
   if (ct2d(o, o->U, o->Bis, 2, o->Bi)) { free(leaf); return -1; }
   fill_cc(o, o->U);
-  /* main.cpp:322-343 dt; note lambda1 takes |rho| + c_f,x (W[..][0], main.cpp:335) */
+  /* main.cpp:209-230 dt; note lambda1 takes |rho| + c_f,x (W[..][0], main.cpp:222) */
   double lambda = 1.E6;
   double *lam_b = (double *)malloc(sizeof(double) * (nL + 1));
 #pragma omp parallel for schedule(dynamic, 1) num_threads(o->nthreads) reduction(| : bad)

@@ -62,9 +62,9 @@ typedef struct oracle oracle;
 oracle *oracle_create(const oracle_cfg *cfg);
 void oracle_destroy(oracle *o);
 int oracle_init(oracle *o);            /* basegrid + IC + W2U + initial admesh */
-int oracle_step(oracle *o);            /* one iteration of main.cpp:241-360 */
+int oracle_step(oracle *o);            /* one iteration of main.cpp:128-247 */
 int oracle_run(oracle *o, int nsteps, double t_stop);  /* steps until count==nsteps or t>t_stop */
-int oracle_done(const oracle *o);      /* 1 when t > tEnd (loop exit of main.cpp:241) */
+int oracle_done(const oracle *o);      /* 1 when t > tEnd (loop exit of main.cpp:128) */
 void oracle_info(const oracle *o, int *ints /*[8]*/, double *dbls /*[8]*/);
 int64_t oracle_get(const oracle *o, int what, void *dst); /* returns #elements */
 const char *oracle_error(const oracle *o);

@@ -11,7 +11,7 @@
 #   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=nofma CTTYPE=2 DIFFUSION=true
 #
 # The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>[_CT2][_DIFF]/main.x; run it in a directory
-# holding input.txt with stdin "2\n0\n" (main.cpp:188,388).
+# holding input.txt with stdin "2\n0\n" (main.cpp:75,275).
 
 REF     ?= /root/reference
 MAXLEVS ?= 5

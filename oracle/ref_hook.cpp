@@ -5,19 +5,19 @@
 // main.cpp with `-Dadmesh=amr_ref_admesh_hook -Dsave4py=amr_ref_save4py`, so
 // main's own calls land here:
 //
-//   * main.cpp:223 (initial remesh) and main.cpp:359 (remesh at the end of
+//   * main.cpp:110 (initial remesh) and main.cpp:246 (remesh at the end of
 //     every step) call amr_ref_admesh_hook, which dumps the full-precision
 //     state (U, W, face B, quadtree) AFTER delegating to the real admesh().
 //     The dump taken at the end of step n is therefore the state after the
 //     two RK stages, CT, the dt reduction and the remesh of step n, i.e. the
 //     state the time loop starts step n+1 from.
-//   * main.cpp:355,375 call amr_ref_save4py, a no-op: the reference's text
+//   * main.cpp:242,262 call amr_ref_save4py, a no-op: the reference's text
 //     writer (savedata.cpp) keeps only 6 significant digits.
 //
 // The hook also pins one undefined behaviour of the reference: main.cpp reads
 // dom.dt (an uninitialised member, defs.hpp:90) in the RK stages of the first
-// step before main.cpp:344 assigns it.  The first call (the initial remesh,
-// main.cpp:223) sets dom.dt = 0, which is what the reference sees in practice
+// step before main.cpp:231 assigns it.  The first call (the initial remesh,
+// main.cpp:110) sets dom.dt = 0, which is what the reference sees in practice
 // on a fresh stack and what every other implementation here assumes.
 //
 // Environment:
@@ -37,7 +37,7 @@ void admesh(meshblock &dom);
 namespace {
 
 int g_calls = 0;      // number of hook calls so far
-double g_t = 0.0;     // replica of main's t (t = t + dt, main.cpp:344)
+double g_t = 0.0;     // replica of main's t (t = t + dt, main.cpp:231)
 
 long env_long(const char *name, long dflt) {
   const char *v = std::getenv(name);

@@ -9,7 +9,7 @@ from parity_util import to_gpu_cfg
 
 @pytest.mark.gpu
 def test_individual_calls_reproduce_one_step(gpu):
-    """main.cpp:241-359 issued call by call equals amr_step (first step, dt = 0)."""
+    """main.cpp:128-246 issued call by call equals amr_step (first step, dt = 0)."""
     kw = to_gpu_cfg(dict(ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=3))
     a = gpu.Simulation(**kw).init()
     b = gpu.Simulation(**kw).init()
@@ -222,3 +222,21 @@ def test_set_tree_refuses_a_broken_tree(gpu):
     sim.run(2)
     a, b = sim.state(), o.state()
     assert P.compare_states(a, b, 2)[0] and np.array_equal(a["U"], b["U"])
+
+
+@pytest.mark.gpu
+def test_remesh_off_then_admesh_is_a_step(gpu):
+    """amr_set_remesh(0) + amr_step + amr_admesh equals amr_step bit for bit:
+    the caller can act between the dt reduction and admesh, as main.cpp:240-246
+    saves there."""
+    kw = to_gpu_cfg(dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4))
+    a = gpu.Simulation(**kw).init()
+    b = gpu.Simulation(**kw).init()
+    b.set_remesh(False)
+    for _ in range(25):
+        a.step()
+        b.step()
+        b.admesh()
+    sa, sb = a.state(), b.state()
+    assert P.compare_states(sa, sb, 2)[0]
+    assert np.array_equal(sa["U"], sb["U"]) and np.array_equal(sa["Bi"], sb["Bi"]) and sa["t"] == sb["t"]

@@ -121,3 +121,35 @@ def test_download_into_callers_array(gpu):
     assert got is buf and np.array_equal(buf, U)
     other = sim.download("U", out=np.zeros((1, 8, 20, 20)))
     assert other.shape == U.shape and np.array_equal(other, U)
+
+
+@pytest.mark.gpu
+def test_driver_runs_an_input_txt(gpu, tmp_path):
+    """amr2d_mhd on a Brio-Wu input.txt runs to t > tEnd, writes a file every
+    20 steps and one at the end (main.cpp:240-243, 262), and its step-20 file,
+    written before that step's admesh, equals the library's save4py at the
+    same point of the same loop."""
+    import re
+    import subprocess
+
+    from amr2d_mhd_gb300 import build as B
+    B.build()
+    (tmp_path / "input.txt").write_text("16 16 8\n1.0 1.0 \n0.4\nBWx MC RUSA\n")
+    r = subprocess.run([B.DRIVER, "--maxlevs", "3", "--quiet"], cwd=tmp_path, input="2\n0\n",
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    steps = int(re.search(r"after (\d+) steps", r.stdout).group(1))
+    files = sorted(os.listdir(tmp_path / "data"))
+    assert steps > 40 and len(files) == steps // 20 + 1
+    sim = gpu.Simulation(**to_gpu_cfg(dict(ic="BWx", limiter="MC", flux="RUSA", cfl=0.4, maxlevs=3))).init()
+    sim.set_remesh(False)
+    for k in range(20):
+        sim.step()
+        if k < 19:
+            sim.admesh()
+    out = tmp_path / "api"
+    out.mkdir()
+    name = sim.save4py(str(out), id=1)
+    first = [f for f in files if f.startswith("BWx001t_")]
+    assert len(first) == 1
+    assert open(name).read() == open(tmp_path / "data" / first[0]).read()
