@@ -43,13 +43,17 @@ def _flags(src: str):
     return ARCH + common + fmad
 
 
-def _stamp() -> float:
+def _stamp(d: str = CSRC) -> float:
+    """Newest input of the library (d = CSRC) or of the host program (d = HOST)."""
     t = 0.0
-    for d in (CSRC, HOST):
-        for f in os.listdir(d):
-            t = max(t, os.path.getmtime(os.path.join(d, f)))
+    for f in os.listdir(d):
+        t = max(t, os.path.getmtime(os.path.join(d, f)))
     t = max(t, os.path.getmtime(os.path.join(HERE, "..", "include", "amr2d_mhd.h")))
     return max(t, os.path.getmtime(__file__))
+
+
+def _driver_stale() -> bool:
+    return not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < max(_stamp(HOST), os.path.getmtime(LIB))
 
 
 def build_driver() -> str:
@@ -74,9 +78,8 @@ def build_driver() -> str:
 
 
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
-    stamp = _stamp()
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= stamp:
-        if not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < stamp:
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _stamp():
+        if _driver_stale():
             build_driver()
         return LIB
     nvcc = _nvcc()
