@@ -89,8 +89,13 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double *g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// device address of g_cfl_scratch on the current device, looked up once per
-// device (in host code the symbol is only a stand-in, not a device address)
+// Set-up of the current device, once per device: the device address of
+// g_cfl_scratch (in host code the symbol is only a stand-in, not a device
+// address), and every kernel of this entry point loaded now (under lazy
+// module loading a kernel first launched inside a stream capture would load
+// there).  The cached address belongs to the device's context: after a
+// cudaDeviceReset it is stale, so this entry point is not used again in that
+// process.
 cudaError_t scratch_for_current_device(double **out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -98,6 +103,10 @@ cudaError_t scratch_for_current_device(double **out) {
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_mu);
   if (!g_scratch_ptr[dev]) {
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k_cfl_static_blocks<2>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, k_cfl_static_blocks<4>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, k_cfl_static_min)) != cudaSuccess) return e;
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_cfl_scratch);
     if (e != cudaSuccess) return e;
@@ -111,16 +120,20 @@ cudaError_t scratch_for_current_device(double **out) {
 }  // namespace amr
 
 extern "C" int amr_cfl_dt_static(const double *U, int32_t nblocks, int32_t nghosts, const double *dxdy,
-                                 double gamma, double *lambda_out, void *stream) {
+                                 double gamma, double *dt_per_cfl_out, void *stream) {
   using namespace amr;
-  if (!U || !dxdy || !lambda_out || nblocks <= 0) return AMR_E_ARG;
+  if (!U || !dxdy || !dt_per_cfl_out || nblocks <= 0) return AMR_E_ARG;
   if (nblocks > kCflStaticMaxBlocks) return AMR_E_TOO_LARGE;
   if (nghosts != 2 && nghosts != 4) return AMR_E_CONFIG;
+  // an error the caller's own earlier work left pending is theirs: report
+  // it without clearing it, and launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return AMR_E_CUDA;
   double *scratch = nullptr;
   if (scratch_for_current_device(&scratch) != cudaSuccess) return AMR_E_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (nghosts == 2) k_cfl_static_blocks<2><<<nblocks, 256, 0, s>>>(U, dxdy, gamma, scratch);
   else k_cfl_static_blocks<4><<<nblocks, 256, 0, s>>>(U, dxdy, gamma, scratch);
-  k_cfl_static_min<<<1, 1024, 0, s>>>(scratch, nblocks, lambda_out);
+  if (cudaGetLastError() != cudaSuccess) return AMR_E_CUDA;
+  k_cfl_static_min<<<1, 1024, 0, s>>>(scratch, nblocks, dt_per_cfl_out);
   return cudaGetLastError() == cudaSuccess ? AMR_OK : AMR_E_CUDA;
 }

@@ -161,7 +161,8 @@ int amr_locate_bounds(amr_handle *h);                        /* locate_bounds.cp
 int amr_boundary(amr_handle *h, int32_t field);              /* boundary/boundaryfc/boundaryec */
 int amr_muscl2d_rk(amr_handle *h, int32_t step);             /* MUSCL2D + main.cpp:144-159 / 176-195 */
 int amr_ct2d(amr_handle *h, int32_t step);                   /* CT2D.cpp:11 with its ghost fills */
-int amr_cfl_dt(amr_handle *h, double *lambda_min);           /* main.cpp:209-230 */
+/* main.cpp:209-230: the reference's `lambda` = dt / CFL of the current state */
+int amr_cfl_dt(amr_handle *h, double *dt_per_cfl);
 int amr_admesh(amr_handle *h);
 /* on = 0: amr_step ends after the dt reduction (main.cpp:209-238) without the
  * closing admesh (main.cpp:246), so that the caller can act in between, as
@@ -287,19 +288,25 @@ int amr_adjoint_recorded(amr_handle *h, int32_t *steps);
  * graph, in allocator-free real-time loops, or in frameworks that own every
  * device allocation).  Same arithmetic as amr_cfl_dt (main.cpp:209-228) on the
  * caller's device arrays:
- *   U          [nblocks][8][16+2g][16+2g] float64 conserved state (leaf blocks)
- *   dxdy       [nblocks][2] float64 cell sizes (dx, dy) of each block
- *   lambda_out one float64 on the device: min(1e6, min over blocks of
- *              min(dx,dy) / max(|rho| + c_f,x, |u| + c_f,y)); NaN if a block's
- *              wave speed is NaN (this variant has no pressure trap)
+ *   U              [nblocks][8][16+2g][16+2g] float64 conserved state (leaf blocks)
+ *   dxdy           [nblocks][2] float64 cell sizes (dx, dy) of each block
+ *   dt_per_cfl_out one float64 on the device: the reference's `lambda`
+ *                  (main.cpp:228), i.e. dt / CFL = min(1e6, min over blocks
+ *                  of min(dx,dy) / max(|rho| + c_f,x, |u| + c_f,y)); NaN if a
+ *                  block's wave speed is NaN (this variant has no pressure
+ *                  trap)
  * The per-block scratch is a fixed file-scope device array of 65536 doubles
  * (512 KiB on every GPU that loads the library, kept until exit); nblocks
  * above 65536 returns AMR_E_TOO_LARGE.  The first call on a device looks up
- * that array's address; make it before any stream capture.  Calls share the
- * array, so calls that overlap on the GPU (different streams) race.  Work is
- * enqueued on `cuda_stream`; the call does not synchronise. */
+ * that array's address and loads the entry point's kernels; make it before
+ * any stream capture, and do not use the entry point after a cudaDeviceReset
+ * in the same process (the looked-up address belongs to the old context).
+ * Calls share the array, so calls that overlap on the GPU (different
+ * streams) race: serialise them on one stream.  An error already pending in
+ * the CUDA runtime is reported as AMR_E_CUDA and left for its owner.  Work
+ * is enqueued on `cuda_stream`; the call does not synchronise. */
 int amr_cfl_dt_static(const double *U, int32_t nblocks, int32_t nghosts, const double *dxdy, double gamma,
-                      double *lambda_out, void *cuda_stream);
+                      double *dt_per_cfl_out, void *cuda_stream);
 
 #ifdef __cplusplus
 }

@@ -1,19 +1,31 @@
 # Test infrastructure: builds the UNMODIFIED reference (spaceauk/AMR2D_MHD)
 # from its sources where they lie, plus oracle/ref_hook.cpp, into oracle/_ref/.
-# Nothing is copied: the only generated source is defs.hpp with `maxlevs`
+# Nothing is copied: the generated sources are defs.hpp with `maxlevs`
 # replaced (it is a compile-time constant in the reference, defs.hpp:28), and
 # `-I-` makes the compiler pick that header instead of the one beside the
-# sources (likewise `nghosts`, defs.hpp:27, which WENO5 needs at 4).  main.cpp is compiled with two renames (see ref_hook.cpp).
+# sources (likewise `nghosts`, defs.hpp:27, which WENO5 needs at 4); with
+# ROTOR_G53=1 also IC2Dtype.cpp with the rotor's gamma (IC2Dtype.cpp:77,
+# 1.4) replaced by 5.0/3.0.  main.cpp is compiled with two renames (see
+# ref_hook.cpp).
 #
-#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=shipped   # makefile:9-13 flags
-#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=nofma     # same + -ffp-contract=off
-#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=omp       # same as shipped + USE_OMP
-#   make -f oracle/ref.mk MAXLEVS=4 FLAVOR=nofma CTTYPE=2 DIFFUSION=true
+# REF (the reference checkout) has no default: pass it, or export
+# AMR_REFERENCE_SRC.
 #
-# The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>[_CT2][_DIFF]/main.x; run it in a directory
-# holding input.txt with stdin "2\n0\n" (main.cpp:75,275).
+#   make -f oracle/ref.mk REF=<src> MAXLEVS=4 FLAVOR=shipped   # makefile:9-13 flags
+#   make -f oracle/ref.mk REF=<src> MAXLEVS=4 FLAVOR=nofma     # same + -ffp-contract=off
+#   make -f oracle/ref.mk REF=<src> MAXLEVS=4 FLAVOR=omp       # same as shipped + USE_OMP
+#   make -f oracle/ref.mk REF=<src> MAXLEVS=4 FLAVOR=nofma CTTYPE=2 DIFFUSION=true
+#   make -f oracle/ref.mk REF=<src> MAXLEVS=5 FLAVOR=nofma ROTOR_G53=1
+#
+# The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>[_CT2][_DIFF][_RG53]/main.x;
+# run it in a directory holding input.txt with stdin "2\n0\n" (main.cpp:75,275).
+# The omp flavour is for timing only: its dt loop (main.cpp:215-223) updates
+# the shared lambda1 / lambda2 from every thread without a reduction.
 
-REF     ?= /root/reference
+REF     ?= $(AMR_REFERENCE_SRC)
+ifeq ($(strip $(REF)),)
+$(error REF is not set: pass REF=<reference checkout> or export AMR_REFERENCE_SRC)
+endif
 MAXLEVS ?= 5
 NGHOSTS ?= 2
 FLAVOR  ?= shipped
@@ -22,8 +34,10 @@ FLAVOR  ?= shipped
 # build directory
 CTTYPE    ?= 1
 DIFFUSION ?= false
+# 1: the rotor IC with gamma = 5/3 instead of the reference's 1.4
+ROTOR_G53 ?= 0
 HERE    := $(dir $(lastword $(MAKEFILE_LIST)))
-VARIANT := $(if $(filter-out 1,$(CTTYPE)),_CT$(CTTYPE))$(if $(filter true,$(DIFFUSION)),_DIFF)
+VARIANT := $(if $(filter-out 1,$(CTTYPE)),_CT$(CTTYPE))$(if $(filter true,$(DIFFUSION)),_DIFF)$(if $(filter 1,$(ROTOR_G53)),_RG53)
 OUT     := $(HERE)_ref/L$(MAXLEVS)_G$(NGHOSTS)_$(FLAVOR)$(VARIANT)
 
 CXX     ?= g++
@@ -69,6 +83,19 @@ $(OUT)/defs.hpp: $(REF)/defs.hpp
 	@grep -q 'const int nghosts=$(NGHOSTS); ' $@ || (echo "nghosts patch failed" && rm -f $@ && false)
 	@grep -q 'const int CTtype=$(CTTYPE);' $@ || (echo "CTtype patch failed" && rm -f $@ && false)
 	@grep -q 'const bool diffusion=$(DIFFUSION);' $@ || (echo "diffusion patch failed" && rm -f $@ && false)
+
+# the rotor branch of IC2Dtype.cpp (between IC=="rotor" and its tEnd) with
+# gamma = 5/3; exactly one line changes
+$(OUT)/IC2Dtype_g53.cpp: $(REF)/IC2Dtype.cpp
+	@mkdir -p $(OUT)
+	sed -e '/IC=="rotor"/,/tEnd=0.295/ s/gamma=1\.4;/gamma=5.0\/3.0;/' $< > $@
+	@test "$$(diff $< $@ | grep -c '^>')" = 1 || (echo "rotor gamma patch failed" && rm -f $@ && false)
+	@grep -q 'gamma=5.0/3.0;' $@ || (echo "rotor gamma patch failed" && rm -f $@ && false)
+
+ifeq ($(ROTOR_G53),1)
+$(OUT)/IC2Dtype.o: $(OUT)/IC2Dtype_g53.cpp $(OUT)/defs.hpp
+	$(CXX) -c $(CFLAGS) $(INC) $< -o $@
+endif
 
 $(OUT)/%.o: $(REF)/%.cpp $(OUT)/defs.hpp
 	$(CXX) -c $(CFLAGS) $(INC) $< -o $@

@@ -25,6 +25,9 @@
 //   AMR_REF_EVERY  dump every k-th step (default 1); step 0 = after the
 //                  initial remesh, before the time loop
 //   AMR_REF_STOP   exit(0) right after the dump of this step (default: run on)
+//   AMR_REF_TLOG   path of a log that receives, for EVERY step (dumped or
+//                  not), one record: i32 step, i32 lastActive, i32 leaves,
+//                  i32 0, f64 t, f64 dt (the dump header's t and dt)
 #include "defs.hpp"
 
 #include <cstdio>
@@ -86,6 +89,22 @@ void dump(meshblock &dom, int step) {
   std::fclose(f);
 }
 
+FILE *g_tlog = nullptr;
+
+void log_step(meshblock &dom, int step) {
+  const char *path = std::getenv("AMR_REF_TLOG");
+  if (!path || !*path) return;
+  if (!g_tlog) {
+    g_tlog = std::fopen(path, "wb");
+    if (!g_tlog) { std::perror(path); std::exit(3); }
+  }
+  int32_t leaves = 0;
+  for (int nb = 0; nb < dom.lastActive; nb++) leaves += dom.leafs[nb] ? 1 : 0;
+  put_i32(g_tlog, step); put_i32(g_tlog, dom.lastActive); put_i32(g_tlog, leaves); put_i32(g_tlog, 0);
+  put_f64(g_tlog, g_t); put_f64(g_tlog, (double)dom.dt);
+  std::fflush(g_tlog);
+}
+
 }  // namespace
 
 void amr_ref_admesh_hook(meshblock &dom) {
@@ -99,6 +118,7 @@ void amr_ref_admesh_hook(meshblock &dom) {
   }
   g_calls++;
   admesh(dom);
+  log_step(dom, step);
   long every = env_long("AMR_REF_EVERY", 1);
   long stop = env_long("AMR_REF_STOP", -1);
   if (every > 0 && step % every == 0) dump(dom, step);

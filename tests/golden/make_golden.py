@@ -1,7 +1,7 @@
 """Generates the golden fixtures of tests/golden/ from the reference itself.
 
-Needs the reference sources (spaceauk/AMR2D_MHD, default /root/reference, or
-AMR_REFERENCE_SRC): it builds the unmodified reference with oracle/ref.mk
+Needs the reference sources (spaceauk/AMR2D_MHD), named by the environment
+variable AMR_REFERENCE_SRC: it builds the unmodified reference with oracle/ref.mk
 (FLAVOR=nofma: the shipped makefile flags plus -ffp-contract=off, so that its
 floating-point operations are not fused and every other implementation can
 reproduce them exactly) and records
@@ -10,7 +10,11 @@ reproduce them exactly) and records
                     dt, leaf counts, per-variable sums) of a time loop;
   state_<name>.npz  one full state (lp, icoord, leafs, U, Bi) of a small run;
   kat_riemann.npz   riemannS() answers for seeded left / right states;
-  kat_limiter.npz   slopelimiter() answers.
+  kat_limiter.npz   slopelimiter() answers;
+  long_<name>.npz   a run to its end time: t, dt and leaf counts of every
+                    step, fingerprints every `every` steps and of the last
+                    step (the bench's rotor, gamma 5/3, built with
+                    ROTOR_G53=1).
 
 Usage: python tests/golden/make_golden.py [name ...]
 """
@@ -53,6 +57,11 @@ RUNS = {
     "bw_L4_mc_rusa_diff_100": ("BWx", "MC", "RUSA", 0.4, 4, 2, 100, dict(diffusion=True)),
     "rotor_L5_mc_hlld_ct2diff_60": ("rotor", "MC", "HLLD", 0.4, 5, 2, 60, dict(ct_type=2, diffusion=True)),
 }
+# name: (ic, limiter, flux, cfl, maxlevs, nghosts, every, build options)
+LONG = {
+    "rotor53_L5_mc_hlld": ("rotor", "MC", "HLLD", 0.4, 5, 2, 25, dict(rotor_g53=True)),
+    "rotor53_L5_mc_rusa": ("rotor", "MC", "RUSA", 0.4, 5, 2, 25, dict(rotor_g53=True)),
+}
 STATES = {  # name: (ic, limiter, flux, cfl, maxlevs, nghosts, step)
     "bw_L2_mc_rusa_step10": ("BWx", "MC", "RUSA", 0.4, 2, 2, 10),
 }
@@ -70,6 +79,34 @@ def make_run(name):
         os.remove(os.path.join(wd, f))
     os.rmdir(wd)
     print(name, "steps", n, "t_end", recs[-1]["t"], "leaves", recs[-1]["nleaves"])
+
+
+def make_long(name):
+    ic, lim, fl, cfl, L, ng, every, opts = LONG[name]
+    recs = {}
+
+    def consume(step, st):
+        recs[step] = record(st, ng)
+        if step % (every * 40) == 0:
+            print(name, "step", step, "t", st["t"], "leaves", recs[step]["nleaves"], flush=True)
+
+    tlog, wd = ref_runner.run_stream(consume, ic, lim, fl, cfl, L, 10 ** 7, nghosts=ng, every=every, **opts)
+    n = tlog[-1][0]
+    assert [r[0] for r in tlog] == list(range(n + 1)), "time log has gaps"
+    assert n in recs, "no dump of the last step"
+    fp = sorted(recs)
+    meta = dict(ic=ic, limiter=lim, flux=fl, cfl=cfl, maxlevs=L, nghosts=ng, steps=n, every=every, gamma=5.0 / 3.0,
+                **opts)
+    np.savez_compressed(os.path.join(HERE, "long_%s.npz" % name), meta=np.array(repr(meta)),
+                        t=np.array([r[3] for r in tlog]), dt=np.array([r[4] for r in tlog]),
+                        nleaves=np.array([r[2] for r in tlog], np.int32),
+                        last_active=np.array([r[1] for r in tlog], np.int32),
+                        fp_step=np.array(fp, np.int32), tree=np.array([recs[s]["tree"] for s in fp]),
+                        leaf=np.array([recs[s]["leaf"] for s in fp]), sums=np.array([recs[s]["sums"] for s in fp]))
+    for f in os.listdir(wd):
+        os.remove(os.path.join(wd, f))
+    os.rmdir(wd)
+    print(name, "steps", n, "t_end", tlog[-1][3], "leaves", tlog[-1][2])
 
 
 def make_state(name):
@@ -107,7 +144,7 @@ def make_kat_riemann():
             for q in range(n):
                 cases.append((fl, d, g[q], wL[q], wR[q]))
     exe = os.path.join(os.path.dirname(ref_runner.build(5, 2, "nofma")), "kat.x")
-    subprocess.check_call(["make", "-s", "-f", os.path.join(REPO, "oracle", "ref.mk"), "REF=" + ref_runner.REF,
+    subprocess.check_call(["make", "-s", "-f", os.path.join(REPO, "oracle", "ref.mk"), "REF=" + ref_runner.ref_dir(),
                            "MAXLEVS=5", "NGHOSTS=2", "FLAVOR=nofma", "kat"], cwd=REPO, stderr=subprocess.DEVNULL)
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in"), os.path.join(td, "out")
@@ -146,12 +183,14 @@ if __name__ == "__main__":
     if not ref_runner.available():
         sys.exit("reference sources not found (set AMR_REFERENCE_SRC)")
     pyoracle.build()
-    names = sys.argv[1:] or (["kat"] + list(STATES) + list(RUNS))
+    names = sys.argv[1:] or (["kat"] + list(STATES) + list(RUNS) + list(LONG))
     for nm in names:
         if nm == "kat":
             make_kat_riemann()
             make_kat_limiter()
         elif nm in STATES:
             make_state(nm)
+        elif nm in LONG:
+            make_long(nm)
         else:
             make_run(nm)

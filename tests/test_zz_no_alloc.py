@@ -5,8 +5,9 @@ inside a captured CUDA graph, allocator-free real-time loops, frameworks that
 own every device allocation -- call amr_cfl_dt_static with their own device
 arrays; its per-block scratch is a fixed 65536-entry array in the library's
 device globals.  The test checks it through the C ABI against amr_cfl_dt, on
-two calls in a row.  This file sorts last so that a run that stops at the
-first failure has already run every other test.
+two calls in a row, with 2 ghost layers (MUSCL) and 4 (WENO5).  This file
+sorts last so that a run that stops at the first failure has already run
+every other test.
 """
 import ctypes
 
@@ -26,11 +27,13 @@ def _dxdy(lp, lf, lenx=1.0, nroots=2, ni=16):
 
 
 @pytest.mark.gpu
-def test_cfl_dt_static_matches_cfl_dt(gpu):
+@pytest.mark.parametrize("limiter,nghosts,maxlevs", [("MC", 2, 4), ("WENO5", 4, 3)])
+def test_cfl_dt_static_matches_cfl_dt(gpu, limiter, nghosts, maxlevs):
     import torch
 
     L = gpu.load()
-    sim = gpu.Simulation(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4).init()
+    sim = gpu.Simulation(ic="rotor", limiter=limiter, flux="HLLD", cfl=0.4, maxlevs=maxlevs,
+                         nghosts=nghosts).init()
     stream = torch.cuda.current_stream()
     out = torch.empty(1, dtype=torch.float64, device="cuda")
     for call in range(2):
@@ -41,7 +44,7 @@ def test_cfl_dt_static_matches_cfl_dt(gpu):
         dxdy = torch.from_numpy(_dxdy(lp, lf)).cuda()
         torch.cuda.synchronize()
         free0 = torch.cuda.mem_get_info()[0]
-        rc = L.amr_cfl_dt_static(ctypes.c_void_p(U.data_ptr()), int(lf.sum()), 2,
+        rc = L.amr_cfl_dt_static(ctypes.c_void_p(U.data_ptr()), int(lf.sum()), nghosts,
                                  ctypes.c_void_p(dxdy.data_ptr()), sim.info()["gamma"],
                                  ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
         assert rc == 0
