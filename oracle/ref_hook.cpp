@@ -22,8 +22,8 @@
 //
 // Environment:
 //   AMR_REF_DUMP   path prefix; dumps go to <prefix>_<step>.bin
-//   AMR_REF_EVERY  dump every k-th step (default 1); step 0 = after the
-//                  initial remesh, before the time loop
+//   AMR_REF_EVERY  dump every k-th step (default 1) and the last step of the
+//                  time loop; step 0 = after the initial remesh, before it
 //   AMR_REF_STOP   exit(0) right after the dump of this step (default: run on)
 //   AMR_REF_TLOG   path of a log that receives, for EVERY step (dumped or
 //                  not), one record: i32 step, i32 lastActive, i32 leaves,
@@ -121,7 +121,10 @@ void amr_ref_admesh_hook(meshblock &dom) {
   log_step(dom, step);
   long every = env_long("AMR_REF_EVERY", 1);
   long stop = env_long("AMR_REF_STOP", -1);
-  if (every > 0 && step % every == 0) dump(dom, step);
+  // the time loop ends after this step when t > tEnd (main.cpp:128): that
+  // step is dumped whatever `every` says
+  const bool last = !(g_t <= (double)dom.tEnd);
+  if (every > 0 && (step % every == 0 || last)) dump(dom, step);
   if (stop >= 0 && step >= stop) {
     if (every <= 0 || step % every != 0) dump(dom, step);
     std::fflush(stdout);
