@@ -139,7 +139,8 @@ cudaError_t launch_dt_cell(const Method &m, const DtArgs &a, int n, cudaStream_t
 
 cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  AMR_DISPATCH_NG_S(m, k_refine, n, 256, 0, s, a);
+  const int per = 4 * (m.ng == 2 ? refine_chunks<2>() : refine_chunks<4>());   // (son, chunk) CTAs per op
+  AMR_DISPATCH_NG_S(m, k_refine, n * per, kRefineChunk, 0, s, a);
   return cudaGetLastError();
 }
 

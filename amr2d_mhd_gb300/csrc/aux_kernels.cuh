@@ -283,10 +283,12 @@ __global__ void __launch_bounds__(128) k_diffuse(CtArgs a) {
 }
 
 // --------------------------------------------- dt (main.cpp:209-230) and
-// refinement criterion (criteria.cpp:6-44) of every leaf: one CTA per leaf,
-// one thread per interior cell, reading the primitive state that k_prim wrote
-// for U (FP64 for the FP64 path; the FP32 path computes the cell values in
-// FP32 and reduces them in FP64).
+// refinement criterion (criteria.cpp:6-44) of every leaf: one CTA per leaf.
+// The CTA first converts the block's U to primitives in shared memory
+// (U2W("main"), main.cpp:213, with its pressure trap on the interior and its
+// NaN trap on every cell, as k_prim), then one thread per interior cell
+// forms the wave speeds and the criterion from them (FP64 for the FP64 path;
+// the FP32 path computes the cell values in FP32 and reduces them in FP64).
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -299,9 +301,10 @@ __device__ __forceinline__ double warp_max(double v) {
 struct DtArgs {
   const LeafTask *tasks;
   const InstParams *inst;
-  const void *W;    // primitive state of U
+  const void *U;    // conserved state after the step
   double *lambda;   // per task: max over cells of max(|rho| + c_f,x, |u| + c_f,y)
   double *grad;     // per task: max relative jump
+  DevError *err;
   int want_grad;
 };
 
@@ -310,13 +313,31 @@ __global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
   pdl_wait();
   using G = Geo<NG>;
   using T = S;
-  constexpr int N = G::N, NN = G::NN;
+  constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
   static_assert(NI * NI == 256, "one thread per interior cell");
   __shared__ double red[2][8];
+  __shared__ S sW[8 * NN];
   const LeafTask t = a.tasks[blockIdx.x];
+  const S *U = static_cast<const S *>(a.U) + static_cast<size_t>(t.slot) * 8 * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    S u[8], w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = U[k * NN + c];
+    cons2prim_cell<S>(u, w, a.inst[t.inst].gamma);
+#pragma unroll
+    for (int k = 0; k < 8; k++) sW[k * NN + c] = w[k];
+    const int i = c % N, j = c / N;
+    if (w[4] <= S(0) && i > LO && i < HI + 1 && j > LO && j < HI + 1)
+      dev_fail(a.err, DERR_PRESSURE, t.slot, i, j, static_cast<double>(w[4]));
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 8; k++) bad |= isnan(w[k]);
+    if (bad) dev_fail(a.err, DERR_NAN, t.slot, i, j, 0.0);
+  }
+  __syncthreads();
   const T g = static_cast<T>(a.inst[t.inst].gamma);
   const int i = NG + threadIdx.x % NI, j = NG + threadIdx.x / NI, c = j * N + i;
-  const S *W = static_cast<const S *>(a.W) + static_cast<size_t>(t.slot) * 8 * NN;
+  const S *W = sW;
   T w[8];
 #pragma unroll
   for (int k = 0; k < 8; k++) w[k] = W[k * NN + c];
@@ -373,18 +394,28 @@ struct TreeOpArgs {
 };
 
 // refine.cpp:17-85 (minmod, the slope multiplies the forward difference) and
-// U2W("refine") on the sons; one CTA per refined block
+// U2W("refine") on the sons, then refineBi_CT.cpp:4-74 for the face field.
+// Work is spread over many CTAs: CTA (op, son, chunk) takes kRefineChunk
+// cells of one son, one thread per cell (8 variables and 2 face components),
+// so the FP64 divisions of a refined block run on many SMs at once.
+constexpr int kRefineChunk = 128;
+template <int NG> __host__ __device__ constexpr int refine_chunks() {
+  return (Geo<NG>::NN + kRefineChunk - 1) / kRefineChunk;
+}
+
 template <int NG, typename S>
-__global__ void k_refine(TreeOpArgs a) {
+__global__ void __launch_bounds__(kRefineChunk) k_refine(TreeOpArgs a) {
   using G = Geo<NG>;
-  constexpr int N = G::N, NN = G::NN, n2 = (N - 1) / 2;
+  constexpr int N = G::N, NN = G::NN, n2 = (N - 1) / 2, CH = refine_chunks<NG>();
   using T = S;
-  const TreeOp op = a.ops[blockIdx.x];
+  const int opi = blockIdx.x / (4 * CH), sq = (blockIdx.x / CH) % 4;
+  const int c = (blockIdx.x % CH) * kRefineChunk + threadIdx.x;
+  if (c >= NN) return;
+  const TreeOp op = a.ops[opi];
   const S *D = static_cast<const S *>(a.U) + static_cast<size_t>(op.dad) * 8 * NN;
   const T E = eps_of<T>();
-  // refine.cpp:45-59 for the 4 sons, each (son, cell) with its 8 variables
-  for (int e = threadIdx.x; e < 4 * NN; e += blockDim.x) {
-    const int sq = e / NN, c = e % NN;
+  // refine.cpp:45-59 for cell c of son sq, its 8 variables
+  {
     const int i = c % N, j = c / N;
     const int sx = (i + NG) % 2, sy = (j + NG) % 2;
     const int ii = (sq & 1) ? (i - NG + 2) / 2 + n2 : (i + NG) / 2;
@@ -411,42 +442,42 @@ __global__ void k_refine(TreeOpArgs a) {
     if (w[4] <= T(0) && i > G::LO && i < G::HI + 1 && j > G::LO && j < G::HI + 1)
       dev_fail(a.err, DERR_PRESSURE, op.son[sq], i, j, static_cast<double>(w[4]));
   }
-  // refineBi_CT.cpp:4-74
+  // refineBi_CT.cpp:4-74, both face components of cell c of son sq
   const double *Bd = a.Bi + static_cast<size_t>(op.dad) * 2 * NN;
-  for (int e = threadIdx.x; e < 4 * NN * 2; e += blockDim.x) {
-    const int k = e / (4 * NN), rem = e % (4 * NN);
-    const int sq = rem / NN, c = rem % NN;
-    const int i0 = c % N, j0 = c / N;
-    const int sx = (i0 + NG) % 2, sy = (j0 + NG) % 2;
-    const int i = (sq & 1) ? (i0 - NG + 2) / 2 + n2 : (i0 + NG) / 2;
-    const int j = (sq & 2) ? (j0 - NG + 2) / 2 + n2 : (j0 + NG) / 2;
-    const double *bx = Bd, *by = Bd + NN;
-    auto X = [&](int di, int dj) { return bx[(j + dj) * N + i + di]; };
-    auto Y = [&](int di, int dj) { return by[(j + dj) * N + i + di]; };
-    const double Bx_jm = X(0, -1), Bx = X(0, 0), Bx_jp = X(0, 1);
-    const double Bx_ip = X(1, 0), Bx_ipjm = X(1, -1), Bx_ipjp = X(1, 1);
-    const double By_im = Y(-1, 0), By = Y(0, 0), By_ip = Y(1, 0);
-    const double By_imjp = Y(-1, 1), By_jp = Y(0, 1), By_ipjp = Y(1, 1);
-    double r;
-    r = (Bx - Bx_jm) / (Bx_jp - Bx + EPS);
-    const double DyBxm = slope_limiter<double>(LIM_MINMOD, r, 0) * (Bx_jp - Bx);
-    r = (Bx_ip - Bx_ipjm) / (Bx_ipjp - Bx_ip + EPS);
-    const double DyBxp = slope_limiter<double>(LIM_MINMOD, r, 0) * (Bx_ipjp - Bx_ip);
-    r = (By - By_im) / (By_ip - By + EPS);
-    const double DxBym = slope_limiter<double>(LIM_MINMOD, r, 0) * (By_ip - By);
-    r = (By_jp - By_imjp) / (By_ipjp - By_jp + EPS);
-    const double DxByp = slope_limiter<double>(LIM_MINMOD, r, 0) * (By_ipjp - By_jp);
-    const double ax = (Bx_ip - Bx);
-    const double by_ = -1. * ax;
-    const double ay = 0.5 * (DyBxp + DyBxm);
-    const double bx_ = 0.5 * (DxByp + DxBym);
-    const double axy = (DyBxp - DyBxm);
-    const double byy = axy / (-2.);
-    const double bxy = (DxByp - DxBym);
-    const double axx = bxy / (-2.);
-    const double a0 = 0.5 * (Bx_ip + Bx) - 0.25 * axx;
-    const double b0 = 0.5 * (By_jp + By) - 0.25 * byy;
-    const double ayy = 0., bxx = 0.;
+  const int i0 = c % N, j0 = c / N;
+  const int sx = (i0 + NG) % 2, sy = (j0 + NG) % 2;
+  const int i = (sq & 1) ? (i0 - NG + 2) / 2 + n2 : (i0 + NG) / 2;
+  const int j = (sq & 2) ? (j0 - NG + 2) / 2 + n2 : (j0 + NG) / 2;
+  const double *bx = Bd, *by = Bd + NN;
+  auto X = [&](int di, int dj) { return bx[(j + dj) * N + i + di]; };
+  auto Y = [&](int di, int dj) { return by[(j + dj) * N + i + di]; };
+  const double Bx_jm = X(0, -1), Bx = X(0, 0), Bx_jp = X(0, 1);
+  const double Bx_ip = X(1, 0), Bx_ipjm = X(1, -1), Bx_ipjp = X(1, 1);
+  const double By_im = Y(-1, 0), By = Y(0, 0), By_ip = Y(1, 0);
+  const double By_imjp = Y(-1, 1), By_jp = Y(0, 1), By_ipjp = Y(1, 1);
+  double r;
+  r = (Bx - Bx_jm) / (Bx_jp - Bx + EPS);
+  const double DyBxm = slope_limiter<double>(LIM_MINMOD, r, 0) * (Bx_jp - Bx);
+  r = (Bx_ip - Bx_ipjm) / (Bx_ipjp - Bx_ip + EPS);
+  const double DyBxp = slope_limiter<double>(LIM_MINMOD, r, 0) * (Bx_ipjp - Bx_ip);
+  r = (By - By_im) / (By_ip - By + EPS);
+  const double DxBym = slope_limiter<double>(LIM_MINMOD, r, 0) * (By_ip - By);
+  r = (By_jp - By_imjp) / (By_ipjp - By_jp + EPS);
+  const double DxByp = slope_limiter<double>(LIM_MINMOD, r, 0) * (By_ipjp - By_jp);
+  const double ax = (Bx_ip - Bx);
+  const double by_ = -1. * ax;
+  const double ay = 0.5 * (DyBxp + DyBxm);
+  const double bx_ = 0.5 * (DxByp + DxBym);
+  const double axy = (DyBxp - DyBxm);
+  const double byy = axy / (-2.);
+  const double bxy = (DxByp - DxBym);
+  const double axx = bxy / (-2.);
+  const double a0 = 0.5 * (Bx_ip + Bx) - 0.25 * axx;
+  const double b0 = 0.5 * (By_jp + By) - 0.25 * byy;
+  const double ayy = 0., bxx = 0.;
+  double *out = a.Bi + static_cast<size_t>(op.son[sq]) * 2 * NN + c;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
     double res;
     if (k == 0) {
       const double tx = sx == 0 ? 0 : 0.5, ty = sy == 0 ? -0.25 : 0.25;
@@ -456,7 +487,7 @@ __global__ void k_refine(TreeOpArgs a) {
       res = b0 + bx_ * tx + by_ * ty + bxx * tx * tx + bxy * tx * ty + byy * ty * ty;
     }
     if (isnan(res)) dev_fail(a.err, DERR_REFINE_NAN, op.son[sq], i0, j0, 0.0);
-    a.Bi[static_cast<size_t>(op.son[sq]) * 2 * NN + k * NN + c] = res;
+    out[k * NN] = res;
   }
 }
 

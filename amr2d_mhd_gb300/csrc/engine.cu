@@ -695,26 +695,19 @@ int Engine::ct2d(int step) {
   return AMR_OK;
 }
 
-// primitive state of U (with the pressure / NaN traps of U2W("main")), then
-// the per-leaf wave-speed maximum and refinement criterion
+// primitive state of U (with the pressure / NaN traps of U2W("main")) and
+// the per-leaf wave-speed maximum and refinement criterion, in one kernel
 int Engine::dt_crit(bool want_grad) {
-  SplitArgs p{};
-  p.tasks = d_tasks_.as<LeafTask>();
-  p.inst = d_params_.as<InstParams>();
-  p.qin = U_;
-  p.W = W_;
-  p.err = d_err_.as<DevError>();
-  p.ntasks = static_cast<int>(tasks_.size());
-  CK(launch_prim(m_, p, stream_), "prim kernel");
   DtArgs a{};
   a.tasks = d_tasks_.as<LeafTask>();
   a.inst = d_params_.as<InstParams>();
-  a.W = W_;
+  a.U = U_;
   a.lambda = d_lambda_.as<double>();
   a.grad = d_grad_.as<double>();
+  a.err = d_err_.as<DevError>();
   a.want_grad = want_grad ? 1 : 0;
   CK(launch_dt_cell(m_, a, static_cast<int>(tasks_.size()), stream_), "dt kernel");
-  prof_.launches += 2;
+  prof_.launches += 1;
   return AMR_OK;
 }
 
