@@ -16,6 +16,41 @@ import torch
 EPS = 1.0e-15
 
 
+class BranchTape:
+    """Branches of the piecewise-smooth parts of the step: the MC limiter
+    (which of 0, 2r, (1+r)/2, 2 it returns), the larger of the two Rusanov
+    wave speeds and the sign inside |u|.  mode "record" appends the branch of
+    every evaluation; mode "replay" evaluates each with the recorded branch
+    instead of its own, i.e. the smooth map of the recorded run, whose
+    central differences converge to the derivative the adjoint computes;
+    `flips` counts evaluations whose own branch differs from the recorded
+    one.  mode None: the plain step."""
+
+    def __init__(self):
+        self.mode, self.rec, self.pos, self.flips, self.evals = None, [], 0, 0, 0
+
+    def start(self, mode):
+        self.mode, self.pos, self.flips, self.evals = mode, 0, 0, 0
+        if mode == "record":
+            self.rec = []
+
+    def branch(self, own):
+        """own: the branch index tensor of this evaluation; returns the one to use"""
+        if self.mode is None:
+            return own
+        if self.mode == "record":
+            self.rec.append(own.to(torch.int8))
+            return own
+        r = self.rec[self.pos].to(own.dtype)
+        self.pos += 1
+        self.flips += int((r != own).sum())
+        self.evals += own.numel()
+        return r
+
+
+TAPE = BranchTape()
+
+
 def kh_ic(a, n=256, gamma=5.0 / 3.0):
     """U [8, n, n], Bx, By [n, n] of the KH layer with perturbation amplitudes
     a (16) on [0,1]^2 (cell centres (i + 1/2) / n)."""
@@ -44,7 +79,30 @@ def prim(U, g):
 
 
 def mc(r):
-    return torch.clamp(torch.minimum(torch.minimum(2.0 * r, 0.5 * (1.0 + r)), torch.full_like(r, 2.0)), min=0.0)
+    """slopelimiter.cpp:23-27, max(0, min(2r, (1+r)/2, 2))"""
+    a, b = 2.0 * r, 0.5 * (1.0 + r)
+    v = torch.clamp(torch.minimum(torch.minimum(a, b), torch.full_like(r, 2.0)), min=0.0)
+    if TAPE.mode is None:
+        return v
+    own = torch.where(v == 0.0, 0, torch.where(v == a, 1, torch.where(v == b, 2, 3)))
+    br = TAPE.branch(own)
+    return torch.where(br == 0, torch.zeros_like(r), torch.where(br == 1, a, torch.where(br == 2, b, torch.full_like(r, 2.0))))
+
+
+def tabs(x):
+    """|x| with its sign branch on the tape"""
+    if TAPE.mode is None:
+        return x.abs()
+    br = TAPE.branch((x < 0).to(torch.int64))
+    return torch.where(br == 1, -x, x)
+
+
+def tmax(a, b):
+    """max(a, b) with its branch on the tape"""
+    if TAPE.mode is None:
+        return torch.maximum(a, b)
+    br = TAPE.branch((b > a).to(torch.int64))
+    return torch.where(br == 1, b, a)
 
 
 def faces(W, d):
@@ -73,7 +131,7 @@ def rusanov_x(wl, wr, g):
         return q, F, cf
     qL, FL, cL = side(wl)
     qR, FR, cR = side(wr)
-    im = torch.maximum(cL + wl[1].abs(), cR + wr[1].abs())
+    im = tmax(cL + tabs(wl[1]), cR + tabs(wr[1]))
     return 0.5 * (FL + FR) - 0.5 * im * (qR - qL)
 
 

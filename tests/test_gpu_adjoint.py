@@ -214,3 +214,62 @@ def test_kh_kinetic_energy_gradient_matches_fd(gpu):
             fd[k] = (loss(run(a0 + e, False)) - loss(run(a0 - e, False))) / (2 * h)
     err = np.abs(g - fd).max() / np.abs(fd).max()
     assert err < 1e-5, (err, g, fd)
+
+
+@pytest.mark.gpu
+def test_kh_gradient_matches_branch_frozen_fd(gpu):
+    """The stated check on the stated loss: d(total density in [0.4, 0.6]^2
+    after 200 steps) / d(a_k) from the library's adjoint against central
+    differences with h = 1e-6, to 1e-5 relative.  Plain differences cannot
+    meet it: the MC limiter, the Rusanov maximum and |u| are piecewise
+    smooth, and a shift by h moves some of their arguments across a kink (the
+    flips counted below), which adds an error of first order in h (3e-3 at h =
+    1e-6, test_kh_gradient_fd_and_reference).  The differences here are those
+    of the smooth map that takes the unperturbed run's branch at every kink
+    (kh_reference.BranchTape), whose derivative at a0 is the derivative of
+    the discrete step almost everywhere, the quantity the adjoint computes."""
+    steps, h = 200, 1e-6
+    sim, c = kh_sim(gpu)
+    ic = sim.tree()[1]
+    B0 = sim.download("Bi")
+    gi, gj = block_index(ic)
+    mask = interior_only(K.to_blocks(K.box_mask().numpy()[None], ic)[:, 0])
+    a0 = torch.tensor(list(c.ic_param[:16]), dtype=torch.float64)
+    a = a0.clone().requires_grad_(True)
+    U, _, _ = K.kh_ic(a)
+    KHLoss.apply(blocks_of(U, gi, gj), sim, B0, steps, mask).backward()
+    g_adj = a.grad.numpy().copy()
+
+    dev = "cuda"
+    box = K.box_mask(device=dev)
+
+    def run(av):
+        with torch.no_grad():
+            U, Bx, By = K.kh_ic(av.to(dev))
+            for _ in range(steps):
+                U, Bx, By = K.step(U, Bx, By, DT, GAMMA, 1.0 / N)
+            return float((U[0] * box).sum())
+
+    try:
+        K.TAPE.start("record")
+        run(a0)
+        fd = np.zeros(16)
+        flips = evals = 0
+        for k in range(16):
+            e = torch.zeros(16, dtype=torch.float64)
+            e[k] = h
+            vals = []
+            for sgn in (1.0, -1.0):
+                K.TAPE.start("replay")
+                vals.append(run(a0 + sgn * e))
+                flips += K.TAPE.flips
+                evals += K.TAPE.evals
+            fd[k] = (vals[0] - vals[1]) / (2 * h)
+    finally:
+        K.TAPE.start(None)
+        K.TAPE.rec = []
+    err = np.abs(g_adj - fd).max() / np.abs(fd).max()
+    print("branch-frozen FD h=%g: max rel diff %.3e; kink flips of the plain +-h runs: %d of %d evaluations"
+          % (h, err, flips, evals))
+    assert flips > 0
+    assert err <= 1e-5, (err, g_adj, fd)
