@@ -4,7 +4,12 @@ amr2d_mhd that drives it (in-tree, amr2d_mhd_gb300/_build/).
 Every translation unit compiles in parallel with nvcc for sm_103a only.  Every
 translation unit but the FP32 stage kernels (stage_f32_*.cu) is compiled with
 -fmad=false and the host code with -ffp-contract=off: that path reproduces the reference's
-floating-point operations one by one, so nothing may be fused.
+floating-point operations one by one, so nothing may be fused.  The FP32 stage
+kernels (the FP32 bulk path's reconstruction, Riemann fluxes and RK update)
+use FMA contraction and the approximate FP32 division and square root
+(-prec-div=false -prec-sqrt=false, about 2 ulp): their results are compared
+with the FP64 path through a tolerance, and the FP64 parts of that path
+(pressure recovery, face field, dt) are compiled elsewhere or stay FP64.
 """
 from __future__ import annotations
 
@@ -39,7 +44,7 @@ def _flags(src: str):
               "-I" + CSRC]
     if src.endswith(".cpp"):
         return ["-x", "cu"] + ARCH + common
-    fmad = [] if src.startswith("stage_f32") else ["-fmad=false"]
+    fmad = ["-prec-div=false", "-prec-sqrt=false"] if src.startswith("stage_f32") else ["-fmad=false"]
     return ARCH + common + fmad
 
 

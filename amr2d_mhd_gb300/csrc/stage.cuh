@@ -73,10 +73,11 @@ __device__ __forceinline__ void cons2prim_cell<double>(const double *u, double *
   w[4] = p - (g - 1) * (0.5 * (u[5] * u[5] + u[6] * u[6] + u[7] * u[7]));
 }
 
-// FP32 path: velocities in FP32; the pressure recovered from the total
-// energy in FP64 (the cancellation E - |m|^2/2rho - |B|^2/2 is where FP32
-// loses digits), with 1/rho from the FP32 reciprocal refined by one FP64
-// Newton step instead of FP64 divisions (FP64 runs at 1/64 of the FP32 rate).
+// FP32 path: the pressure recovered from the total energy in FP64 (the
+// cancellation E - |m|^2/2rho - |B|^2/2 is where FP32 loses digits), with
+// 1/rho from the FP32 reciprocal refined by one FP64 Newton step instead of
+// FP64 divisions (FP64 runs at 1/64 of the FP32 rate); the velocities in FP32
+// from the same FP32 reciprocal.
 template <>
 __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, double g) {
   const float ir = 1.0f / u[0];
@@ -90,9 +91,9 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
   // recovered pressure below zero where the FP64 path stays positive
   if (!(p > kPressureFloor)) p = kPressureFloor;
   w[0] = u[0];
-  w[1] = static_cast<float>(mx * ird);  // correctly rounded to ~1e-14 before the cast
-  w[2] = static_cast<float>(my * ird);
-  w[3] = static_cast<float>(mz * ird);
+  w[1] = u[1] * ir;
+  w[2] = u[2] * ir;
+  w[3] = u[3] * ir;
   w[4] = static_cast<float>(p);
   w[5] = u[5];
   w[6] = u[6];
@@ -103,6 +104,16 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
 // 64-rotor FP32 batch 2.11 ms per stage launch against 2.31 ms at 3 CTAs
 #ifndef AMR_STAGE_F32_MINB
 #define AMR_STAGE_F32_MINB 4
+#endif
+// threads per CTA of the FP32 fused stage: 2 x 17 x 17 = 578 faces per block
+// take 3 rounds at 256 threads (the last a quarter full), 2 at 320
+#ifndef AMR_STAGE_F32_THREADS
+#define AMR_STAGE_F32_THREADS 256
+#endif
+// 1: the FP32 fused stage keeps the block's conserved state in shared memory
+// beside the primitive state, so the RK update does not read it again
+#ifndef AMR_STAGE_F32_KEEPU
+#define AMR_STAGE_F32_KEEPU 0
 #endif
 
 // ------------------------------------------------------------ bulk staging
@@ -143,9 +154,13 @@ __device__ __forceinline__ bool bulk_stage_wait(uint64_t *bar, uint32_t phase) {
 // instantiation trades registers for occupancy (it is latency-bound)
 template <typename S> struct StageMinBlocks { static constexpr int value = 1; };
 template <> struct StageMinBlocks<float> { static constexpr int value = AMR_STAGE_F32_MINB; };
+template <typename S> struct StageThreads { static constexpr int value = 256; };
+template <> struct StageThreads<float> { static constexpr int value = AMR_STAGE_F32_THREADS; };
+template <typename S> struct StageKeepU { static constexpr bool value = false; };
+template <> struct StageKeepU<float> { static constexpr bool value = AMR_STAGE_F32_KEEPU != 0; };
 
 template <int NG, int RECON, int FLUX, typename S>
-__global__ void __launch_bounds__(256, StageMinBlocks<S>::value) k_stage(StageArgs a) {
+__global__ void __launch_bounds__(StageThreads<S>::value, StageMinBlocks<S>::value) k_stage(StageArgs a) {
   pdl_wait();
   using G = Geo<NG>;
   using T = S;
@@ -154,6 +169,8 @@ __global__ void __launch_bounds__(256, StageMinBlocks<S>::value) k_stage(StageAr
   T *sW = reinterpret_cast<T *>(smem_raw);   // [8][NN]
   T *sFx = sW + 8 * NN;                      // [8][NF][NFX]   face i = LO + col, row j = LO + r
   T *sFy = sFx + 8 * NF * NFX;               // [8][NFX][NF]   face j = LO + row, col i = LO + c
+  constexpr bool KEEPU = StageKeepU<S>::value;
+  S *sU = KEEPU ? sFy + 8 * NFX * NF : sW;   // [8][NN] the conserved state (KEEPU), else staged in sW
 
   const LeafTask task = a.tasks[blockIdx.x];
   const InstParams ip = a.inst[task.inst];
@@ -173,18 +190,19 @@ __global__ void __launch_bounds__(256, StageMinBlocks<S>::value) k_stage(StageAr
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0) bulk_stage_issue(sW, Q, static_cast<uint32_t>(8 * NN * sizeof(S)), &bar);
+  if (tid == 0) bulk_stage_issue(sU, Q, static_cast<uint32_t>(8 * NN * sizeof(S)), &bar);
   if (!bulk_stage_wait(&bar, 0)) {
     if (tid == 0) dev_fail(a.err, DERR_TIMEOUT, task.slot, 0, 0, 0.0);
     bulk_stage_wait(&bar, 0);  // let the copy land before the CTA's shared memory is released
     return;
   }
 
-  // 1. primitive variables of every cell (U2W / Us2W), in place, with the traps
+  // 1. primitive variables of every cell (U2W / Us2W), with the traps (in
+  // place unless the conserved state is kept)
   for (int c = tid; c < NN; c += nthr) {
     S u[8], w[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) u[k] = sW[k * NN + c];
+    for (int k = 0; k < 8; k++) u[k] = sU[k * NN + c];
     cons2prim_cell<S>(u, w, ip.gamma);
 #pragma unroll
     for (int k = 0; k < 8; k++) sW[k * NN + c] = w[k];
@@ -284,7 +302,7 @@ __global__ void __launch_bounds__(256, StageMinBlocks<S>::value) k_stage(StageAr
       res = (sFx[(k * NF + r) * NFX + cx + 1] - sFx[(k * NF + r) * NFX + cx]) / dx +
             (sFy[(k * NFX + r + 1) * NF + cx] - sFy[(k * NFX + r) * NF + cx]) / dy;
     }
-    const T q = Q[e];
+    const T q = KEEPU ? sU[e] : Q[e];
     if (a.step == 1) out[e] = q - dt * res;                         // Us = U - dt res
     else out[e] = T(0.5) * (out[e] + q - dt * res);                 // U = (U + Us - dt res)/2
   }
@@ -293,7 +311,7 @@ __global__ void __launch_bounds__(256, StageMinBlocks<S>::value) k_stage(StageAr
 template <int NG, typename S>
 constexpr int stage_smem_bytes() {
   using G = Geo<NG>;
-  return static_cast<int>(sizeof(S)) * (8 * G::NN + 2 * 8 * G::NF * G::NFX);
+  return static_cast<int>(sizeof(S)) * ((StageKeepU<S>::value ? 16 : 8) * G::NN + 2 * 8 * G::NF * G::NFX);
 }
 
 }  // namespace amr

@@ -20,7 +20,7 @@ cudaError_t launch_stage_t(const StageArgs &a, int ntasks, int pdl, cudaStream_t
     attr_set = true;
   }
   if (ntasks <= 0) return cudaSuccess;
-  return launch_k(pdl, k_stage<NG, RECON, FLUX, S>, ntasks, 256, smem, s, a);
+  return launch_k(pdl, k_stage<NG, RECON, FLUX, S>, ntasks, StageThreads<S>::value, smem, s, a);
 }
 
 template <int FLUX, typename S>
