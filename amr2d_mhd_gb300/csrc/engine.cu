@@ -79,7 +79,8 @@ Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (void *p : {U_, Us_, ff_, gg_, W_}) if (p) cudaFree(p);
   for (double *p : {Bi_, Bis_, EMF_}) if (p) cudaFree(p);
-  for (DevBuf *b : {&d_tasks_, &d_params_, &d_lambda_, &d_grad_, &d_err_, &d_snap_, &d_treeops_, &d_stage_, &d_slots_})
+  for (DevBuf *b : {&d_tasks_, &d_params_, &d_lambda_, &d_grad_, &d_err_, &d_snap_, &d_treeops_, &d_stage_, &d_slots_,
+                    &d_ctr_})
     b->release();
   d_ops_.release();
   d_snaps_.release();
@@ -193,6 +194,8 @@ int Engine::create(const amr_config *cfgs, int n) {
   built_version_.assign(n, ~0ull);
   CK(d_err_.ensure(sizeof(DevError)), "alloc");
   CK(cudaMemsetAsync(d_err_.p, 0, sizeof(DevError), stream_), "memset");
+  CK(d_ctr_.ensure(2 * sizeof(unsigned)), "alloc");   // k_faces_dyn's counters, zero between launches
+  CK(cudaMemsetAsync(d_ctr_.p, 0, 2 * sizeof(unsigned), stream_), "memset");
   CK(h_err_.ensure(sizeof(DevError)), "alloc");
   CK(h_params_.ensure(sizeof(InstParams) * n), "alloc");
   CK(d_params_.ensure(sizeof(InstParams) * n), "alloc");
@@ -560,6 +563,7 @@ int Engine::stage(int step) {
     a.ff = ff_;
     a.gg = gg_;
     a.err = d_err_.as<DevError>();
+    a.ctr = d_ctr_.as<unsigned>();
     a.step = step;
     a.ntasks = n;
     CK(launch_prim(m_, a, stream_), "prim kernel");
@@ -612,7 +616,7 @@ int Engine::autotune(int reps, char *report, size_t len) {
   std::vector<Cand> cands;
   for (int gb : {128, 256, 512}) {
     cands.push_back({false, 128, 256, gb, 0, 0.f});
-    for (int pers : {0, 1})
+    for (int pers : {0, 1, 2})
       for (int fb : {64, 128})
         for (int cb : {256, 512}) cands.push_back({true, fb, cb, gb, pers, 0.f});
   }
@@ -662,7 +666,8 @@ int Engine::autotune(int reps, char *report, size_t len) {
     char line[160];
     for (const Cand &c : cands) {
       std::snprintf(line, sizeof line, "%s%s faces %d%s cells %d ghosts %d: %.4f ms\n", &c == best ? "* " : "  ",
-                    c.split ? "split" : "fused", c.fb, c.pers ? " persistent" : "", c.cb, c.gb, c.ms);
+                    c.split ? "split" : "fused", c.fb, c.pers == 2 ? " dynamic" : (c.pers ? " persistent" : ""), c.cb,
+                    c.gb, c.ms);
       s += line;
     }
     std::strncpy(report, s.c_str(), len - 1);

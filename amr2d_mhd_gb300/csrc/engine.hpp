@@ -179,7 +179,7 @@ class Engine {
   int compile_programs();          // recompile changed instances (host threads)
   int layout_programs(bool relayout);
   DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_, d_snaps_;
-  DevBuf d_treeops_, d_stage_, d_slots_;
+  DevBuf d_treeops_, d_stage_, d_slots_, d_ctr_;
   HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_ops_, h_snaps_, h_tasks_;
   std::vector<GhostCompiler *> gcs_;  // one per compile thread
   HostPool pool_;                      // host threads of the parallel loops (remesh, compile, layout)

@@ -24,7 +24,8 @@ struct Method {
   int faces_block = 128;
   int cell_block = 256;
   int ghost_block = 256;
-  int persistent = 0;   // face fluxes by a grid of resident CTAs looping over the face list
+  int persistent = 0;   // face fluxes by a grid of resident CTAs looping over the face list: 1 in
+                        // strides, 2 claiming 32 faces per warp from a counter (k_faces_dyn)
   // the step's kernels are launched as programmatic dependents of their
   // predecessor (each begins with pdl_wait()); AMR2D_PDL=0 turns it off
   int pdl = 1;

@@ -37,17 +37,21 @@ cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, c
 #define AMR_FACES_MINB 3
 #endif
 
+// persistent: 0 one CTA per 128 (64) faces; 1 a grid of resident CTAs
+// striding over the face list; 2 the same with dynamic claims of 32 faces
+// per warp (k_faces_dyn, needs a.ctr)
 template <int NG, int RECON, int FLUX, typename S>
-cudaError_t launch_faces_t(const SplitArgs &a, int block, bool persistent, int pdl, cudaStream_t s) {
+cudaError_t launch_faces_t(const SplitArgs &a, int block, int persistent, int pdl, cudaStream_t s) {
   constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
   const size_t n = static_cast<size_t>(a.ntasks) * PER;
   if (n == 0) return cudaSuccess;
   if (block != 64) block = 128;  // the kernel is bounded at 128 threads per CTA
   size_t grid = (n + block - 1) / block;
+  if (persistent == 2 && !a.ctr) persistent = 1;
   if (persistent) {
-    // resident CTAs per SM for each block size, looked up once
-    static int per_sm[2] = {0, 0}, sms = 0;
-    int &ps = per_sm[block == 64 ? 0 : 1];
+    // resident CTAs per SM for each (variant, block size), looked up once
+    static int per_sm[2][2] = {{0, 0}, {0, 0}}, sms = 0;
+    int &ps = per_sm[persistent == 2 ? 1 : 0][block == 64 ? 0 : 1];
     if (!sms) {
       int dev = 0;
       cudaError_t e = cudaGetDevice(&dev);
@@ -55,13 +59,19 @@ cudaError_t launch_faces_t(const SplitArgs &a, int block, bool persistent, int p
       if (e != cudaSuccess) return e;
     }
     if (!ps) {
-      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &ps, k_faces_persist<NG, RECON, FLUX, S, AMR_FACES_MINB>, block, 0);
+      cudaError_t e = persistent == 2
+          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, k_faces_dyn<NG, RECON, FLUX, S, AMR_FACES_MINB>,
+                                                          block, 0)
+          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, k_faces_persist<NG, RECON, FLUX, S, AMR_FACES_MINB>,
+                                                          block, 0);
       if (e != cudaSuccess) return e;
       if (ps < 1) ps = 1;
     }
     const size_t cap = static_cast<size_t>(sms) * ps;
     if (grid > cap) grid = cap;
+    if (persistent == 2)
+      return launch_k(pdl, k_faces_dyn<NG, RECON, FLUX, S, AMR_FACES_MINB>, static_cast<unsigned>(grid), block, 0,
+                      s, a);
     return launch_k(pdl, k_faces_persist<NG, RECON, FLUX, S, AMR_FACES_MINB>, static_cast<unsigned>(grid), block, 0,
                     s, a);
   }
@@ -71,7 +81,7 @@ cudaError_t launch_faces_t(const SplitArgs &a, int block, bool persistent, int p
 template <int FLUX, typename S>
 cudaError_t launch_faces_flux(const Method &m, const SplitArgs &a, cudaStream_t s) {
   const int b = m.faces_block;
-  const bool p = m.persistent != 0;
+  const int p = m.persistent;
   if (m.ng == 2 && m.recon == REC_MUSCL) return launch_faces_t<2, REC_MUSCL, FLUX, S>(a, b, p, m.pdl, s);
   if (m.ng == 2 && m.recon == REC_WENO3) return launch_faces_t<2, REC_WENO3, FLUX, S>(a, b, p, m.pdl, s);
   if (m.ng == 4 && m.recon == REC_MUSCL) return launch_faces_t<4, REC_MUSCL, FLUX, S>(a, b, p, m.pdl, s);

@@ -20,6 +20,7 @@ struct SplitArgs {
   void *ff;
   void *gg;
   DevError *err;
+  unsigned *ctr;      // [2] work counter and finished-CTA counter of k_faces_dyn (zero between launches)
   int step;
   int ntasks;
 };
@@ -139,6 +140,35 @@ __global__ void __launch_bounds__(128, MINB) k_faces_persist(SplitArgs a) {
   const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
   for (size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n; e += stride)
     face_flux<NG, RECON, FLUX, S>(a, e);
+}
+
+// persistent variant with dynamic work distribution: a grid of the CTAs the
+// SMs hold at once, each warp claiming the next 32 faces of the step's face
+// list from a global counter, so that warps that met cheap faces (uniform
+// regions, where the limiter ratios need no division) take more; the last
+// CTA to finish zeroes the counters for the next launch (every CTA has left
+// its loop by then, so nothing claims work any more)
+template <int NG, int RECON, int FLUX, typename S, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_faces_dyn(SplitArgs a) {
+  pdl_wait();
+  constexpr int PER = 2 * Geo<NG>::NF * Geo<NG>::NF;
+  const unsigned n = static_cast<unsigned>(a.ntasks) * PER;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&a.ctr[0], 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    if (base + lane < n) face_flux<NG, RECON, FLUX, S>(a, base + lane);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&a.ctr[1], 1u) == gridDim.x - 1) {
+      a.ctr[0] = 0;
+      a.ctr[1] = 0;
+    }
+  }
 }
 
 // residual on [LO, HI]^2 (zero elsewhere) and the RK stage on every cell
