@@ -137,6 +137,16 @@ cudaError_t launch_dt_cell(const Method &m, const DtArgs &a, int n, cudaStream_t
   return AMR_DISPATCH_NG_S_PDL(m, k_dt_cell, n, 256, 0, s, a);
 }
 
+cudaError_t launch_ic(const Method &m, const IcDev *blocks, int n, const double *tabs, void *U, double *Bi,
+                      double *grad, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (m.ng == 2 && !m.f32) k_ic<2, double><<<n, 256, 0, s>>>(blocks, tabs, static_cast<double *>(U), Bi, grad);
+  else if (m.ng == 2) k_ic<2, float><<<n, 256, 0, s>>>(blocks, tabs, static_cast<float *>(U), Bi, grad);
+  else if (!m.f32) k_ic<4, double><<<n, 256, 0, s>>>(blocks, tabs, static_cast<double *>(U), Bi, grad);
+  else k_ic<4, float><<<n, 256, 0, s>>>(blocks, tabs, static_cast<float *>(U), Bi, grad);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int per = 4 * (m.ng == 2 ? refine_chunks<2>() : refine_chunks<4>());   // (son, chunk) CTAs per op

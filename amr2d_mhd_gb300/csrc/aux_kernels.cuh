@@ -5,6 +5,7 @@
 #include <type_traits>
 
 #include "amr_common.h"
+#include "ic.hpp"
 #include "physics.cuh"
 #include "stage.cuh"
 
@@ -381,6 +382,112 @@ __global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
     }
     a.lambda[blockIdx.x] = mm;
     a.grad[blockIdx.x] = gg;
+  }
+}
+
+// ------------------------------------------------- initial condition (amr_init)
+// IC2Dtype.cpp:6-190 + W2U (meshblock.cpp:181-199) for one root block per CTA:
+// the primitive state of every cell (ghosts included) into shared memory and
+// the conserved state to the block's slot, the face field from the cell
+// averages (IC2Dtype.cpp:172-189), and the block's refinement criterion
+// (criteria.cpp:11-29) for amr_init's first admesh.  Constants and the 1-D
+// profiles that need the C library (sin, exp, cos) come from the host
+// (IcDev, ic_prepare); everything else is evaluated here in the host code's
+// order, without FMA contraction, so the state is the host evaluation's.
+template <int NG, typename S>
+__global__ void __launch_bounds__(256) k_ic(const IcDev *blocks, const double *tabs, S *U, double *Bi, double *grad) {
+  constexpr int N = Geo<NG>::N, NN = N * N;
+  __shared__ double sW[8 * NN];
+  __shared__ double red[8];
+  const IcDev d = blocks[blockIdx.x];
+  const double *t0 = d.tab >= 0 ? tabs + static_cast<size_t>(d.tab) * N : nullptr;
+  S *u = U + static_cast<size_t>(d.slot) * 8 * NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    const double x = ((i + d.icoord_x - NG) + 0.5) * d.dx - d.shift_x;
+    const double y = ((j + d.icoord_y - NG) + 0.5) * d.dy - d.shift_y;
+    double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (d.ic <= IC_BWY1) {  // quadrants, IC2Dtype.cpp:114-168
+      int k;
+      if (x >= 0.5 && y >= 0.5) k = 0;
+      else if (x < 0.5 && y >= 0.5) k = 1;
+      else if (x < 0.5 && y < 0.5) k = 2;
+      else k = 3;
+      w[0] = d.c[k]; w[4] = d.c[4 + k]; w[5] = d.c[8 + k]; w[6] = d.c[12 + k];
+    } else if (d.ic == IC_ROTOR) {  // IC2Dtype.cpp:90-113
+      const double radius = sqrt((x - 0.5) * (x - 0.5) + (y - 0.5) * (y - 0.5));
+      const double fr = (23. - 200. * radius) / 3.;
+      w[4] = 0.5;
+      w[5] = d.c[0];
+      if (radius <= 0.1) {
+        w[0] = 10.; w[1] = -(y - 0.5) / 0.1; w[2] = (x - 0.5) / 0.1;
+      } else if (radius > 0.1 && radius < 0.115) {
+        w[0] = (1 + 9. * fr); w[1] = (-(y - 0.5) * fr / 0.1); w[2] = (x - 0.5) * fr / 0.1;
+      } else {
+        w[0] = 1.;
+      }
+    } else if (d.ic == IC_OT) {
+      const double sx = t0[i], s2x = t0[N + i], sy = t0[2 * N + j];
+      w[0] = d.c[0]; w[4] = d.c[1];
+      w[1] = -sy; w[2] = sx;
+      w[5] = -sy / d.c[2]; w[6] = s2x / d.c[2];
+    } else if (d.ic == IC_BLAST) {
+      const double rr = sqrt((x - d.c[4]) * (x - d.c[4]) + (y - d.c[5]) * (y - d.c[5]));
+      w[0] = 1.0; w[4] = rr < d.c[0] ? d.c[1] : 0.1;
+      w[5] = d.c[2]; w[6] = d.c[3];
+    } else if (d.ic == IC_KH) {
+      const bool in = fabs(y - 0.5) <= 0.25;
+      w[0] = in ? 2.0 : 1.0; w[1] = in ? 0.5 : -0.5; w[4] = 2.5;
+      w[5] = d.c[0];
+      w[2] = t0[i] * t0[N + j];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) sW[k * NN + c] = w[k];
+    // W2U (meshblock.cpp:181-199)
+    const double g = d.gamma;
+    const double e = (w[4] / (g - 1)) + 0.5 * w[0] * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+    const double q[8] = {w[0], w[1] * w[0], w[2] * w[0], w[3] * w[0],
+                         e + 0.5 * (w[5] * w[5] + w[6] * w[6] + w[7] * w[7]), w[5], w[6], w[7]};
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k * NN + c] = static_cast<S>(q[k]);
+  }
+  __syncthreads();
+  // IC2Dtype.cpp:172-189: Bx at i-1/2 from the two cell averages (the first
+  // face takes the second's value), By likewise
+  double *bx = Bi + static_cast<size_t>(d.slot) * 2 * NN, *by = bx + NN;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    const int i = c % N, j = c / N;
+    const int il = i > 0 ? i - 1 : 0, jl = j > 0 ? j - 1 : 0;
+    bx[c] = 0.5 * (sW[5 * NN + j * N + il] + sW[5 * NN + j * N + il + 1]);
+    by[c] = 0.5 * (sW[6 * NN + jl * N + i] + sW[6 * NN + (jl + 1) * N + i]);
+  }
+  // criteria.cpp:11-29 over the interior (one thread per interior cell)
+  static_assert(NI * NI == 256, "one thread per interior cell");
+  const int i = NG + threadIdx.x % NI, j = NG + threadIdx.x / NI, c = j * N + i;
+  double gr = 0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int v = q == 0 ? 4 : (q == 1 ? 0 : q + 3);   // p, rho, Bx, By
+    const double *x = sW + v * NN + c;
+    const double c0 = x[0];
+    const double dm = 1.0E-15 > fabs(c0) ? 1.0E-15 : fabs(c0);
+    double dd = fabs(x[1] - c0);
+    double ee = fabs(x[-1] - c0);
+    dd = dd > ee ? dd : ee;
+    ee = fabs(x[N] - c0);
+    dd = dd > ee ? dd : ee;
+    ee = fabs(x[-N] - c0);
+    dd = dd > ee ? dd : ee;
+    const double r = dd / dm;
+    gr = gr > r ? gr : r;
+  }
+  gr = warp_max(gr);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = gr;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = red[0];
+    for (int q = 1; q < 8; q++) m = m < red[q] ? red[q] : m;
+    grad[blockIdx.x] = m;
   }
 }
 

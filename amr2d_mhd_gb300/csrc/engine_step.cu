@@ -66,9 +66,8 @@ int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
 }
 
 // admesh.cpp:17-102 for the instances in `which`; the criterion comes from the
-// device reduction of the last dt_crit (or, at initialisation, from the IC's
-// primitive state on the host), or the caller's marks replace it (`marks`,
-// one instance).  The refine / coarsen kernels run while the
+// device reduction of the last dt_crit (or, at initialisation, from k_ic's),
+// or the caller's marks replace it (`marks`, one instance).  The refine / coarsen kernels run while the
 // host compiles the changed instances' ghost programs; the device error check
 // (U2W("refine") traps) follows, so errors surface before the call returns.
 int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vector<double>> *host_grad,
@@ -137,34 +136,61 @@ int Engine::admesh_all(const std::vector<int> &which, const std::vector<std::vec
   return check_device_error();  // also keeps `all` alive until the copy is done
 }
 
-// basegrid + IC2Dtype + W2U + initial admesh (main.cpp:97-116)
+// basegrid + IC2Dtype + W2U + initial admesh (main.cpp:97-116).  The root
+// blocks' initial condition, face field and criterion come from k_ic (one
+// launch over the roots of every instance); the host prepares each block's
+// constants and 1-D profiles (ic_prepare) and runs the initial admesh on the
+// criterion.
 int Engine::init() {
   if (initialised_) return fail(AMR_E_STATE, "amr_init called twice");
   if (poisoned_) return fail(AMR_E_STATE, "engine stopped by an earlier error");
-  std::vector<std::vector<double>> grads(inst_.size());
+  std::vector<IcDev> blocks;
+  std::vector<double> tabs;
+  std::vector<std::pair<int, int>> owner;   // (instance, block ID) of each root block
   for (size_t q = 0; q < inst_.size(); q++) {
     Instance &in = inst_[q];
     in.tree.basegrid();
     if (int rc = assign_slots(in)) return rc;
-    const int nr = in.tree.lastActive;
-    std::vector<double> W(static_cast<size_t>(8) * nn_), U(static_cast<size_t>(nr) * 8 * nn_),
-        B(static_cast<size_t>(nr) * 2 * nn_);
-    grads[q].assign(nr, 0.0);
-    for (int nb = 0; nb < nr; nb++) {
+    for (int nb = 0; nb < in.tree.lastActive; nb++) {
       IcBlock b{n_, ng_, in.tree.icoord[nb][0], in.tree.icoord[nb][1], in.dx[0], in.dy[0],
                 in.cfg.geometry == 0 ? in.dx[0] : 0.0, in.cfg.geometry == 0 ? in.dy[0] : 0.0};
-      ic_fill(in.ic, in.cfg.ic_param, b, W.data(), B.data() + static_cast<size_t>(nb) * 2 * nn_);
-      prim_to_cons(W.data(), U.data() + static_cast<size_t>(nb) * 8 * nn_, nn_, in.gamma);
-      grads[q][nb] = criteria_grad(W.data(), n_, ng_);
+      IcDev d;
+      std::vector<double> t(static_cast<size_t>(3) * n_);
+      if (ic_prepare(in.ic, in.cfg.ic_param, b, in.gamma, d, t.data())) {
+        d.tab = static_cast<int>(tabs.size() / n_);
+        tabs.insert(tabs.end(), t.begin(), t.end());
+      }
+      d.slot = in.slot[nb];
+      blocks.push_back(d);
+      owner.emplace_back(static_cast<int>(q), nb);
     }
-    if (int rc = xfer(in, AMR_FIELD_U, U.data(), true)) return rc;
-    if (int rc = xfer(in, AMR_FIELD_BI, B.data(), true)) return rc;
     in.t = 0.0;
     in.dt = 0.0;  // dom.dt is read before its first assignment (main.cpp:154 vs :231)
     in.dtn = 0.0;
     if (in.cfg.dt_fixed > 0) in.dt = in.dtn = in.cfg.dt_fixed;
     in.count = 0;
   }
+  const size_t nb = blocks.size();
+  if (tabs.empty()) tabs.assign(1, 0.0);
+  DevBuf d_blocks, d_tabs;
+  CK(d_blocks.ensure(sizeof(IcDev) * nb), "alloc");
+  CK(d_tabs.ensure(sizeof(double) * tabs.size()), "alloc");
+  CK(d_grad_.ensure(sizeof(double) * nb), "alloc");
+  CK(h_grad_.ensure(sizeof(double) * nb), "alloc");
+  CK(cudaMemcpyAsync(d_blocks.p, blocks.data(), sizeof(IcDev) * nb, cudaMemcpyHostToDevice, stream_), "h2d");
+  CK(cudaMemcpyAsync(d_tabs.p, tabs.data(), sizeof(double) * tabs.size(), cudaMemcpyHostToDevice, stream_), "h2d");
+  CK(launch_ic(m_, d_blocks.as<IcDev>(), static_cast<int>(nb), d_tabs.as<double>(), U_, Bi_, d_grad_.as<double>(),
+               stream_), "initial condition");
+  CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nb, cudaMemcpyDeviceToHost, stream_), "d2h");
+  CK(cudaStreamSynchronize(stream_), "sync");  // also keeps the host arrays alive until the copies ran
+  prof_.launches += 1;
+  prof_.h2d_bytes += static_cast<int64_t>(sizeof(IcDev) * nb + sizeof(double) * tabs.size());
+  prof_.d2h_bytes += static_cast<int64_t>(sizeof(double) * nb);
+  d_blocks.release();
+  d_tabs.release();
+  std::vector<std::vector<double>> grads(inst_.size());
+  for (size_t q = 0; q < inst_.size(); q++) grads[q].assign(inst_[q].tree.lastActive, 0.0);
+  for (size_t k = 0; k < nb; k++) grads[owner[k].first][owner[k].second] = h_grad_.as<double>()[k];
   std::vector<int> all(inst_.size());
   for (size_t q = 0; q < inst_.size(); q++) all[q] = static_cast<int>(q);
   if (int rc = admesh_all(all, &grads)) return rc;

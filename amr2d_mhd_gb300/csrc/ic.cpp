@@ -56,104 +56,67 @@ void ic_params(IcId ic, double &gamma, double &tend) {
   }
 }
 
-void ic_fill(IcId ic, const double *P, const IcBlock &b, double *W, double *Bi) {
-  const int n = b.n, nn = n * n;
+bool ic_prepare(IcId ic, const double *P, const IcBlock &b, double gamma, IcDev &d, double *tab) {
+  const int n = b.n;
+  std::memset(&d, 0, sizeof d);
+  d.ic = ic;
+  d.icoord_x = b.icoord_x;
+  d.icoord_y = b.icoord_y;
+  d.dx = b.dx;
+  d.dy = b.dy;
+  d.shift_x = b.shift_x;
+  d.shift_y = b.shift_y;
+  d.gamma = gamma;
+  d.tab = -1;
   Quad q;
-  const bool quad = quad_states(ic, q);
-  for (int i = 0; i < n; i++) {
-    const double x = ((i + b.icoord_x - b.ng) + 0.5) * b.dx - b.shift_x;
-    for (int j = 0; j < n; j++) {
-      const double y = ((j + b.icoord_y - b.ng) + 0.5) * b.dy - b.shift_y;
-      double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (quad) {
-        int k;
-        if (x >= 0.5 && y >= 0.5) k = 0;
-        else if (x < 0.5 && y >= 0.5) k = 1;
-        else if (x < 0.5 && y < 0.5) k = 2;
-        else k = 3;
-        w[0] = q.r[k]; w[4] = q.p[k]; w[5] = q.bx[k]; w[6] = q.by[k];
-      } else if (ic == IC_ROTOR) {  // IC2Dtype.cpp:90-113
-        const double radius = std::sqrt((x - 0.5) * (x - 0.5) + (y - 0.5) * (y - 0.5));
-        const double fr = (23. - 200. * radius) / 3.;
-        w[4] = 0.5;
-        w[5] = 2.5 / (std::sqrt(4 * kPiRef));
-        if (radius <= 0.1) {
-          w[0] = 10.; w[1] = -(y - 0.5) / 0.1; w[2] = (x - 0.5) / 0.1;
-        } else if (radius > 0.1 && radius < 0.115) {
-          w[0] = (1 + 9. * fr); w[1] = (-(y - 0.5) * fr / 0.1); w[2] = (x - 0.5) * fr / 0.1;
-        } else {
-          w[0] = 1.;
-        }
-      } else if (ic == IC_OT) {  // Orszag-Tang on [0, 2 pi]^2
-        const double s4p = std::sqrt(4.0 * kPi);
-        w[0] = 25.0 / (36.0 * kPi); w[4] = 5.0 / (12.0 * kPi);
-        w[1] = -std::sin(y); w[2] = std::sin(x);
-        w[5] = -std::sin(y) / s4p; w[6] = std::sin(2.0 * x) / s4p;
-      } else if (ic == IC_BLAST) {  // P: r0, p_in, |B|, theta, xc, yc
-        const double rr = std::sqrt((x - P[4]) * (x - P[4]) + (y - P[5]) * (y - P[5]));
-        w[0] = 1.0; w[4] = rr < P[0] ? P[1] : 0.1;
-        w[5] = P[2] * std::cos(P[3]); w[6] = P[2] * std::sin(P[3]);
-      } else if (ic == IC_KH) {  // P: a_1..a_16
-        const bool in = std::fabs(y - 0.5) <= 0.25;
-        w[0] = in ? 2.0 : 1.0; w[1] = in ? 0.5 : -0.5; w[4] = 2.5;
-        w[5] = 0.1 / std::sqrt(4.0 * kPi);
-        const double env = std::exp(-(y - 0.25) * (y - 0.25) / 0.01) +
-                           std::exp(-(y - 0.75) * (y - 0.75) / 0.01);
+  if (quad_states(ic, q)) {  // IC2Dtype.cpp:20-68
+    for (int k = 0; k < 4; k++) {
+      d.c[k] = q.r[k];
+      d.c[4 + k] = q.p[k];
+      d.c[8 + k] = q.bx[k];
+      d.c[12 + k] = q.by[k];
+    }
+    return false;
+  }
+  // the cell centres, as the kernel forms them
+  auto X = [&](int i) { return ((i + b.icoord_x - b.ng) + 0.5) * b.dx - b.shift_x; };
+  auto Y = [&](int j) { return ((j + b.icoord_y - b.ng) + 0.5) * b.dy - b.shift_y; };
+  switch (ic) {
+    case IC_ROTOR:  // IC2Dtype.cpp:80
+      d.c[0] = 2.5 / (std::sqrt(4 * kPiRef));
+      return false;
+    case IC_OT:  // Orszag-Tang on [0, 2 pi]^2
+      d.c[0] = 25.0 / (36.0 * kPi);
+      d.c[1] = 5.0 / (12.0 * kPi);
+      d.c[2] = std::sqrt(4.0 * kPi);
+      for (int i = 0; i < n; i++) {
+        tab[i] = std::sin(X(i));
+        tab[n + i] = std::sin(2.0 * X(i));
+        tab[2 * n + i] = std::sin(Y(i));
+      }
+      return true;
+    case IC_BLAST:  // P: r0, p_in, |B|, theta, xc, yc
+      d.c[0] = P[0];
+      d.c[1] = P[1];
+      d.c[2] = P[2] * std::cos(P[3]);
+      d.c[3] = P[2] * std::sin(P[3]);
+      d.c[4] = P[4];
+      d.c[5] = P[5];
+      return false;
+    case IC_KH:  // P: a_1..a_16
+      d.c[0] = 0.1 / std::sqrt(4.0 * kPi);
+      for (int i = 0; i < n; i++) {
+        const double x = X(i), y = Y(i);
         double v = 0.0;
         for (int k = 0; k < 16; k++) v += P[k] * std::sin(2.0 * kPi * (k + 1) * x);
-        w[2] = v * env;
+        tab[i] = v;
+        tab[n + i] = std::exp(-(y - 0.25) * (y - 0.25) / 0.01) + std::exp(-(y - 0.75) * (y - 0.75) / 0.01);
+        tab[2 * n + i] = 0.0;
       }
-      for (int k = 0; k < 8; k++) W[k * nn + j * n + i] = w[k];
-    }
+      return true;
+    default:
+      return false;
   }
-  // IC2Dtype.cpp:172-189
-  double *Bx = Bi, *By = Bi + nn;
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) {
-      if (i < n - 1) Bx[j * n + i + 1] = 0.5 * (W[5 * nn + j * n + i] + W[5 * nn + j * n + i + 1]);
-      else Bx[j * n + 0] = Bx[j * n + 1];
-      if (j < n - 1) By[(j + 1) * n + i] = 0.5 * (W[6 * nn + j * n + i] + W[6 * nn + (j + 1) * n + i]);
-      else By[0 * n + i] = By[1 * n + i];
-    }
-}
-
-void prim_to_cons(const double *W, double *U, int nn, double g) {
-  for (int c = 0; c < nn; c++) {
-    double w[8];
-    for (int k = 0; k < 8; k++) w[k] = W[k * nn + c];
-    U[0 * nn + c] = w[0];
-    U[1 * nn + c] = w[1] * w[0];
-    U[2 * nn + c] = w[2] * w[0];
-    U[3 * nn + c] = w[3] * w[0];
-    const double e = (w[4] / (g - 1)) + 0.5 * w[0] * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
-    U[4 * nn + c] = e + 0.5 * (w[5] * w[5] + w[6] * w[6] + w[7] * w[7]);
-    U[5 * nn + c] = w[5];
-    U[6 * nn + c] = w[6];
-    U[7 * nn + c] = w[7];
-  }
-}
-
-double criteria_grad(const double *W, int n, int ng) {
-  const int nn = n * n;
-  static const int var[4] = {4, 0, 5, 6};
-  double grad = 0;
-  for (int i = ng; i <= n - 1 - ng; i++)
-    for (int j = ng; j <= n - 1 - ng; j++)
-      for (int q = 0; q < 4; q++) {
-        const double *w = W + var[q] * nn;
-        const double c0 = w[j * n + i];
-        const double dm = 1.0E-15 > std::fabs(c0) ? 1.0E-15 : std::fabs(c0);
-        double d = std::fabs(w[j * n + i + 1] - c0);
-        double e = std::fabs(w[j * n + i - 1] - c0);
-        d = d > e ? d : e;
-        e = std::fabs(w[(j + 1) * n + i] - c0);
-        d = d > e ? d : e;
-        e = std::fabs(w[(j - 1) * n + i] - c0);
-        d = d > e ? d : e;
-        const double r = d / dm;
-        grad = grad > r ? grad : r;
-      }
-  return grad;
 }
 
 }  // namespace amr

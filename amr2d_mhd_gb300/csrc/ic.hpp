@@ -1,6 +1,6 @@
-// Initial conditions (IC2Dtype.cpp) evaluated on the host for the root blocks,
-// plus the extension problems.  Not on the hot path: the result is uploaded
-// once by amr_init.
+// Initial conditions (IC2Dtype.cpp) for the root blocks, plus the extension
+// problems: the host prepares each block's constants and 1-D profiles, the
+// device kernel k_ic (aux_kernels.cuh) fills the cells.
 #pragma once
 
 #include <string>
@@ -23,16 +23,31 @@ struct IcBlock {
   double shift_x, shift_y;  // subtracted from cell centres (dx[0] in the reference geometry)
 };
 
-// Primitive state W[8][n][n] (all cells, ghosts included) and face field
-// Bi[2][n][n] from the cell averages (IC2Dtype.cpp:172-189).
-void ic_fill(IcId ic, const double *ic_param, const IcBlock &b, double *W, double *Bi);
+// One block of amr_init's initial condition as the device generator k_ic
+// takes it.  The host fills what needs the C library's transcendental
+// functions (IC2Dtype.cpp's sqrt(4 pi) constants, the blast field's cos /
+// sin, the Orszag-Tang and Kelvin-Helmholtz profiles): every such function
+// depends on x alone or on y alone, so the host evaluates it on the n cell
+// centres of each direction (`tab`, three rows of n) and the device builds
+// the n x n cells from those rows with the same arithmetic as before; the
+// result is bit for bit the host evaluation's.
+struct IcDev {
+  int ic;                 // IcId
+  int slot;               // physical slot of the block
+  int icoord_x, icoord_y;
+  double dx, dy, shift_x, shift_y;
+  double gamma;
+  double c[16];           // per IC: quadrant states r[4] p[4] bx[4] by[4] (SST*, BW*); rotor: c[0] =
+                          // 2.5/sqrt(4 pi); OT: c[0] = rho, c[1] = p, c[2] = sqrt(4 pi); blast: r0, p_in,
+                          // |B| cos(theta), |B| sin(theta), xc, yc; KH: c[0] = 0.1/sqrt(4 pi)
+  int tab;                // first of this block's three table rows, -1 if none
+  int pad;
+};
 
-// W2U (meshblock.cpp:181-199) of one block, [8][n][n] arrays
-void prim_to_cons(const double *W, double *U, int ncell, double gamma);
-
-// max over interior cells of criteria.cpp:11-29 (relative jumps of p, rho,
-// Bx, By) of one block given its primitive state
-double criteria_grad(const double *W, int n, int ng);
+// The IcDev and table rows [3][n] of one block: OT sin(x_i), sin(2 x_i),
+// sin(y_j); KH the perturbation sum over k of a_k sin(2 pi k x_i), its
+// envelope at y_j, unused.  Returns true if the block has table rows.
+bool ic_prepare(IcId ic, const double *ic_param, const IcBlock &b, double gamma, IcDev &d, double *tab);
 
 }  // namespace amr
 

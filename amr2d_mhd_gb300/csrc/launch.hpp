@@ -83,6 +83,10 @@ cudaError_t launch_diffuse(const Method &m, const CtArgs &a, int ntasks, cudaStr
 // per-leaf max wave speed and refinement criterion from the primitive state
 cudaError_t launch_dt_cell(const Method &m, const DtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_refine(const Method &m, const TreeOpArgs &a, int nops, cudaStream_t s);
+// initial condition of n root blocks (IC2Dtype.cpp + W2U), their face field and criterion
+struct IcDev;
+cudaError_t launch_ic(const Method &m, const IcDev *blocks, int n, const double *tabs, void *U, double *Bi,
+                      double *grad, cudaStream_t s);
 cudaError_t launch_coarsen(const Method &m, const TreeOpArgs &a, int nops, cudaStream_t s);
 
 cudaError_t launch_gather(const int *slots, int nblk, const void *src, int f32, int per, double *dst,
