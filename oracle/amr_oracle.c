@@ -374,16 +374,87 @@ static int hlld(const double *wL, const double *wR, double gamma, double *flux) 
   return 0;
 }
 
-/* riemannS.cpp:7-56: rotate y faces, dispatch, rotate back.  ROE is
- * rejected with a magnetic field (riemannS.cpp:39-40; MAG_field is always
- * true, defs.hpp:32). */
-int oracle_riemann(int fluxm, const double *wL, const double *wR, double gamma, int dir_y,
-                   double *out) {
+/* riemannS.cpp:297-395, the hydrodynamic Roe solver (Toro, p. 376); the
+ * normal is x (xnorm = 1, ynorm = 0, written out as the reference does) and
+ * the field enters the physical fluxes only.  (gamma-1)/pow(a,2) as the
+ * reference writes it (:366). */
+static int roe(const double *wL, const double *wR, double gamma, double *flux) {
+  const double xnorm = 1.0, ynorm = 0.0;
+  double vnL = wL[1] * xnorm + wL[2] * ynorm, BnL = wL[5] * xnorm + wL[6] * ynorm;
+  double eL = (wL[4] / (wL[0] * (gamma - 1))) + 0.5 * (wL[1] * wL[1] + wL[2] * wL[2] + wL[3] * wL[3]) +
+              0.5 * (wL[5] * wL[5] + wL[6] * wL[6] + wL[7] * wL[7]) / wL[0];
+  eL = eL * wL[0];
+  double HL = (eL + wL[4] + 0.5 * (wL[5] * wL[5] + wL[6] * wL[6] + wL[7] * wL[7])) / wL[0];
+  double qL[8], qR[8], FL[8], FR[8];
+  for (int k = 0; k < 8; k++) { qL[k] = wL[k]; qR[k] = wR[k]; }
+  qL[1] = wL[0] * wL[1]; qL[2] = wL[0] * wL[2]; qL[3] = wL[0] * wL[3]; qL[4] = eL;
+  double vnR = wR[1] * xnorm + wR[2] * ynorm, BnR = wR[5] * xnorm + wR[6] * ynorm;
+  double eR = (wR[4] / (wR[0] * (gamma - 1))) + 0.5 * (wR[1] * wR[1] + wR[2] * wR[2] + wR[3] * wR[3]) +
+              0.5 * (wR[5] * wR[5] + wR[6] * wR[6] + wR[7] * wR[7]) / wR[0];
+  eR = eR * wR[0];
+  double HR = (eR + wR[4] + 0.5 * (wR[5] * wR[5] + wR[6] * wR[6] + wR[7] * wR[7])) / wR[0];
+  qR[1] = wR[0] * wR[1]; qR[2] = wR[0] * wR[2]; qR[3] = wR[0] * wR[3]; qR[4] = eR;
+  /* 1) Roe averages */
+  double RT = sqrt(wR[0] / wL[0]);
+  double u = (wL[1] + RT * wR[1]) / (1 + RT);
+  double v = (wL[2] + RT * wR[2]) / (1 + RT);
+  double w = (wL[3] + RT * wR[3]) / (1 + RT);
+  double H = (HL + RT * HR) / (1 + RT);
+  double a = sqrt((gamma - 1) * (H - 0.5 * (u * u + v * v + w * w)));
+  /* 2) eigenvalues, 3) right eigenvectors */
+  double lambda[5] = {u - a, u, u, u, u + a};
+  double K[5][8] = {{1., u - a, v, w, H - u * a, 0., 0., 0.},
+                    {1., u, v, w, 0.5 * (u * u + v * v + w * w), 0., 0., 0.},
+                    {0., 0., 1., 0., v, 0., 0., 0.},
+                    {0., 0., 0., 1., w, 0., 0., 0.},
+                    {1., u + a, v, w, H + u * a, 0., 0., 0.}};
+  /* 4) wave strengths */
+  double alpha[5];
+  alpha[2] = (qR[2] - qL[2]) - v * (qR[0] - qL[0]);
+  alpha[3] = (qR[3] - qL[3]) - w * (qR[0] - qL[0]);
+  double du5bar = (qR[4] - qL[4]) - (alpha[2]) * v - (alpha[3]) * w;
+  alpha[1] = ((gamma - 1) / pow(a, 2)) * ((qR[0] - qL[0]) * (H - u * u) + u * (qR[1] - qL[1]) - du5bar);
+  alpha[0] = 0.5 * (1 / a) * ((qR[0] - qL[0]) * (u + a) - (qR[1] - qL[1]) - a * alpha[1]);
+  alpha[4] = (qR[0] - qL[0]) - (alpha[0] + alpha[1]);
+  /* 5) physical fluxes and the Roe flux */
+  double ptL = wL[4] + 0.5 * (wL[5] * wL[5] + wL[6] * wL[6] + wL[7] * wL[7]);
+  FL[0] = wL[0] * vnL;
+  FL[1] = wL[0] * vnL * wL[1] + xnorm * ptL - BnL * wL[5];
+  FL[2] = wL[0] * vnL * wL[2] + ynorm * ptL - BnL * wL[6];
+  FL[3] = wL[0] * vnL * wL[3] - BnL * wL[7];
+  FL[4] = wL[0] * vnL * HL - BnL * (wL[1] * wL[5] + wL[2] * wL[6] + wL[3] * wL[7]);
+  FL[5] = vnL * wL[5] - BnL * wL[1];
+  FL[6] = vnL * wL[6] - BnL * wL[2];
+  FL[7] = vnL * wL[7] - BnL * wL[3];
+  double ptR = wR[4] + 0.5 * (wR[5] * wR[5] + wR[6] * wR[6] + wR[7] * wR[7]);
+  FR[0] = wR[0] * vnR;
+  FR[1] = wR[0] * vnR * wR[1] + xnorm * ptR - BnR * wR[5];
+  FR[2] = wR[0] * vnR * wR[2] + ynorm * ptR - BnR * wR[6];
+  FR[3] = wR[0] * vnR * wR[3] - BnR * wR[7];
+  FR[4] = wR[0] * vnR * HR - BnR * (wR[1] * wR[5] + wR[2] * wR[6] + wR[3] * wR[7]);
+  FR[5] = vnR * wR[5] - BnR * wR[1];
+  FR[6] = vnR * wR[6] - BnR * wR[2];
+  FR[7] = vnR * wR[7] - BnR * wR[3];
+  for (int k = 0; k < 8; k++) {
+    double summ = 0.;
+    for (int j = 0; j < 5; j++) summ += alpha[j] * fabs(lambda[j]) * K[j][k];
+    flux[k] = 0.5 * (FL[k] + FR[k]) - 0.5 * summ;
+  }
+  return 0;
+}
+
+/* riemannS.cpp:7-56: rotate y faces (the field components only with
+ * MAG_field, :18,51), dispatch, rotate back.  ROE is rejected with a
+ * magnetic field (riemannS.cpp:39-40); the time loop always runs with
+ * MAG_field (defs.hpp:32), the hydrodynamic configuration is reachable here
+ * through mag_field = 0. */
+int oracle_riemann_mf(int fluxm, const double *wL, const double *wR, double gamma, int dir_y, int mag_field,
+                      double *out) {
   double l[8], r[8], f[8] = {0};
   for (int k = 0; k < 8; k++) { l[k] = wL[k]; r[k] = wR[k]; }
   if (dir_y) {
     l[1] = wL[2]; l[2] = wL[1]; r[1] = wR[2]; r[2] = wR[1];
-    l[5] = wL[6]; l[6] = wL[5]; r[5] = wR[6]; r[6] = wR[5];
+    if (mag_field) { l[5] = wL[6]; l[6] = wL[5]; r[5] = wR[6]; r[6] = wR[5]; }
   }
   int rc;
   switch (fluxm) {
@@ -391,15 +462,23 @@ int oracle_riemann(int fluxm, const double *wL, const double *wR, double gamma, 
     case OR_FLUX_HLLE: rc = hlle(l, r, gamma, f); break;
     case OR_FLUX_HLLC: rc = hllc(l, r, gamma, f); break;
     case OR_FLUX_HLLD: rc = hlld(l, r, gamma, f); break;
+    case OR_FLUX_ROE:
+      if (mag_field) return -4;
+      rc = roe(l, r, gamma, f);
+      break;
     default: return -4;
   }
   if (rc) return rc;
   for (int k = 0; k < 8; k++) out[k] = f[k];
   if (dir_y) {
     out[1] = f[2]; out[2] = f[1];
-    out[5] = f[6]; out[6] = f[5];
+    if (mag_field) { out[5] = f[6]; out[6] = f[5]; }
   }
   return 0;
+}
+
+int oracle_riemann(int fluxm, const double *wL, const double *wR, double gamma, int dir_y, double *out) {
+  return oracle_riemann_mf(fluxm, wL, wR, gamma, dir_y, 1, out);
 }
 
 /* ---------------------------------------------------------- meshblock.cpp */

@@ -84,6 +84,10 @@ int oracle_fill(oracle *o, double *field, int nv, int kind);
 double oracle_slopelimiter(int limiter, double r, double eta);
 int oracle_riemann(int flux, const double *wL, const double *wR, double gamma, int dir_y,
                    double *out);
+/* the same with the reference's compile-time MAG_field (defs.hpp:32) as an
+ * argument: 0 is its hydrodynamic configuration, where ROE runs */
+int oracle_riemann_mf(int flux, const double *wL, const double *wR, double gamma, int dir_y, int mag_field,
+                      double *out);
 void oracle_wavespeeds(const double *w, double gamma, int norm, double *out4);
 
 #ifdef __cplusplus

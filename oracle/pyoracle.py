@@ -85,6 +85,8 @@ def lib():
         L.oracle_slopelimiter.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.oracle_riemann.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_riemann_mf.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.oracle_wavespeeds.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_void_p]
     return _lib
@@ -202,12 +204,14 @@ def slopelimiter(limiter, r, eta=0.0):
     return lib().oracle_slopelimiter(LIMITERS.index(limiter), r, eta)
 
 
-def riemann(flux, wL, wR, gamma, dir_y=False):
+def riemann(flux, wL, wR, gamma, dir_y=False, mag_field=True):
+    """riemannS.cpp:7-56; mag_field = the reference's compile-time MAG_field
+    (defs.hpp:32), False for its hydrodynamic configuration (where ROE runs)."""
     a = np.ascontiguousarray(wL, np.float64)
     b = np.ascontiguousarray(wR, np.float64)
     out = np.zeros(8)
-    rc = lib().oracle_riemann(FLUXES.index(flux), a.ctypes.data, b.ctypes.data, gamma,
-                              int(dir_y), out.ctypes.data)
+    rc = lib().oracle_riemann_mf(FLUXES.index(flux), a.ctypes.data, b.ctypes.data, gamma,
+                                 int(dir_y), int(bool(mag_field)), out.ctypes.data)
     if rc != 0:
         raise OracleError("riemann rc=%d" % rc)
     return out

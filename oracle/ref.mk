@@ -16,8 +16,9 @@
 #   make -f oracle/ref.mk REF=<src> MAXLEVS=4 FLAVOR=omp       # same as shipped + USE_OMP
 #   make -f oracle/ref.mk REF=<src> MAXLEVS=4 FLAVOR=nofma CTTYPE=2 DIFFUSION=true
 #   make -f oracle/ref.mk REF=<src> MAXLEVS=5 FLAVOR=nofma ROTOR_G53=1
+#   make -f oracle/ref.mk REF=<src> FLAVOR=nofma MAGFIELD=false kat
 #
-# The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>[_CT2][_DIFF][_RG53]/main.x;
+# The result is oracle/_ref/L<MAXLEVS>_G<NGHOSTS>_<FLAVOR>[_CT2][_DIFF][_RG53][_HYDRO]/main.x;
 # run it in a directory holding input.txt with stdin "2\n0\n" (main.cpp:75,275).
 # The omp flavour is for timing only: its dt loop (main.cpp:215-223) updates
 # the shared lambda1 / lambda2 from every thread without a reduction.
@@ -36,8 +37,11 @@ CTTYPE    ?= 1
 DIFFUSION ?= false
 # 1: the rotor IC with gamma = 5/3 instead of the reference's 1.4
 ROTOR_G53 ?= 0
+# MAG_field (defs.hpp:32): false builds the reference's hydrodynamic
+# configuration, the only one in which riemannS reaches ROE (riemannS.cpp:39)
+MAGFIELD ?= true
 HERE    := $(dir $(lastword $(MAKEFILE_LIST)))
-VARIANT := $(if $(filter-out 1,$(CTTYPE)),_CT$(CTTYPE))$(if $(filter true,$(DIFFUSION)),_DIFF)$(if $(filter 1,$(ROTOR_G53)),_RG53)
+VARIANT := $(if $(filter-out 1,$(CTTYPE)),_CT$(CTTYPE))$(if $(filter true,$(DIFFUSION)),_DIFF)$(if $(filter 1,$(ROTOR_G53)),_RG53)$(if $(filter false,$(MAGFIELD)),_HYDRO)
 OUT     := $(HERE)_ref/L$(MAXLEVS)_G$(NGHOSTS)_$(FLAVOR)$(VARIANT)
 
 CXX     ?= g++
@@ -78,11 +82,13 @@ $(OUT)/defs.hpp: $(REF)/defs.hpp
 	sed -e 's/^const int maxlevs=5;/const int maxlevs=$(MAXLEVS);/' \
 	    -e 's/^const int nghosts=2; /const int nghosts=$(NGHOSTS); /' \
 	    -e 's/^const int CTtype=1;/const int CTtype=$(CTTYPE);/' \
-	    -e 's/^const bool diffusion=false;/const bool diffusion=$(DIFFUSION);/' $< > $@
+	    -e 's/^const bool diffusion=false;/const bool diffusion=$(DIFFUSION);/' \
+	    -e 's/^const bool MAG_field=true;/const bool MAG_field=$(MAGFIELD);/' $< > $@
 	@grep -q 'const int maxlevs=$(MAXLEVS);' $@ || (echo "maxlevs patch failed" && rm -f $@ && false)
 	@grep -q 'const int nghosts=$(NGHOSTS); ' $@ || (echo "nghosts patch failed" && rm -f $@ && false)
 	@grep -q 'const int CTtype=$(CTTYPE);' $@ || (echo "CTtype patch failed" && rm -f $@ && false)
 	@grep -q 'const bool diffusion=$(DIFFUSION);' $@ || (echo "diffusion patch failed" && rm -f $@ && false)
+	@grep -q 'const bool MAG_field=$(MAGFIELD);' $@ || (echo "MAG_field patch failed" && rm -f $@ && false)
 
 # the rotor branch of IC2Dtype.cpp (between IC=="rotor" and its tEnd) with
 # gamma = 5/3; exactly one line changes

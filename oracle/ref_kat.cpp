@@ -3,7 +3,7 @@
 // Known-answer harness linked with the reference's own riemannS.o, misc.o and
 // slopelimiter.o (oracle/ref.mk target `kat`).  Reads cases from a binary file
 // and writes the reference's answers:
-//   riemann case:  i32 flux (0 RUSA 1 HLLE 2 HLLC 3 HLLD), i32 dir (0 x, 1 y),
+//   riemann case:  i32 flux (0 RUSA 1 HLLE 2 HLLC 3 HLLD 4 ROE), i32 dir (0 x, 1 y),
 //                  f64 gamma, f64 wL[8], f64 wR[8]  ->  i32 status, f64 flux[8]
 //   limiter case:  i32 limiter (index into kLim), f64 r, f64 eta  ->  f64 phi
 // Usage: kat.x riemann|limiter <in> <out>
@@ -23,7 +23,7 @@ int main(int argc, char **argv) {
   FILE *in = std::fopen(argv[2], "rb");
   FILE *out = std::fopen(argv[3], "wb");
   if (!in || !out) return 3;
-  static const char *kFlux[] = {"RUSA", "HLLE", "HLLC", "HLLD"};
+  static const char *kFlux[] = {"RUSA", "HLLE", "HLLC", "HLLD", "ROE"};
   static const char *kLim[] = {"1st", "noSL", "minmod", "VanLeer", "Superbee", "MC", "Koren", "Cada3rd"};
   if (!std::strcmp(argv[1], "riemann")) {
     int32_t fl, dir;

@@ -11,6 +11,9 @@ reproduce them exactly) and records
   state_<name>.npz  one full state (lp, icoord, leafs, U, Bi) of a small run;
   kat_riemann.npz   riemannS() answers for seeded left / right states;
   kat_limiter.npz   slopelimiter() answers;
+  kat_riemann_hydro.npz  riemannS() answers of the reference built with
+                    MAG_field = false (defs.hpp:32), every solver including
+                    ROE (riemannS.cpp:297-395), which only that build reaches;
   long_<name>.npz   a run to its end time: t, dt and leaf counts of every
                     step, fingerprints every `every` steps and of the last
                     step (the bench's rotor, gamma 5/3, built with
@@ -162,6 +165,39 @@ def make_kat_riemann():
     print("kat_riemann", len(cases), "cases,", int(out["st"].sum()), "throw")
 
 
+def make_kat_riemann_hydro():
+    rng = np.random.default_rng(20261204)
+    cases = []
+    for fl in range(5):
+        for d in range(2):
+            n = 64
+            wL, wR = _states(rng, n), _states(rng, n)
+            wL[:, 5:8] = 0.0       # no field in the hydrodynamic configuration (meshblock.cpp:13)
+            wR[:, 5:8] = 0.0
+            wR[n // 2: n // 2 + 4] = wL[n // 2: n // 2 + 4]  # identical states
+            g = rng.choice([1.4, 5.0 / 3.0, 2.0], n)
+            for q in range(n):
+                cases.append((fl, d, g[q], wL[q], wR[q]))
+    subprocess.check_call(["make", "-s", "-f", os.path.join(REPO, "oracle", "ref.mk"), "REF=" + ref_runner.ref_dir(),
+                           "MAXLEVS=5", "NGHOSTS=2", "FLAVOR=nofma", "MAGFIELD=false", "kat"], cwd=REPO,
+                          stderr=subprocess.DEVNULL)
+    exe = os.path.join(REPO, "oracle", "_ref", "L5_G2_nofma_HYDRO", "kat.x")
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in"), os.path.join(td, "out")
+        with open(fin, "wb") as f:
+            for fl, d, g, a, b in cases:
+                f.write(struct.pack("<iid", fl, d, g) + a.astype("<f8").tobytes() + b.astype("<f8").tobytes())
+        subprocess.check_call([exe, "riemann", fin, fout])
+        raw = open(fout, "rb").read()
+    rec = np.dtype([("st", "<i4"), ("f", "<f8", 8)])
+    out = np.frombuffer(raw, rec)
+    np.savez_compressed(os.path.join(HERE, "kat_riemann_hydro.npz"),
+                        flux=np.array([c[0] for c in cases], np.int32), dir=np.array([c[1] for c in cases], np.int32),
+                        gamma=np.array([c[2] for c in cases]), wL=np.array([c[3] for c in cases]),
+                        wR=np.array([c[4] for c in cases]), status=out["st"].copy(), out=out["f"].copy())
+    print("kat_riemann_hydro", len(cases), "cases,", int(out["st"].sum()), "throw")
+
+
 def make_kat_limiter():
     r = np.concatenate([np.linspace(-3, 5, 161), [0.0, -0.0, 1.0, 2.0, 0.5, 1e-18, -1e-18, 1e6, -1e6, 3.0]])
     eta = [0.0, 0.5, 1.0 - 2e-15, 1.0 - 5e-16, 1.0, 1.0 + 5e-16, 1.0 + 2e-15, 3.0]
@@ -188,6 +224,9 @@ if __name__ == "__main__":
         if nm == "kat":
             make_kat_riemann()
             make_kat_limiter()
+            make_kat_riemann_hydro()
+        elif nm == "kat_hydro":
+            make_kat_riemann_hydro()
         elif nm in STATES:
             make_state(nm)
         elif nm in LONG:

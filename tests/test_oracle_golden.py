@@ -64,3 +64,16 @@ def test_run_fingerprints(name):
         assert st["t"] == d["t"][s] and st["dt"] == d["dt"][s], s
         assert tree_hash(st) == d["tree"][s], s
         assert leaf_hash(st) == d["leaf"][s], s
+
+
+def test_kat_riemann_hydro():
+    """riemannS of the reference built without a magnetic field (MAG_field =
+    false, defs.hpp:32), where ROE (riemannS.cpp:297-395) runs: the oracle's
+    restatement, bit for bit, every solver."""
+    d = np.load(os.path.join(GOLDEN, "kat_riemann_hydro.npz"))
+    assert set(d["flux"]) == {0, 1, 2, 3, 4}
+    for q in range(len(d["flux"])):
+        assert d["status"][q] == 0
+        got = P.riemann(P.FLUXES[d["flux"][q]], d["wL"][q], d["wR"][q], d["gamma"][q], bool(d["dir"][q]),
+                        mag_field=False)
+        assert np.array_equal(got.view(np.int64), d["out"][q].view(np.int64)), q
