@@ -29,7 +29,7 @@ EXPORTS = ["amr_config_default", "amr_config_from_input", "amr_config_blast", "a
            "amr_create", "amr_create_batch", "amr_destroy", "amr_set_stream", "amr_last_error",
            "amr_init", "amr_step", "amr_step_begin", "amr_step_end", "amr_run", "amr_get_info", "amr_locate_bounds", "amr_boundary",
            "amr_muscl2d_rk", "amr_ct2d", "amr_cfl_dt", "amr_admesh", "amr_get_tree", "amr_set_tree", "amr_download",
-           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_criteria", "amr_criteria_flags", "amr_admesh_marked", "amr_set_remesh", "amr_autotune", "amr_save4py",
+           "amr_upload", "amr_profile_enable", "amr_profile_read", "amr_cfl_dt_static", "amr_riemann", "amr_criteria", "amr_criteria_flags", "amr_admesh_marked", "amr_set_remesh", "amr_autotune", "amr_save4py",
            "amr_checkpoint_save", "amr_checkpoint_load", "amr_adjoint_enable",
            "amr_adjoint_seed", "amr_adjoint_step", "amr_adjoint_read", "amr_adjoint_recorded"]
 
@@ -116,6 +116,7 @@ def load(build_if_missing: bool = True):
         "amr_set_remesh": (ctypes.c_int, [vp, i32]),
         "amr_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(Profile)]),
         "amr_cfl_dt_static": (ctypes.c_int, [dp, i32, i32, dp, ctypes.c_double, dp, vp]),
+        "amr_riemann": (ctypes.c_int, [i32, i32, i32, ctypes.c_double, dp, dp, dp, vp, ctypes.c_int64]),
         "amr_criteria": (ctypes.c_int, [vp, dp, i32]),
         "amr_criteria_flags": (ctypes.c_int, [vp, dp, dp, i32]),
         "amr_admesh_marked": (ctypes.c_int, [vp, dp, dp, i32]),
@@ -175,6 +176,24 @@ def blast_config(seed, index, precision="fp64") -> Config:
         raise AmrError(rc, "amr_config_blast")
     c.precision = {"fp64": 0, "fp32": 1}[precision]
     return c
+
+
+def riemann(flux, wL, wR, gamma, dir_y=False, mag_field=True):
+    """riemannS (riemannS.cpp:7-56) on the GPU (amr_riemann) for arrays of
+    face states wL, wR [n, 8]; returns (fluxes [n, 8], status [n])."""
+    wL = np.ascontiguousarray(np.atleast_2d(wL), np.float64)
+    wR = np.ascontiguousarray(np.atleast_2d(wR), np.float64)
+    if wL.shape != wR.shape or wL.shape[1] != 8:
+        raise ValueError("wL, wR: [n, 8] arrays of the same shape")
+    out = np.zeros_like(wL)
+    st = np.zeros(len(wL), np.int32)
+    names = ["RUSA", "HLLE", "HLLC", "HLLD", "ROE"]
+    fl = names.index(flux) if isinstance(flux, str) else int(flux)
+    rc = load().amr_riemann(fl, int(bool(dir_y)), int(bool(mag_field)), float(gamma), wL.ctypes.data,
+                            wR.ctypes.data, out.ctypes.data, st.ctypes.data, len(wL))
+    if rc:
+        raise AmrError(rc, "amr_riemann")
+    return out, st
 
 
 def kh_config(seed, precision="fp64") -> Config:

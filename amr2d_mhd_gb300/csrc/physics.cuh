@@ -420,11 +420,86 @@ __device__ __forceinline__ int flux_hlld(const T *wL, const T *wR, T gamma, T *f
   return 0;
 }
 
+// riemannS.cpp:297-395: the hydrodynamic Roe solver (Toro's, "not suited
+// for MHD"), which riemannS only reaches in the reference's configuration
+// without a magnetic field (riemannS.cpp:39-40).  The normal is x (xnorm = 1,
+// ynorm = 0, written out as the reference does; a field enters only the
+// physical fluxes).  The reference's (gamma-1)/pow(a,2) is (gamma-1)/(a*a)
+// here, the correctly rounded square; the C library's pow rounds a few in a
+// thousand squares differently, so this solver matches the reference to a
+// few ulp rather than bit for bit.
+template <typename T>
+__device__ __forceinline__ int flux_roe(const T *wL, const T *wR, T gamma, T *flux) {
+  const T xnorm = T(1.0), ynorm = T(0.0);
+  const T vnL = wL[1] * xnorm + wL[2] * ynorm, BnL = wL[5] * xnorm + wL[6] * ynorm;
+  T eL = (wL[4] / (wL[0] * (gamma - T(1)))) + T(0.5) * (wL[1] * wL[1] + wL[2] * wL[2] + wL[3] * wL[3]) +
+         T(0.5) * (wL[5] * wL[5] + wL[6] * wL[6] + wL[7] * wL[7]) / wL[0];
+  eL = eL * wL[0];
+  const T HL = (eL + wL[4] + T(0.5) * (wL[5] * wL[5] + wL[6] * wL[6] + wL[7] * wL[7])) / wL[0];
+  const T vnR = wR[1] * xnorm + wR[2] * ynorm, BnR = wR[5] * xnorm + wR[6] * ynorm;
+  T eR = (wR[4] / (wR[0] * (gamma - T(1)))) + T(0.5) * (wR[1] * wR[1] + wR[2] * wR[2] + wR[3] * wR[3]) +
+         T(0.5) * (wR[5] * wR[5] + wR[6] * wR[6] + wR[7] * wR[7]) / wR[0];
+  eR = eR * wR[0];
+  const T HR = (eR + wR[4] + T(0.5) * (wR[5] * wR[5] + wR[6] * wR[6] + wR[7] * wR[7])) / wR[0];
+  const T qL[5] = {wL[0], wL[0] * wL[1], wL[0] * wL[2], wL[0] * wL[3], eL};
+  const T qR[5] = {wR[0], wR[0] * wR[1], wR[0] * wR[2], wR[0] * wR[3], eR};
+  // Roe averages, eigenvalues, right eigenvectors (rows K[j], columns 0..4;
+  // the field columns are zero)
+  const T RT = sqrt(wR[0] / wL[0]);
+  const T u = (wL[1] + RT * wR[1]) / (T(1) + RT);
+  const T v = (wL[2] + RT * wR[2]) / (T(1) + RT);
+  const T w = (wL[3] + RT * wR[3]) / (T(1) + RT);
+  const T H = (HL + RT * HR) / (T(1) + RT);
+  const T a = sqrt((gamma - T(1)) * (H - T(0.5) * (u * u + v * v + w * w)));
+  const T lambda[5] = {u - a, u, u, u, u + a};
+  const T K[5][5] = {{T(1.), u - a, v, w, H - u * a},
+                     {T(1.), u, v, w, T(0.5) * (u * u + v * v + w * w)},
+                     {T(0.), T(0.), T(1.), T(0.), v},
+                     {T(0.), T(0.), T(0.), T(1.), w},
+                     {T(1.), u + a, v, w, H + u * a}};
+  // wave strengths
+  T alpha[5];
+  alpha[2] = (qR[2] - qL[2]) - v * (qR[0] - qL[0]);
+  alpha[3] = (qR[3] - qL[3]) - w * (qR[0] - qL[0]);
+  const T du5bar = (qR[4] - qL[4]) - (alpha[2]) * v - (alpha[3]) * w;
+  alpha[1] = ((gamma - T(1)) / (a * a)) * ((qR[0] - qL[0]) * (H - u * u) + u * (qR[1] - qL[1]) - du5bar);
+  alpha[0] = T(0.5) * (T(1) / a) * ((qR[0] - qL[0]) * (u + a) - (qR[1] - qL[1]) - a * alpha[1]);
+  alpha[4] = (qR[0] - qL[0]) - (alpha[0] + alpha[1]);
+  // physical fluxes
+  const T ptL = wL[4] + T(0.5) * (wL[5] * wL[5] + wL[6] * wL[6] + wL[7] * wL[7]);
+  const T ptR = wR[4] + T(0.5) * (wR[5] * wR[5] + wR[6] * wR[6] + wR[7] * wR[7]);
+  const T FL[8] = {wL[0] * vnL,
+                   wL[0] * vnL * wL[1] + xnorm * ptL - BnL * wL[5],
+                   wL[0] * vnL * wL[2] + ynorm * ptL - BnL * wL[6],
+                   wL[0] * vnL * wL[3] - BnL * wL[7],
+                   wL[0] * vnL * HL - BnL * (wL[1] * wL[5] + wL[2] * wL[6] + wL[3] * wL[7]),
+                   vnL * wL[5] - BnL * wL[1],
+                   vnL * wL[6] - BnL * wL[2],
+                   vnL * wL[7] - BnL * wL[3]};
+  const T FR[8] = {wR[0] * vnR,
+                   wR[0] * vnR * wR[1] + xnorm * ptR - BnR * wR[5],
+                   wR[0] * vnR * wR[2] + ynorm * ptR - BnR * wR[6],
+                   wR[0] * vnR * wR[3] - BnR * wR[7],
+                   wR[0] * vnR * HR - BnR * (wR[1] * wR[5] + wR[2] * wR[6] + wR[3] * wR[7]),
+                   vnR * wR[5] - BnR * wR[1],
+                   vnR * wR[6] - BnR * wR[2],
+                   vnR * wR[7] - BnR * wR[3]};
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    T summ = T(0.);
+#pragma unroll
+    for (int j = 0; j < 5; j++) summ += alpha[j] * fabs(lambda[j]) * (k < 5 ? K[j][k] : T(0.));
+    flux[k] = T(0.5) * (FL[k] + FR[k]) - T(0.5) * summ;
+  }
+  return 0;
+}
+
 template <int FLUX, typename T>
 __device__ __forceinline__ int riemann(const T *wL, const T *wR, T gamma, T *f) {
   if (FLUX == FLX_RUSA) return flux_rusa<T>(wL, wR, gamma, f);
   if (FLUX == FLX_HLLE) return flux_hlle<T>(wL, wR, gamma, f);
   if (FLUX == FLX_HLLC) return flux_hllc<T>(wL, wR, gamma, f);
+  if (FLUX == FLX_ROE) return flux_roe<T>(wL, wR, gamma, f);
   return flux_hlld<T>(wL, wR, gamma, f);
 }
 

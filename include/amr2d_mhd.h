@@ -191,6 +191,21 @@ int amr_criteria_flags(amr_handle *h, uint8_t *iref, uint8_t *icoarse, int32_t c
  * equal to amr_criteria_flags give amr_admesh's result.  n >= last_active. */
 int amr_admesh_marked(amr_handle *h, const uint8_t *iref, const uint8_t *icoarse, int32_t n);
 
+/* riemannS (riemannS.cpp:7-56) on the GPU for n independent face states:
+ * wL, wR and flux_out are [n][8] arrays in host memory (primitive states
+ * rho u v w p Bx By Bz; fluxes of the conserved variables).  flux: 0 RUSA,
+ * 1 HLLE, 2 HLLC, 3 HLLD, 4 ROE (riemannS.cpp:297-395); dir_y: 0 x face, 1
+ * y face (the reference's rotation); mag_field: the reference's
+ * compile-time MAG_field (defs.hpp:32), 1 in every run of the time loop, 0
+ * its hydrodynamic configuration (no field rotation; the only one in which
+ * ROE is accepted, riemannS.cpp:39-40: with mag_field = 1 ROE returns
+ * AMR_E_UNSUPPORTED).  status (may be NULL) receives 0 or AMR_E_HLLC (the
+ * traps of riemannS.cpp:269-276) per pair.  FP64 with the reference's
+ * arithmetic; ROE's (gamma-1)/pow(a,2) uses the correctly rounded square.
+ * Synchronous; allocates device memory for the batch. */
+int amr_riemann(int32_t flux, int32_t dir_y, int32_t mag_field, double gamma, const double *wL, const double *wR,
+                double *flux_out, int32_t *status, int64_t n);
+
 /* ---- handing over a run (extension: no counterpart in the reference) -----
  * Instance `instance` of a created handle takes the quadtree and time state
  * of a run the caller owns, e.g. a reference run stopped after some step:

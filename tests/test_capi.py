@@ -80,7 +80,7 @@ def test_every_entry_point_rejects_a_null_handle():
     L = amr.load()
     handle_first = {"amr_destroy", "amr_set_stream", "amr_last_error"} | {
         n for n in amr.EXPORTS
-        if n not in ("amr_cfl_dt_static", "amr_config_default", "amr_config_from_input", "amr_config_blast",
+        if n not in ("amr_cfl_dt_static", "amr_riemann", "amr_config_default", "amr_config_from_input", "amr_config_blast",
                      "amr_config_kh", "amr_abi_version", "amr_status_string", "amr_create", "amr_create_batch")}
     assert "amr_criteria_flags" in handle_first and "amr_set_tree" in handle_first
     for n in sorted(handle_first):
@@ -90,3 +90,9 @@ def test_every_entry_point_rejects_a_null_handle():
         assert fn(*args) == (0 if n == "amr_destroy" else -12), n
     # the allocation-free CFL reduction checks its pointers before any launch
     assert L.amr_cfl_dt_static(None, 4, 2, None, 5 / 3, None, None) == -12
+    # riemannS on arrays: pointers, solver and ROE's magnetic-field rejection
+    # (riemannS.cpp:39-40) are checked before any device call
+    w = (ctypes.c_double * 8)()
+    assert L.amr_riemann(0, 0, 1, 1.4, None, w, w, None, 1) == -12
+    assert L.amr_riemann(7, 0, 1, 1.4, w, w, w, None, 1) == -1
+    assert L.amr_riemann(4, 0, 1, 1.4, w, w, w, None, 1) == -11
