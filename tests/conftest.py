@@ -10,6 +10,8 @@ if REPO not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # pytest-timeout's marker, registered here too for runs without the plugin
+    config.addinivalue_line("markers", "timeout(seconds): per-test time limit (pytest-timeout)")
 
 
 def have_gpu():

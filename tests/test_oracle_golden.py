@@ -77,3 +77,27 @@ def test_kat_riemann_hydro():
         got = P.riemann(P.FLUXES[d["flux"][q]], d["wL"][q], d["wR"][q], d["gamma"][q], bool(d["dir"][q]),
                         mag_field=False)
         assert np.array_equal(got.view(np.int64), d["out"][q].view(np.int64)), q
+
+
+LONG = sorted(os.path.basename(p)[5:-4] for p in glob.glob(os.path.join(GOLDEN, "long_*.npz")))
+LONG_CPU_STEPS = 50
+
+
+@pytest.mark.parametrize("name", LONG)
+def test_long_run_first_steps(name):
+    """The gamma-5/3 rotor of the reference (to t_end in the GPU tests): the
+    oracle's first steps, t and dt each step, fingerprints where recorded."""
+    d = np.load(os.path.join(GOLDEN, "long_%s.npz" % name))
+    meta = ast.literal_eval(str(d["meta"]))
+    o = P.Oracle(ic=meta["ic"], limiter=meta["limiter"], flux=meta["flux"], cfl=meta["cfl"],
+                 maxlevs=meta["maxlevs"], nghosts=meta["nghosts"], gamma=meta["gamma"], nthreads=4).init()
+    fp = {int(s): q for q, s in enumerate(d["fp_step"])}
+    for s in range(LONG_CPU_STEPS + 1):
+        if s:
+            o.step()
+        inf = o.info()
+        assert inf["t"] == d["t"][s] and inf["dt"] == d["dt"][s], s
+        if s in fp:
+            st = o.state()
+            assert tree_hash(st) == d["tree"][fp[s]], s
+            assert leaf_hash(st) == d["leaf"][fp[s]], s
