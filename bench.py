@@ -450,7 +450,13 @@ def run_batch(stream, steps, advance):
 OT_RUNS = ((3, "WENO5", 0.003), (4, "MC", 0.0015))
 
 
-def run_orszag_tang(stream):
+def ot_runs_at(levels):
+    """MUSCL-MC + HLLD runs at the given levels, dt halved per level from the
+    4-level run's 0.0015 (the finest cells set the stable step)."""
+    return [(ml, "MC", 0.0015 * 2.0 ** (4 - ml)) for ml in levels]
+
+
+def run_orszag_tang(stream, runs=OT_RUNS):
     """Orszag-Tang to t = pi in FP64 and in FP32 on a common fixed time grid;
     relative L1 difference of every conserved variable on the finest uniform
     grid, and the throughput of both paths."""
@@ -459,7 +465,7 @@ def run_orszag_tang(stream):
     import amr2d_mhd_gb300 as amr
     out = []
     flush = L2Flush(stream)
-    for ml, lim, dt in OT_RUNS:
+    for ml, lim, dt in runs:
         res, rate = {}, {}
         for prec in ("fp64", "fp32"):
             sim = amr.Simulation(amr.ot_config(ml, prec, limiter=lim, dt_fixed=dt))
@@ -691,9 +697,21 @@ def main():
     ap.add_argument("--ncu-rotor-batch", type=int, default=0,
                     help="profiling case: the %d-rotor batch, fused stage kernel, this many steps, then exit"
                          % ROTOR_BATCH)
+    ap.add_argument("--ot-levels", default="",
+                    help="only the Orszag-Tang FP32-vs-FP64 comparison, MUSCL-MC + HLLD at these levels "
+                         "(comma-separated, e.g. 5,6), one JSON line")
     ap.add_argument("--adjoint-case", type=int, default=0,
                     help="profiling case: this many recorded and reversed steps of the KH adjoint, then exit")
     args = ap.parse_args()
+    if args.ot_levels:
+        import torch
+        levels = [int(x) for x in args.ot_levels.split(",")]
+        runs = run_orszag_tang(torch.cuda.current_stream(), ot_runs_at(levels))
+        print(json.dumps({"orszag_tang": runs, "workload": "Orszag-Tang on [0,2pi]^2, periodic, 4x4 roots of "
+                          "16x16, gamma 5/3, MUSCL-MC + HLLD + CT, RK2, to t=pi on a fixed dt shared by both "
+                          "precisions; FP32 bulk vs FP64, relative L1 per conserved variable on the finest "
+                          "uniform grid"}))
+        return 0
     if args.adjoint_case:
         import amr2d_mhd_gb300 as amr
         sim = amr.Simulation(amr.kh_config(5)).init()
