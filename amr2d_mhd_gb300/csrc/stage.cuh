@@ -100,18 +100,21 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
   w[7] = u[7];
 }
 
-// 4 resident CTAs per SM (64 registers, ~170 B of spills to L1): on the
-// 64-rotor FP32 batch 2.11 ms per stage launch against 2.31 ms at 3 CTAs
+// FP32 fused stage: 320 threads per CTA (the 2 x 17 x 17 = 578 faces of a
+// block in two rounds; 256 threads take three, the last a quarter full),
+// compiled for 3 resident CTAs per SM (64 registers, ~120 B of spills to L1).
+// Timed on the 64-rotor FP32 batch (one GB300, 20 steps): 5.17 ms per step
+// against 5.52 ms at 256 threads / 4 CTAs, 5.57 ms at 320 / 2 CTAs (96
+// registers, no spills); the 512-blast batch 24.7 against 25.1 and 27.8 ms.
 #ifndef AMR_STAGE_F32_MINB
-#define AMR_STAGE_F32_MINB 4
+#define AMR_STAGE_F32_MINB 3
 #endif
-// threads per CTA of the FP32 fused stage: 2 x 17 x 17 = 578 faces per block
-// take 3 rounds at 256 threads (the last a quarter full), 2 at 320
 #ifndef AMR_STAGE_F32_THREADS
-#define AMR_STAGE_F32_THREADS 256
+#define AMR_STAGE_F32_THREADS 320
 #endif
 // 1: the FP32 fused stage keeps the block's conserved state in shared memory
-// beside the primitive state, so the RK update does not read it again
+// beside the primitive state, so the RK update does not read it again (no
+// gain measured: 5.60 against 5.52 ms per step of the 64-rotor batch)
 #ifndef AMR_STAGE_F32_KEEPU
 #define AMR_STAGE_F32_KEEPU 0
 #endif
