@@ -795,18 +795,22 @@ def main():
                                   "2 flops per issue slot, this kernel issues mostly DADD / DMUL")
     except Exception as ex:  # noqa: BLE001
         fp64["error"] = str(ex)
+    sched = r64["schedule"]
+    face_kernel = ("k_stage<2,MUSCL,HLLD,double>" if sched.startswith("fused") else
+                   "k_faces_dyn<2,MUSCL,HLLD,double>" if " dynamic" in sched else
+                   "k_faces_persist<2,MUSCL,HLLD,double>" if " persistent" in sched else "k_faces<2,MUSCL,HLLD,double>")
     hbm_view = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind, "traffic": traffic, "bytes_per_launch": alg_bytes}
     if "frac" in fp64:
         roofline = {"bound": "fp64", "achieved": fp64["achieved_tflops"], "peak": fp64["peak_tflops_dgemm"],
                     "unit": "TFLOP/s", "frac": fp64["frac"], "peak_source": "measured (cuBLAS DGEMM 4096^3, this run)",
-                    "traffic": traffic, "kernel": "k_faces<2,MUSCL,HLLD,double>", "launch_ms": stage_ms_avg,
+                    "traffic": traffic, "kernel": face_kernel, "launch_ms": stage_ms_avg,
                     "flops_per_launch": fp64["flops_per_launch"],
                     "note": "FP64 flops per cell from ncu (DADD + DMUL + 2 DFMA, profiles/faces_fp64_rotor_hlld.md) x "
                             "cells per launch / CUDA-event launch time; the kernel's HBM fraction is in `hbm`",
                     "hbm": hbm_view}
     else:
-        roofline = dict(hbm_view, kernel="k_faces<2,MUSCL,HLLD,double>", launch_ms=stage_ms_avg)
+        roofline = dict(hbm_view, kernel=face_kernel, launch_ms=stage_ms_avg)
     cpu = None
     if not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
