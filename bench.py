@@ -694,6 +694,8 @@ def main():
     ap.add_argument("--ncu-t0", type=float, default=0.0,
                     help="with --ncu-case / --ncu-rotor-batch: first advance to this time (untimed), then run the steps")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="precision of --ncu-case")
+    ap.add_argument("--ncu-tune", action="store_true",
+                    help="with --ncu-case: run the autotuner before the profiled steps (the bench's schedule)")
     ap.add_argument("--ncu-rotor-batch", type=int, default=0,
                     help="profiling case: the %d-rotor batch, fused stage kernel, this many steps, then exit"
                          % ROTOR_BATCH)
@@ -745,9 +747,11 @@ def main():
         sim.profile(True)
         if args.ncu_t0 > 0:
             advance_to(sim, args.ncu_t0)
+        sched = sim.autotune() if args.ncu_tune else ""
         before = sim.profile()["launches"]
         sim.run(args.ncu_case)
-        print(json.dumps(dict(sim.info(), launches_before=before, launches=sim.profile()["launches"] - before)))
+        print(json.dumps(dict(sim.info(), launches_before=before, launches=sim.profile()["launches"] - before,
+                              schedule=next((l[2:] for l in sched.splitlines() if l.startswith("*")), "default"))))
         return 0
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
