@@ -582,7 +582,9 @@ int Engine::stage(int step) {
     a.ff = ff_;
     a.gg = gg_;
     a.err = d_err_.as<DevError>();
+    a.ctr = d_ctr_.as<unsigned>();
     a.step = step;
+    a.ntasks = n;
     if (int rc = ev_begin()) return rc;
     CK(launch_stage(m_, a, n, stream_), "stage kernel");
     if (int rc = ev_end()) return rc;
@@ -616,6 +618,7 @@ int Engine::autotune(int reps, char *report, size_t len) {
   std::vector<Cand> cands;
   for (int gb : {128, 256, 512}) {
     cands.push_back({false, 128, 256, gb, 0, 0.f});
+    cands.push_back({false, 128, 256, gb, 2, 0.f});   // fused, persistent over the leaf list
     for (int pers : {0, 1, 2})
       for (int fb : {64, 128})
         for (int cb : {256, 512}) cands.push_back({true, fb, cb, gb, pers, 0.f});
@@ -667,7 +670,7 @@ int Engine::autotune(int reps, char *report, size_t len) {
     for (const Cand &c : cands) {
       std::snprintf(line, sizeof line, "%s%s faces %d%s cells %d ghosts %d: %.4f ms\n", &c == best ? "* " : "  ",
                     c.split ? "split" : "fused", c.fb, c.pers == 2 ? " dynamic" : (c.pers ? " persistent" : ""), c.cb,
-                    c.gb, c.ms);
+                    c.gb, c.ms);  // fused + dynamic: k_stage_dyn
       s += line;
     }
     std::strncpy(report, s.c_str(), len - 1);

@@ -32,7 +32,9 @@ struct StageArgs {
   void *ff;
   void *gg;
   DevError *err;
+  unsigned *ctr;      // [2] block counter and finished-CTA counter of k_stage_dyn (zero between launches)
   int step;
+  int ntasks;         // leaf blocks (k_stage_dyn)
 };
 
 // First statement of every kernel of the step: when the kernel was launched
@@ -162,9 +164,13 @@ template <> struct StageThreads<float> { static constexpr int value = AMR_STAGE_
 template <typename S> struct StageKeepU { static constexpr bool value = false; };
 template <> struct StageKeepU<float> { static constexpr bool value = AMR_STAGE_F32_KEEPU != 0; };
 
+// One leaf block of the fused stage: task `ti`, its conserved state staged
+// into shared memory by a bulk copy completing on `bar` (initialised by the
+// caller) in phase `phase`.  Returns false (after recording DERR_TIMEOUT and
+// letting the copy land) when the bounded wait gave up; the decision is the
+// same in every thread of the CTA.
 template <int NG, int RECON, int FLUX, typename S>
-__global__ void __launch_bounds__(StageThreads<S>::value, StageMinBlocks<S>::value) k_stage(StageArgs a) {
-  pdl_wait();
+__device__ __forceinline__ bool stage_block(const StageArgs &a, int ti, uint64_t *bar, uint32_t phase) {
   using G = Geo<NG>;
   using T = S;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI, NF = G::NF, NFX = G::NFX;
@@ -175,7 +181,7 @@ __global__ void __launch_bounds__(StageThreads<S>::value, StageMinBlocks<S>::val
   constexpr bool KEEPU = StageKeepU<S>::value;
   S *sU = KEEPU ? sFy + 8 * NFX * NF : sW;   // [8][NN] the conserved state (KEEPU), else staged in sW
 
-  const LeafTask task = a.tasks[blockIdx.x];
+  const LeafTask task = a.tasks[ti];
   const InstParams ip = a.inst[task.inst];
   const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
   const S *Q = static_cast<const S *>(a.qin) + base;
@@ -185,19 +191,14 @@ __global__ void __launch_bounds__(StageThreads<S>::value, StageMinBlocks<S>::val
   const double *By = Bx + NN;
   const int tid = threadIdx.x, nthr = blockDim.x;
 
-  // 0. the block's conserved state (8 planes, contiguous) into sW by TMA
-  __shared__ __align__(8) uint64_t bar;
+  // 0. the block's conserved state (8 planes, contiguous) into shared memory by TMA
   static_assert((8 * NN * sizeof(S)) % 16 == 0, "bulk copies move multiples of 16 bytes");
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)), "r"(1) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  if (tid == 0) bulk_stage_issue(sU, Q, static_cast<uint32_t>(8 * NN * sizeof(S)), &bar);
-  if (!bulk_stage_wait(&bar, 0)) {
+  if (tid == 0) bulk_stage_issue(sU, Q, static_cast<uint32_t>(8 * NN * sizeof(S)), bar);
+  const bool late = !bulk_stage_wait(bar, phase);
+  if (__syncthreads_or(late)) {
     if (tid == 0) dev_fail(a.err, DERR_TIMEOUT, task.slot, 0, 0, 0.0);
-    bulk_stage_wait(&bar, 0);  // let the copy land before the CTA's shared memory is released
-    return;
+    bulk_stage_wait(bar, phase);  // let the copy land before the CTA's shared memory is released
+    return false;
   }
 
   // 1. primitive variables of every cell (U2W / Us2W), with the traps (in
@@ -308,6 +309,51 @@ __global__ void __launch_bounds__(StageThreads<S>::value, StageMinBlocks<S>::val
     const T q = KEEPU ? sU[e] : Q[e];
     if (a.step == 1) out[e] = q - dt * res;                         // Us = U - dt res
     else out[e] = T(0.5) * (out[e] + q - dt * res);                 // U = (U + Us - dt res)/2
+  }
+  return true;
+}
+
+__device__ __forceinline__ void stage_bar_init(uint64_t *bar) {
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// one CTA per leaf block
+template <int NG, int RECON, int FLUX, typename S>
+__global__ void __launch_bounds__(StageThreads<S>::value, StageMinBlocks<S>::value) k_stage(StageArgs a) {
+  pdl_wait();
+  __shared__ __align__(8) uint64_t bar;
+  stage_bar_init(&bar);
+  stage_block<NG, RECON, FLUX, S>(a, blockIdx.x, &bar, 0);
+}
+
+// persistent: a grid of the CTAs the SMs hold at once sweeps the leaf list of
+// all instances and levels, each CTA claiming the next block from a global
+// counter (the mbarrier phase alternates per block); the last CTA to finish
+// zeroes the counters for the next launch
+template <int NG, int RECON, int FLUX, typename S>
+__global__ void __launch_bounds__(StageThreads<S>::value, StageMinBlocks<S>::value) k_stage_dyn(StageArgs a) {
+  pdl_wait();
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int next;
+  stage_bar_init(&bar);
+  for (uint32_t it = 0;; it++) {
+    if (threadIdx.x == 0) next = static_cast<int>(atomicAdd(&a.ctr[0], 1u));
+    __syncthreads();
+    const int ti = next;
+    if (ti >= a.ntasks) break;
+    if (!stage_block<NG, RECON, FLUX, S>(a, ti, &bar, it & 1u)) break;
+    __syncthreads();  // shared memory free for the next block's copy
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&a.ctr[1], 1u) == gridDim.x - 1) {
+      a.ctr[0] = 0;
+      a.ctr[1] = 0;
+    }
   }
 }
 

@@ -9,27 +9,44 @@
 
 namespace amr {
 
+// persistent = 2 (and a.ctr set): k_stage_dyn on a grid of the CTAs the SMs
+// hold at once; otherwise one CTA per leaf block
 template <int NG, int RECON, int FLUX, typename S>
-cudaError_t launch_stage_t(const StageArgs &a, int ntasks, int pdl, cudaStream_t s) {
+cudaError_t launch_stage_t(const StageArgs &a, int ntasks, int pdl, int persistent, cudaStream_t s) {
   constexpr int smem = stage_smem_bytes<NG, S>();
+  constexpr int threads = StageThreads<S>::value;
   static bool attr_set = false;
+  static int per_sm = 0, sms = 0;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_stage<NG, RECON, FLUX, S>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(k_stage<NG, RECON, FLUX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_stage_dyn<NG, RECON, FLUX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_dyn<NG, RECON, FLUX, S>, threads, smem);
     if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
     attr_set = true;
   }
   if (ntasks <= 0) return cudaSuccess;
-  return launch_k(pdl, k_stage<NG, RECON, FLUX, S>, ntasks, StageThreads<S>::value, smem, s, a);
+  if (persistent == 2 && a.ctr) {
+    const int grid = ntasks < sms * per_sm ? ntasks : sms * per_sm;
+    return launch_k(pdl, k_stage_dyn<NG, RECON, FLUX, S>, grid, threads, smem, s, a);
+  }
+  return launch_k(pdl, k_stage<NG, RECON, FLUX, S>, ntasks, threads, smem, s, a);
 }
 
 template <int FLUX, typename S>
 cudaError_t launch_stage_flux(const Method &m, const StageArgs &a, int ntasks, cudaStream_t s) {
-  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_stage_t<2, REC_MUSCL, FLUX, S>(a, ntasks, m.pdl, s);
-  if (m.ng == 2 && m.recon == REC_WENO3) return launch_stage_t<2, REC_WENO3, FLUX, S>(a, ntasks, m.pdl, s);
-  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_stage_t<4, REC_MUSCL, FLUX, S>(a, ntasks, m.pdl, s);
-  if (m.ng == 4 && m.recon == REC_WENO3) return launch_stage_t<4, REC_WENO3, FLUX, S>(a, ntasks, m.pdl, s);
-  if (m.ng == 4 && m.recon == REC_WENO5) return launch_stage_t<4, REC_WENO5, FLUX, S>(a, ntasks, m.pdl, s);
+  const int p = m.persistent;
+  if (m.ng == 2 && m.recon == REC_MUSCL) return launch_stage_t<2, REC_MUSCL, FLUX, S>(a, ntasks, m.pdl, p, s);
+  if (m.ng == 2 && m.recon == REC_WENO3) return launch_stage_t<2, REC_WENO3, FLUX, S>(a, ntasks, m.pdl, p, s);
+  if (m.ng == 4 && m.recon == REC_MUSCL) return launch_stage_t<4, REC_MUSCL, FLUX, S>(a, ntasks, m.pdl, p, s);
+  if (m.ng == 4 && m.recon == REC_WENO3) return launch_stage_t<4, REC_WENO3, FLUX, S>(a, ntasks, m.pdl, p, s);
+  if (m.ng == 4 && m.recon == REC_WENO5) return launch_stage_t<4, REC_WENO5, FLUX, S>(a, ntasks, m.pdl, p, s);
   return cudaErrorInvalidValue;
 }
 

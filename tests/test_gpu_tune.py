@@ -24,7 +24,7 @@ def test_autotune_keeps_parity(gpu):
     sim.run(10)
     report = sim.autotune(2)
     lines = report.strip().splitlines()
-    assert len(lines) == 39 and sum(l.startswith("*") for l in lines) == 1
+    assert len(lines) == 42 and sum(l.startswith("*") for l in lines) == 1
     sim.run(20)
     o.run(30)
     assert same_as_oracle(sim, o)
