@@ -450,10 +450,11 @@ def run_batch(stream, steps, advance):
 OT_RUNS = ((3, "WENO5", 0.003), (4, "MC", 0.0015))
 
 
-def ot_runs_at(levels):
+def ot_runs_at(levels, dt_scale=1.0):
     """MUSCL-MC + HLLD runs at the given levels, dt halved per level from the
-    4-level run's 0.0015 (the finest cells set the stable step)."""
-    return [(ml, "MC", 0.0015 * 2.0 ** (4 - ml)) for ml in levels]
+    4-level run's 0.0015 (the finest cells set the stable step), times
+    dt_scale."""
+    return [(ml, "MC", dt_scale * 0.0015 * 2.0 ** (4 - ml)) for ml in levels]
 
 
 def run_orszag_tang(stream, runs=OT_RUNS):
@@ -702,13 +703,20 @@ def main():
     ap.add_argument("--ot-levels", default="",
                     help="only the Orszag-Tang FP32-vs-FP64 comparison, MUSCL-MC + HLLD at these levels "
                          "(comma-separated, e.g. 5,6), one JSON line")
+    ap.add_argument("--ot-dt-scale", type=float, default=1.0, help="with --ot-levels: scale of the fixed dt")
     ap.add_argument("--adjoint-case", type=int, default=0,
                     help="profiling case: this many recorded and reversed steps of the KH adjoint, then exit")
     args = ap.parse_args()
     if args.ot_levels:
         import torch
         levels = [int(x) for x in args.ot_levels.split(",")]
-        runs = run_orszag_tang(torch.cuda.current_stream(), ot_runs_at(levels))
+        runs = []
+        for ml in levels:   # one level at a time: a level that fails leaves the others' results
+            try:
+                runs += run_orszag_tang(torch.cuda.current_stream(), ot_runs_at([ml], args.ot_dt_scale))
+            except Exception as e:  # noqa: BLE001 - reported in the line
+                runs.append({"maxlevs": ml, "limiter": "MC", "flux": "HLLD",
+                             "dt": ot_runs_at([ml], args.ot_dt_scale)[0][2], "error": str(e)})
         print(json.dumps({"orszag_tang": runs, "workload": "Orszag-Tang on [0,2pi]^2, periodic, 4x4 roots of "
                           "16x16, gamma 5/3, MUSCL-MC + HLLD + CT, RK2, to t=pi on a fixed dt shared by both "
                           "precisions; FP32 bulk vs FP64, relative L1 per conserved variable on the finest "

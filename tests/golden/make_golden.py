@@ -14,6 +14,10 @@ reproduce them exactly) and records
   kat_riemann_hydro.npz  riemannS() answers of the reference built with
                     MAG_field = false (defs.hpp:32), every solver including
                     ROE (riemannS.cpp:297-395), which only that build reaches;
+  oracle_<name>.npz the same for a run the reference cannot make (the
+                    bench's geometry: 16 x 16 cells of 1/32 on [0,1]^2),
+                    made by the oracle (oracle/amr_oracle.c, itself pinned
+                    to the reference by the fixtures above);
   long_<name>.npz   a run to its end time: t, dt and leaf counts of every
                     step, fingerprints every `every` steps and of the last
                     step (the bench's rotor, gamma 5/3, built with
@@ -110,6 +114,37 @@ def make_long(name):
         os.remove(os.path.join(wd, f))
     os.rmdir(wd)
     print(name, "steps", n, "t_end", tlog[-1][3], "leaves", tlog[-1][2])
+
+
+ORACLE_LONG = {  # name: oracle keywords, fingerprint every
+    "rotor53_bench_L5_mc_hlld": (dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, nghosts=2,
+                                      geom_ref=False, gamma=5.0 / 3.0), 250),
+}
+
+
+def make_oracle_long(name, nthreads=4):
+    kw, every = ORACLE_LONG[name]
+    o = pyoracle.Oracle(**kw, nthreads=nthreads).init()
+    t, dt, nl, fps = [], [], [], {}
+    s = 0
+    while True:
+        inf = o.info()
+        t.append(inf["t"])
+        dt.append(inf["dt"])
+        nl.append(int(o.get("leafs").sum()))
+        if s % every == 0 or o.done:
+            fps[s] = record(o.state(), kw["nghosts"])
+        if o.done:
+            break
+        o.step()
+        s += 1
+    fp = sorted(fps)
+    meta = dict(kw, steps=s, every=every, made_by="oracle")
+    np.savez_compressed(os.path.join(HERE, "oracle_%s.npz" % name), meta=np.array(repr(meta)), t=np.array(t),
+                        dt=np.array(dt), nleaves=np.array(nl, np.int32), fp_step=np.array(fp, np.int32),
+                        tree=np.array([fps[k]["tree"] for k in fp]), leaf=np.array([fps[k]["leaf"] for k in fp]),
+                        sums=np.array([fps[k]["sums"] for k in fp]))
+    print(name, "steps", s, "t_end", t[-1], "leaves", nl[-1])
 
 
 def make_state(name):
@@ -216,10 +251,10 @@ def make_kat_limiter():
 
 
 if __name__ == "__main__":
-    if not ref_runner.available():
-        sys.exit("reference sources not found (set AMR_REFERENCE_SRC)")
+    names = sys.argv[1:] or (["kat"] + list(STATES) + list(RUNS) + list(LONG) + list(ORACLE_LONG))
     pyoracle.build()
-    names = sys.argv[1:] or (["kat"] + list(STATES) + list(RUNS) + list(LONG))
+    if any(nm not in ORACLE_LONG for nm in names) and not ref_runner.available():
+        sys.exit("reference sources not found (set AMR_REFERENCE_SRC)")
     for nm in names:
         if nm == "kat":
             make_kat_riemann()
@@ -231,5 +266,7 @@ if __name__ == "__main__":
             make_state(nm)
         elif nm in LONG:
             make_long(nm)
+        elif nm in ORACLE_LONG:
+            make_oracle_long(nm)
         else:
             make_run(nm)

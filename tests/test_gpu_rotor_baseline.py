@@ -7,21 +7,22 @@
   t and dt of every step, and the tree and leaf-state fingerprints every 25
   steps and at the last step, bit for bit, with HLLD and with RUSA
   (tests/golden/long_rotor53_L5_mc_*.npz, tests/golden/make_golden.py).
-* The bench's geometry (16 x 16 cells of 1/32 on [0,1]^2): the FP64 CUDA path
-  against the oracle to t_end, bit for bit at checkpoints (the oracle runs on
-  host threads beside the GPU run), and the FP32 bulk path's density at t_end
-  within 1e-4 relative L1 of FP64 on the finest uniform grid.
+* The bench's geometry (16 x 16 cells of 1/32 on [0,1]^2), which the
+  reference cannot run: the FP64 CUDA path against the oracle to t_end, t and
+  dt of every step and fingerprints every 250 steps and at the last, bit for
+  bit (tests/golden/oracle_rotor53_bench_L5_mc_hlld.npz, made by the oracle,
+  which the fixtures above pin to the reference), and the FP32 bulk path's
+  density at t_end within 1e-4 relative L1 of FP64 on the finest uniform
+  grid.
 """
 import ast
 import glob
 import os
 import sys
-import threading
 
 import numpy as np
 import pytest
 
-from oracle import pyoracle as P
 from parity_util import to_gpu_cfg
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -31,7 +32,6 @@ from golden_util import leaf_hash, tree_hash  # noqa: E402
 LONG = sorted(os.path.basename(p)[5:-4] for p in glob.glob(os.path.join(GOLDEN, "long_*.npz")))
 BENCH_ROTOR = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5, nghosts=2, geom_ref=False,
                    gamma=5.0 / 3.0)
-CHECK_EVERY = 1000
 
 
 @pytest.mark.gpu
@@ -57,42 +57,28 @@ def test_gpu_long_run_matches_reference(gpu, name):
     assert m["steps"] in fp
 
 
-def _fingerprint(st):
-    return (st["t"], tree_hash(st), leaf_hash(st))
-
-
 @pytest.mark.gpu
 @pytest.mark.timeout(900)
 def test_gpu_bench_rotor_to_t_end(gpu):
-    # the oracle on half the host cores, beside the GPU run (whose host
-    # thread and remesh / compile threads keep the other half)
-    ora = P.Oracle(**BENCH_ROTOR, nthreads=max(1, (os.cpu_count() or 2) // 2)).init()
-    ora_fp, err = {}, []
-
-    def oracle_run():
-        try:
-            while not ora.done:
-                ora.run(CHECK_EVERY)
-                ora_fp[ora.info()["count"]] = _fingerprint(ora.state())
-        except Exception as e:  # noqa: BLE001
-            err.append(e)
-
-    th = threading.Thread(target=oracle_run)
-    th.start()
+    d = np.load(os.path.join(GOLDEN, "oracle_rotor53_bench_L5_mc_hlld.npz"))
+    m = ast.literal_eval(str(d["meta"]))
     cfg = to_gpu_cfg(BENCH_ROTOR)
     a = gpu.Simulation(**cfg).init()
-    gpu_fp = {}
-    while not a.info()["done"]:
-        a.run(CHECK_EVERY)
-        gpu_fp[a.info()["steps"]] = _fingerprint(a.state())
+    fp = {int(s): q for q, s in enumerate(d["fp_step"])}
+    for s in range(m["steps"] + 1):
+        if s:
+            a.step()
+        inf = a.info()
+        assert inf["t"] == d["t"][s] and inf["dt"] == d["dt"][s], s
+        assert inf["n_leaves"] == d["nleaves"][s], s
+        if s in fp:
+            st = a.state()
+            assert tree_hash(st) == d["tree"][fp[s]], s
+            assert leaf_hash(st) == d["leaf"][fp[s]], s
+    assert a.info()["done"] == 1 and a.info()["t"] > 0.295
     b = gpu.Simulation(**dict(cfg, precision="fp32")).init()
     b.run()
-    th.join()
-    assert not err, err
-    assert sorted(gpu_fp) == sorted(ora_fp) and len(gpu_fp) >= 5
-    for s in sorted(gpu_fp):
-        assert gpu_fp[s] == ora_fp[s], s
-    assert a.info()["t"] > 0.295 and b.info()["t"] > 0.295
+    assert b.info()["t"] > 0.295
     r64, r32 = a.uniform(0), b.uniform(0)
     l1 = float(np.abs(r32 - r64).sum() / np.abs(r64).sum())
     print("rotor t_end FP32 vs FP64 density relative L1: %.3e" % l1)
