@@ -23,6 +23,22 @@ template <> __device__ __forceinline__ double eps_of<double>() { return 1.0E-15;
 // the WENO weights and limiter ratios, i.e. the scheme, not just the rounding.
 template <> __device__ __forceinline__ float eps_of<float>() { return 1.0E-15f; }
 
+// Classification of a value from its bit pattern in the integer pipe: the
+// same predicates as isfinite / == 0 / isnan, which would take slots of the
+// FP64 pipe (on GB300 2 per SM per clock) in the FP64-bound face kernel.
+__device__ __forceinline__ bool bits_finite(double x) {
+  return (__double_as_longlong(x) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool bits_finite(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
+__device__ __forceinline__ bool bits_zero(double x) {
+  return (static_cast<unsigned long long>(__double_as_longlong(x)) << 1) == 0ull;
+}
+__device__ __forceinline__ bool bits_zero(float x) { return (__float_as_uint(x) << 1) == 0u; }
+__device__ __forceinline__ bool bits_nan(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool bits_nan(float x) { return (__float_as_uint(x) & 0x7fffffffu) > 0x7f800000u; }
+
 // slopelimiter.cpp:6-54
 template <typename T>
 __device__ __forceinline__ T slope_limiter(int lim, T r, T eta) {
@@ -73,9 +89,9 @@ __device__ __forceinline__ T slope_limiter(int lim, T r, T eta) {
 template <typename T>
 __device__ __forceinline__ T limiter_ratio(int lim, T num, T den) {
   if (lim == LIM_1ST) return T(0);
-  if (den != T(0) && isfinite(den) && isfinite(num)) {
+  if (!bits_zero(den) && bits_finite(den) && bits_finite(num)) {
     const bool neg = signbit(num) != signbit(den);
-    if (num == T(0)) return neg ? T(-0.0) : T(0.0);
+    if (bits_zero(num)) return neg ? T(-0.0) : T(0.0);
     if (neg && (lim == LIM_MINMOD || lim == LIM_MC || lim == LIM_SUPERBEE || lim == LIM_KOREN)) return T(-1);
   }
   return num / den;

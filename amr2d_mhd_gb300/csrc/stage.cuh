@@ -215,7 +215,7 @@ __device__ __forceinline__ bool stage_block(const StageArgs &a, int ti, uint64_t
       dev_fail(a.err, DERR_PRESSURE, task.slot, i, j, static_cast<double>(w[4]));
     bool bad = false;
 #pragma unroll
-    for (int k = 0; k < 8; k++) bad |= isnan(w[k]);
+    for (int k = 0; k < 8; k++) bad |= bits_nan(w[k]);
     if (bad) dev_fail(a.err, DERR_NAN, task.slot, i, j, 0.0);
   }
   // fluxes MUSCL2D does not recompute: the x face at LO and the y face at LO
@@ -281,7 +281,7 @@ __device__ __forceinline__ bool stage_block(const StageArgs &a, int ti, uint64_t
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      bad |= isnan(fl[k]);
+      bad |= bits_nan(fl[k]);
       if (!yf) {
         sFx[(k * NF + r) * NFX + (c + 1)] = fl[k];
         ff[k * NN + fpos] = fl[k];

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(512) k_prim(SplitArgs a) {
     dev_fail(a.err, DERR_PRESSURE, task.slot, i, j, static_cast<double>(w[4]));
   bool bad = false;
 #pragma unroll
-  for (int k = 0; k < 8; k++) bad |= isnan(w[k]);
+  for (int k = 0; k < 8; k++) bad |= bits_nan(w[k]);
   if (bad) dev_fail(a.err, DERR_NAN, task.slot, i, j, 0.0);
 }
 
@@ -115,7 +115,7 @@ __device__ __forceinline__ void face_flux(const SplitArgs &a, size_t e) {
   bool bad = false;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    bad |= isnan(fl[k]);
+    bad |= bits_nan(fl[k]);
     out[k * NN] = fl[k];
   }
   if (bad) dev_fail(a.err, DERR_NAN, task.slot, fpos % N, fpos / N, 0.0);
