@@ -299,6 +299,17 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// warp maximum in the storage type (the reduction above, before widening)
+template <typename T>
+__device__ __forceinline__ T warp_max_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = v < u ? u : v;
+  }
+  return v;
+}
+
 struct DtArgs {
   const LeafTask *tasks;
   const InstParams *inst;
@@ -353,8 +364,11 @@ __global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
     const T i0 = (ca * ca) + (as * as), i1 = (ca * ca) - (as * as);
     cf[q] = sqrt(T(0.5) * (i0 + sqrt(i1 * i1 + T(4.) * (as * as) * ((ca * ca) - (can * can)))));
   }
-  double lam = smax(static_cast<double>(fabs(w[0]) + cf[0]), static_cast<double>(fabs(w[1]) + cf[1]));
-  double gr = 0.;
+  // the maxima in the storage type, widened to FP64 once per warp: the
+  // widening is exact and monotonic, so this equals the maximum of the
+  // widened values (and keeps FP32 maxima off the FP64 pipe)
+  T lamT = smax(fabs(w[0]) + cf[0], fabs(w[1]) + cf[1]);
+  T grT = T(0.);
   if (a.want_grad) {
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -366,11 +380,11 @@ __global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
       T d2 = mmax(d1, fabs(x[-1] - c0));
       d1 = mmax(d2, fabs(x[N] - c0));
       d2 = mmax(d1, fabs(x[-N] - c0));
-      gr = mmax(gr, static_cast<double>(d2 / dm));
+      grT = mmax(grT, d2 / dm);
     }
   }
-  lam = warp_max(lam);
-  gr = warp_max(gr);
+  const double lam = static_cast<double>(warp_max_t(lamT));
+  const double gr = static_cast<double>(warp_max_t(grT));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) { red[0][wid] = lam; red[1][wid] = gr; }
   __syncthreads();

@@ -157,6 +157,8 @@ int Engine::create(const amr_config *cfgs, int n) {
   if (const char *k = std::getenv("AMR2D_STAGE_KERNEL")) split_ = std::strcmp(k, "fused") != 0;
   if (const char *g = std::getenv("AMR2D_GRAPHS")) graph_on_ = std::strcmp(g, "0") != 0;
   if (const char *p = std::getenv("AMR2D_PDL")) m_.pdl = std::strcmp(p, "0") != 0 ? 1 : 0;
+  if (const char *f = std::getenv("AMR2D_FACE_KERNEL"))
+    m_.persistent = !std::strcmp(f, "dynamic") ? 2 : (!std::strcmp(f, "persistent") ? 1 : 0);
   ng_ = m_.ng;
   n_ = NI + 2 * ng_;
   nn_ = n_ * n_;
