@@ -457,10 +457,14 @@ def ot_runs_at(levels, dt_scale=1.0):
     return [(ml, "MC", dt_scale * 0.0015 * 2.0 ** (4 - ml)) for ml in levels]
 
 
-def run_orszag_tang(stream, runs=OT_RUNS):
-    """Orszag-Tang to t = pi in FP64 and in FP32 on a common fixed time grid;
-    relative L1 difference of every conserved variable on the finest uniform
-    grid, and the throughput of both paths."""
+class OTFailed(RuntimeError):
+    """An Orszag-Tang run stopped by the library (e.g. negative pressure), with its time."""
+
+
+def run_orszag_tang(stream, runs=OT_RUNS, t_end=None):
+    """Orszag-Tang to t = pi (or t_end) in FP64 and in FP32 on a common fixed
+    time grid; relative L1 difference of every conserved variable on the
+    finest uniform grid, and the throughput of both paths."""
     import torch
 
     import amr2d_mhd_gb300 as amr
@@ -469,13 +473,19 @@ def run_orszag_tang(stream, runs=OT_RUNS):
     for ml, lim, dt in runs:
         res, rate = {}, {}
         for prec in ("fp64", "fp32"):
-            sim = amr.Simulation(amr.ot_config(ml, prec, limiter=lim, dt_fixed=dt))
+            cfg = amr.ot_config(ml, prec, limiter=lim, dt_fixed=dt)
+            if t_end:
+                cfg.t_end = t_end
+            sim = amr.Simulation(cfg)
             sim.set_stream(stream.cuda_stream)
             sim.init()
             torch.cuda.synchronize()
             ms = 0.0
-            while not sim.info()["done"]:   # steps past the end are no-ops
-                ms += timed_steps(sim.step, 50, stream, flush)
+            try:
+                while not sim.info()["done"]:   # steps past the end are no-ops
+                    ms += timed_steps(sim.step, 50, stream, flush)
+            except amr.AmrError as e:
+                raise OTFailed("%s: %s at t in (%.6g, %.6g]" % (prec, e, sim.info()["t"], sim.info()["t"] + 50 * dt))
             inf = sim.info()
             rate[prec] = inf["cell_updates"] / (ms * 1e-3)
             res[prec] = [sim.uniform(k) for k in range(8)]
@@ -484,7 +494,7 @@ def run_orszag_tang(stream, runs=OT_RUNS):
         names = ["rho", "mx", "my", "mz", "E", "Bx", "By", "Bz"]
         l1 = {names[k]: float(np.abs(res["fp32"][k] - res["fp64"][k]).sum() / np.abs(res["fp64"][k]).sum())
               for k in range(8) if np.abs(res["fp64"][k]).sum() > 0}
-        out.append(dict(maxlevs=ml, limiter=lim, flux="HLLD", dt=dt, steps=steps,
+        out.append(dict(maxlevs=ml, limiter=lim, flux="HLLD", dt=dt, steps=steps, t_end=t_end or "pi",
                         effective_grid=64 * 2 ** (ml - 1), fp64_cell_updates_per_s=rate["fp64"],
                         fp32_cell_updates_per_s=rate["fp32"], rel_l1_fp32_vs_fp64=l1))
     return out
@@ -704,6 +714,7 @@ def main():
                     help="only the Orszag-Tang FP32-vs-FP64 comparison, MUSCL-MC + HLLD at these levels "
                          "(comma-separated, e.g. 5,6), one JSON line")
     ap.add_argument("--ot-dt-scale", type=float, default=1.0, help="with --ot-levels: scale of the fixed dt")
+    ap.add_argument("--ot-t-end", type=float, default=0.0, help="with --ot-levels: end time (default pi)")
     ap.add_argument("--adjoint-case", type=int, default=0,
                     help="profiling case: this many recorded and reversed steps of the KH adjoint, then exit")
     args = ap.parse_args()
@@ -713,7 +724,8 @@ def main():
         runs = []
         for ml in levels:   # one level at a time: a level that fails leaves the others' results
             try:
-                runs += run_orszag_tang(torch.cuda.current_stream(), ot_runs_at([ml], args.ot_dt_scale))
+                runs += run_orszag_tang(torch.cuda.current_stream(), ot_runs_at([ml], args.ot_dt_scale),
+                                        args.ot_t_end or None)
             except Exception as e:  # noqa: BLE001 - reported in the line
                 runs.append({"maxlevs": ml, "limiter": "MC", "flux": "HLLD",
                              "dt": ot_runs_at([ml], args.ot_dt_scale)[0][2], "error": str(e)})
