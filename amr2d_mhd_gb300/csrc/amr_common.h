@@ -38,6 +38,13 @@ struct LeafTask {
   // the formulas that multiply by the rounded reciprocal (CT2D.cpp:80,86)
   double rcp_dx, rcp_dy;
   int flags;      // TASK_DIFFUSE
+  // the block's share of the step's compiled ghost fill, for fills fused into
+  // the step's kernels: the ops that write its ghost cells, and the
+  // snapshots of its cells (ranges of the device program)
+  int op_count;
+  int op_begin;
+  int snap_begin;
+  int snap_count;
   int pad;
 };
 // the block takes diffusivity.cpp after stage 2 (main.cpp:190-193)

@@ -58,6 +58,12 @@ cudaError_t launch_prim(const Method &m, const SplitArgs &a, cudaStream_t s) {
   const int nn = m.ng == 2 ? Geo<2>::NN : Geo<4>::NN;
   const size_t n = static_cast<size_t>(a.ntasks) * nn;
   if (n == 0) return cudaSuccess;
+  if (a.fuse.apply.nseg) {  // fused fill: one CTA per leaf
+    if (m.ng == 2 && !m.f32) return launch_k(m.pdl, k_prim_task<2, double>, a.ntasks, 256, 0, s, a);
+    if (m.ng == 2) return launch_k(m.pdl, k_prim_task<2, float>, a.ntasks, 256, 0, s, a);
+    if (!m.f32) return launch_k(m.pdl, k_prim_task<4, double>, a.ntasks, 256, 0, s, a);
+    return launch_k(m.pdl, k_prim_task<4, float>, a.ntasks, 256, 0, s, a);
+  }
   const int b = cell_threads(m);
   const unsigned g = static_cast<unsigned>((n + b - 1) / b);
   if (m.ng == 2 && !m.f32) return launch_k(m.pdl, k_prim<2, double>, g, b, 0, s, a);

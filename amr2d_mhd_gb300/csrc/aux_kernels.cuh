@@ -12,39 +12,7 @@
 namespace amr {
 
 // ------------------------------------------------------------ ghost fills
-// One compiled program (ops + snapshots) serves every field; a launch applies
-// it to up to kMaxSeg fields at once.
-constexpr int kMaxSeg = 3;
-struct GhostSeg {
-  void *field;
-  int nv;
-  int kind;           // FILL_CC / FILL_FC / FILL_EC (ghost_compile.hpp)
-  int f32;            // field stored as float
-};
-struct GhostLaunch {
-  const GhostOp *ops;
-  const GhostSnap *snaps;
-  int nops, nsnaps;
-  GhostSeg seg[kMaxSeg];
-  int nseg;
-  double *snapbuf;    // [nseg][nsnaps][8]
-  // variable rows of the launch: segment q owns rows [row0[q], row0[q+1]);
-  // set by launch_ghost
-  int row0[kMaxSeg + 1];
-};
-
-// A fill kernel runs on a 2-D grid: blockIdx.y is the variable row, so that
-// consecutive threads take consecutive items (ops or snapshots) of the same
-// variable and every load of an item is independent of the others.  The
-// segment is picked with constant indices into the parameter block.
-__device__ __forceinline__ GhostSeg ghost_seg(const GhostLaunch &g, int row, int &q, int &k) {
-  GhostSeg s = g.seg[0];
-  q = 0;
-  k = row;
-  if (g.nseg > 1 && row >= g.row0[1]) { s = g.seg[1]; q = 1; k = row - g.row0[1]; }
-  if (g.nseg > 2 && row >= g.row0[2]) { s = g.seg[2]; q = 2; k = row - g.row0[2]; }
-  return s;
-}
+// (GhostLaunch and the gather of one op: ghost.cuh)
 
 // save the pre-fill values the same fill overwrites
 template <int N>
@@ -60,46 +28,6 @@ __global__ void k_ghost_snap(GhostLaunch g) {
   const size_t at = (static_cast<size_t>(sn.slot) * s.nv + k) * NN + sn.pos;
   g.snapbuf[(static_cast<size_t>(q) * g.nsnaps + r) * 8 + k] =
       s.f32 ? static_cast<double>(static_cast<const float *>(s.field)[at]) : static_cast<const double *>(s.field)[at];
-}
-
-// fine-to-coarse value of one variable from the patch (i,j) (i,j+1) (i+1,j)
-// (i+1,j+1): boundary.cpp:48 / boundaryfc.cpp:48 / boundaryec.cpp:46
-template <typename F>
-__device__ __forceinline__ F fine_value(int kind, int k, F a00, F a01, F a10, F a11) {
-  F v = F(0.);
-  if (kind == 0) {
-    v += a00; v += a01; v += a10; v += a11;
-    return F(0.25) * v;
-  }
-  if (kind == 1) {
-    v += a00;
-    v += k == 0 ? a01 : a10;
-    return F(0.5) * v;
-  }
-  return a00;
-}
-
-// variable k of one gather
-template <int N, typename F>
-__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, int k, const double *snap) {
-  constexpr int NN = N * N;
-  F *fld = static_cast<F *>(s.field);
-  F *dst = fld + (static_cast<size_t>(op.dst_slot) * s.nv + k) * NN + op.dst_pos;
-  if (op.type == GOP_COPY2) {  // even positions in an even-sized plane: aligned pair
-    using P2 = typename std::conditional<sizeof(F) == 4, float2, double2>::type;
-    *reinterpret_cast<P2 *>(dst) =
-        *reinterpret_cast<const P2 *>(fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos);
-    return;
-  }
-  if (op.type == GOP_COPY || op.type == GOP_FINE) {
-    const F *c = fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos;
-    *dst = op.type == GOP_COPY ? c[0] : fine_value<F>(s.kind, k, c[0], c[N], c[1], c[1 + N]);
-  } else {
-    const double *r = snap + static_cast<size_t>(op.src_slot) * 8 + k;
-    *dst = op.type == GOP_SNAP ? static_cast<F>(r[0])
-                               : fine_value<F>(s.kind, k, static_cast<F>(r[0]), static_cast<F>(r[8]),
-                                               static_cast<F>(r[16]), static_cast<F>(r[24]));
-  }
 }
 
 template <int N>
@@ -127,7 +55,24 @@ struct CtArgs {
   void *q;                // cell state corrected by the face average
   DevError *err;
   int step;
+  FillFuse fuse;          // fused fills: the consumed fill first, the next one's snapshots last
 };
+
+// prologue and epilogue of a per-block kernel of the step with fused fills
+template <int N>
+__device__ __forceinline__ void fuse_apply(const FillFuse &f, const LeafTask &t) {
+  if (f.apply.nseg) {
+    fill_apply_task<N, double>(f, t, threadIdx.x, blockDim.x, nullptr);
+    __syncthreads();
+  }
+}
+template <int N>
+__device__ __forceinline__ void fuse_save(const FillFuse &f, const LeafTask &t) {
+  if (f.save.nseg) {
+    __syncthreads();
+    fill_save_task<N>(f, t, threadIdx.x, blockDim.x);
+  }
+}
 
 // CT2D.cpp:28-75, CTtype 2 ("upwind (not ready)", defs.hpp:34), for the block
 // of task t: pressure and speed of every cell of q in shared memory (:36-40),
@@ -183,9 +128,11 @@ __global__ void k_ct_emf(CtArgs a) {
   pdl_wait();
   constexpr int N = Geo<NG>::N, NN = N * N;
   const LeafTask t = a.tasks[blockIdx.x];
+  fuse_apply<N>(a.fuse, t);
   if (a.inst[t.inst].ct_type == 2) {
     __shared__ S sp[NN], sC[NN];
     ct_emf_upwind<NG, S>(a, t, sp, sC);
+    fuse_save<N>(a.fuse, t);
     return;
   }
   const S *ff = static_cast<const S *>(a.ff) + static_cast<size_t>(t.slot) * 8 * NN;
@@ -202,6 +149,7 @@ __global__ void k_ct_emf(CtArgs a) {
     const S f6a = ff[6 * NN + (j - 1) * N + i], f6b = ff[6 * NN + c];
     E[c] = static_cast<double>(S(0.25) * ((g5a + g5b) - (f6a + f6b)));
   }
+  fuse_save<N>(a.fuse, t);
 }
 
 // CT2D.cpp:78-92 face update with the RK2 combine
@@ -210,6 +158,7 @@ __global__ void k_ct_face(CtArgs a) {
   pdl_wait();
   constexpr int N = Geo<NG>::N, NN = N * N;
   const LeafTask t = a.tasks[blockIdx.x];
+  fuse_apply<N>(a.fuse, t);
   const double dt = a.inst[t.inst].dt;
   const double *E = a.EMF + static_cast<size_t>(t.slot) * NN;
   const double *B0 = a.Bsrc + static_cast<size_t>(t.slot) * 2 * NN;
@@ -224,6 +173,7 @@ __global__ void k_ct_face(CtArgs a) {
     if (a.step == 1) B1[NN + c] = B0[NN + c] - dt * res;
     else B1[NN + c] = 0.5 * (B0[NN + c] + B1[NN + c] - dt * res);
   }
+  fuse_save<N>(a.fuse, t);
 }
 
 // CT2D.cpp:95-123 cell B := face average, with the energy correction, on
@@ -233,6 +183,7 @@ __global__ void k_ct_cell(CtArgs a) {
   pdl_wait();
   constexpr int N = Geo<NG>::N, NN = N * N;
   const LeafTask t = a.tasks[blockIdx.x];
+  fuse_apply<N>(a.fuse, t);
   const double *B = a.Bnew + static_cast<size_t>(t.slot) * 2 * NN;
   S *q = static_cast<S *>(a.q) + static_cast<size_t>(t.slot) * 8 * NN;
   for (int c = threadIdx.x; c < NN; c += blockDim.x) {
@@ -248,6 +199,7 @@ __global__ void k_ct_cell(CtArgs a) {
     q[5 * NN + c] = bx;
     q[6 * NN + c] = by;
   }
+  fuse_save<N>(a.fuse, t);
 }
 
 // diffusivity.cpp:6-17 on the blocks flagged TASK_DIFFUSE (main.cpp:190-193:
@@ -318,6 +270,7 @@ struct DtArgs {
   double *grad;     // per task: max relative jump
   DevError *err;
   int want_grad;
+  FillFuse fuse;    // fused fills: the fill of U after the step, gathered first
 };
 
 template <int NG, typename S>
@@ -330,6 +283,7 @@ __global__ void __launch_bounds__(256) k_dt_cell(DtArgs a) {
   __shared__ double red[2][8];
   __shared__ S sW[8 * NN];
   const LeafTask t = a.tasks[blockIdx.x];
+  fuse_apply<N>(a.fuse, t);
   const S *U = static_cast<const S *>(a.U) + static_cast<size_t>(t.slot) * 8 * NN;
   for (int c = threadIdx.x; c < NN; c += blockDim.x) {
     S u[8], w[8];

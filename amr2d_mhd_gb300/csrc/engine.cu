@@ -157,6 +157,7 @@ int Engine::create(const amr_config *cfgs, int n) {
   if (const char *k = std::getenv("AMR2D_STAGE_KERNEL")) split_ = std::strcmp(k, "fused") != 0;
   if (const char *g = std::getenv("AMR2D_GRAPHS")) graph_on_ = std::strcmp(g, "0") != 0;
   if (const char *p = std::getenv("AMR2D_PDL")) m_.pdl = std::strcmp(p, "0") != 0 ? 1 : 0;
+  if (const char *f = std::getenv("AMR2D_FUSED_FILLS")) fuse_fills_ = std::strcmp(f, "0") != 0;
   if (const char *f = std::getenv("AMR2D_FACE_KERNEL"))
     m_.persistent = !std::strcmp(f, "dynamic") ? 2 : (!std::strcmp(f, "persistent") ? 1 : 0);
   ng_ = m_.ng;
@@ -388,6 +389,7 @@ int Engine::layout_programs(bool relayout) {
   nops_ = o;
   nsnaps_ = sn;
   CK(d_snap_.ensure(sizeof(double) * 8 * (static_cast<size_t>(kMaxSeg) * nsnaps_ + 1)), "alloc");
+  CK(d_snap3_.ensure(sizeof(double) * 8 * (3 * static_cast<size_t>(kMaxSeg) * nsnaps_ + 1)), "alloc");
   GhostOp *ho = h_ops_.as<GhostOp>();
   GhostSnap *hs = h_snaps_.as<GhostSnap>();
   const GhostOp nop{0, 0, 0, 0, GOP_NOP, {0, 0, 0}};
@@ -468,7 +470,8 @@ int Engine::rebuild() {
       const int flags = in.cfg.diffusion && lev >= in.cfg.maxlevs - 2 ? TASK_DIFFUSE : 0;
       diffuse_any_ |= flags != 0;
       tasks_.push_back(LeafTask{in.slot[nb], a, in.dx[lev], in.dy[lev], exact_reciprocal(in.dx[lev]),
-                                exact_reciprocal(in.dy[lev]), 1. / in.dx[lev], 1. / in.dy[lev], flags, 0});
+                                exact_reciprocal(in.dy[lev]), 1. / in.dx[lev], 1. / in.dy[lev], flags, 0, 0, 0, 0,
+                                0});
       task_blk_.push_back(nb);
     }
     in.task_end = static_cast<int>(tasks_.size());
@@ -476,6 +479,20 @@ int Engine::rebuild() {
   }
   built_active_ = active_;
   if (int rc = layout_programs(relayout)) return rc;
+  // each leaf's share of its instance's program (the program is grouped by
+  // block; the fused fills need every written or saved block to be a leaf)
+  fuse_ok_ = true;
+  for (int a : active_) fuse_ok_ = fuse_ok_ && inst_[a].prog.by_block;
+  if (fuse_ok_)
+    for (size_t k = 0; k < tasks_.size(); k++) {
+      const Instance &in = inst_[tasks_[k].inst];
+      const int nb = task_blk_[k];
+      LeafTask &t = tasks_[k];
+      t.op_begin = static_cast<int>(in.ops_off) + in.prog.op_start[nb];
+      t.op_count = in.prog.op_start[nb + 1] - in.prog.op_start[nb];
+      t.snap_begin = static_cast<int>(in.snaps_off) + in.prog.snap_start[nb];
+      t.snap_count = in.prog.snap_start[nb + 1] - in.prog.snap_start[nb];
+    }
   const size_t nt = tasks_.size();
   CK(d_tasks_.ensure(sizeof(LeafTask) * nt), "alloc");
   CK(h_tasks_.ensure(sizeof(LeafTask) * nt), "alloc");
@@ -533,7 +550,49 @@ int Engine::fill(std::initializer_list<std::pair<FillKind, int>> what) {
   return AMR_OK;
 }
 
-int Engine::stage(int step) {
+FillPass Engine::fill_pass(std::initializer_list<std::pair<FillKind, int>> what, int buf, int tile_seg) {
+  FillPass p{};
+  int q = 0;
+  for (const auto &w : what) {
+    GhostSeg &g = p.seg[q++];
+    g.field = field_ptr(w.second);
+    g.nv = field_nv(w.second);
+    g.kind = w.first;
+    g.f32 = field_f32(w.second) ? 1 : 0;
+    p.rows += g.nv;
+  }
+  p.nseg = q;
+  p.tile_seg = tile_seg;
+  p.snapbuf = d_snap3_.as<double>() + static_cast<size_t>(buf) * kMaxSeg * nsnaps_ * 8;
+  return p;
+}
+
+FillFuse Engine::fill_fuse(const FillPass *apply, const FillPass *save) const {
+  FillFuse f{};
+  f.ops = d_ops_.as<GhostOp>();
+  f.snaps = d_snaps_.as<GhostSnap>();
+  f.nsnaps = static_cast<int>(nsnaps_);
+  if (apply) f.apply = *apply;
+  if (save) f.save = *save;
+  return f;
+}
+
+int Engine::snap_only(const FillPass &p) {
+  if (nsnaps_ == 0) return AMR_OK;
+  GhostLaunch g{};
+  g.ops = d_ops_.as<GhostOp>();
+  g.snaps = d_snaps_.as<GhostSnap>();
+  g.nops = 0;
+  g.nsnaps = static_cast<int>(nsnaps_);
+  for (int q = 0; q < p.nseg; q++) g.seg[q] = p.seg[q];
+  g.nseg = p.nseg;
+  g.snapbuf = p.snapbuf;
+  CK(launch_ghost(m_, g, stream_), "ghost snapshots");
+  prof_.launches += 1;
+  return AMR_OK;
+}
+
+int Engine::stage(int step, const FillFuse *fuse) {
   // profiling events bracket the dominant kernel: the face-flux kernel of the
   // split stage, or the fused stage kernel
   auto ev_begin = [&]() -> int {
@@ -568,6 +627,7 @@ int Engine::stage(int step) {
     a.ctr = d_ctr_.as<unsigned>();
     a.step = step;
     a.ntasks = n;
+    if (fuse) a.fuse = *fuse;
     CK(launch_prim(m_, a, stream_), "prim kernel");
     if (int rc = ev_begin()) return rc;
     CK(launch_faces(m_, a, stream_), "face kernel");
@@ -587,6 +647,7 @@ int Engine::stage(int step) {
     a.ctr = d_ctr_.as<unsigned>();
     a.step = step;
     a.ntasks = n;
+    if (fuse) a.fuse = *fuse;
     if (int rc = ev_begin()) return rc;
     CK(launch_stage(m_, a, n, stream_), "stage kernel");
     if (int rc = ev_end()) return rc;
@@ -629,6 +690,13 @@ int Engine::autotune(int reps, char *report, size_t len) {
   CK(cudaEventCreate(&e0), "event");
   CK(cudaEventCreate(&e1), "event");
   auto probe = [&]() -> int {
+    if (fused_fills()) {  // the step's form: snapshots, then the stage with the fill inside
+      const FillPass f1 = fill_pass({{FILL_CC, AMR_FIELD_U}, {FILL_FC, AMR_FIELD_BI}}, 0, 0);
+      const FillPass f2 = fill_pass({{FILL_FC, AMR_FIELD_BI}, {FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}}, 1);
+      if (int rc = snap_only(f1)) return rc;
+      const FillFuse s1 = fill_fuse(&f1, &f2);
+      return stage(1, &s1);
+    }
     if (int rc = fill({{FILL_CC, AMR_FIELD_U}, {FILL_FC, AMR_FIELD_BI}})) return rc;
     if (int rc = stage(1)) return rc;
     return fill({{FILL_FC, AMR_FIELD_BI}, {FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}});
@@ -682,8 +750,11 @@ int Engine::autotune(int reps, char *report, size_t len) {
 }
 
 // CT2D.cpp:11-124: EMF, its ghost fill, the face update, its ghost fill and
-// the cell-centred B / energy correction
-int Engine::ct2d(int step) {
+// the cell-centred B / energy correction.  With `in` (fused fills) the EMF
+// kernel gathers the fill `in`, the fills of the EMF and of the new face field
+// run inside the next kernel (snapshots in rotating buffers emf_buf and
+// bnew_buf), and the cell kernel saves the snapshots of `out`.
+int Engine::ct2d(int step, const FillPass *in, const FillPass *out, int emf_buf, int bnew_buf) {
   CtArgs a{};
   a.tasks = d_tasks_.as<LeafTask>();
   a.inst = d_params_.as<InstParams>();
@@ -696,6 +767,18 @@ int Engine::ct2d(int step) {
   a.err = d_err_.as<DevError>();
   a.step = step;
   const int n = static_cast<int>(tasks_.size());
+  if (in) {
+    const FillPass emf = fill_pass({{FILL_EC, AMR_FIELD_EMF}}, emf_buf);
+    const FillPass bnew = fill_pass({{FILL_FC, step == 1 ? AMR_FIELD_BIS : AMR_FIELD_BI}}, bnew_buf);
+    a.fuse = fill_fuse(in, &emf);
+    CK(launch_ct_emf(m_, a, n, stream_), "ct emf");
+    a.fuse = fill_fuse(&emf, &bnew);
+    CK(launch_ct_face(m_, a, n, stream_), "ct face");
+    a.fuse = fill_fuse(&bnew, out);
+    CK(launch_ct_cell(m_, a, n, stream_), "ct cell");
+    prof_.launches += 3;
+    return AMR_OK;
+  }
   CK(launch_ct_emf(m_, a, n, stream_), "ct emf");
   if (int rc = fill({{FILL_EC, AMR_FIELD_EMF}})) return rc;
   CK(launch_ct_face(m_, a, n, stream_), "ct face");
@@ -707,7 +790,7 @@ int Engine::ct2d(int step) {
 
 // primitive state of U (with the pressure / NaN traps of U2W("main")) and
 // the per-leaf wave-speed maximum and refinement criterion, in one kernel
-int Engine::dt_crit(bool want_grad) {
+int Engine::dt_crit(bool want_grad, const FillFuse *fuse) {
   DtArgs a{};
   a.tasks = d_tasks_.as<LeafTask>();
   a.inst = d_params_.as<InstParams>();
@@ -716,14 +799,37 @@ int Engine::dt_crit(bool want_grad) {
   a.grad = d_grad_.as<double>();
   a.err = d_err_.as<DevError>();
   a.want_grad = want_grad ? 1 : 0;
+  if (fuse) a.fuse = *fuse;
   CK(launch_dt_cell(m_, a, static_cast<int>(tasks_.size()), stream_), "dt kernel");
   prof_.launches += 1;
   return AMR_OK;
 }
 
-// main.cpp:129-202: ghost fills, stage 1 with CT, stage 2 with CT
+// main.cpp:129-202: ghost fills, stage 1 with CT, stage 2 with CT.  With
+// fused fills the nine fills of the step run inside the kernels that consume
+// them (the dt kernel takes the last), each kernel saving the next fill's
+// snapshots; the first fill's snapshots are a launch of their own.  Snapshot
+// buffers rotate over three, so that a kernel never writes the buffer it
+// reads.
 int Engine::enqueue_stage_sequence() {
   int rc;
+  if (fused_fills()) {
+    const FillPass f1 = fill_pass({{FILL_CC, AMR_FIELD_U}, {FILL_FC, AMR_FIELD_BI}}, 0, 0);
+    const FillPass f2 = fill_pass({{FILL_FC, AMR_FIELD_BI}, {FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}}, 1);
+    const FillPass f5 = fill_pass({{FILL_CC, AMR_FIELD_US}}, 1, 0);
+    const FillPass f6 = fill_pass({{FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}}, 2);
+    const FillPass f9 = fill_pass({{FILL_CC, AMR_FIELD_U}}, 2);
+    if ((rc = snap_only(f1))) return rc;
+    const FillFuse s1 = fill_fuse(&f1, &f2);
+    if ((rc = stage(1, &s1))) return rc;
+    if ((rc = ct2d(1, &f2, &f5, 2, 0))) return rc;     // EMF fill in buffer 2, Bis fill in 0
+    const FillFuse s2 = fill_fuse(&f5, &f6);
+    if ((rc = stage(2, &s2))) return rc;
+    if ((rc = ct2d(2, &f6, &f9, 0, 1))) return rc;     // EMF fill in buffer 0, Bi fill in 1
+    dt_fuse_ = fill_fuse(&f9, nullptr);
+    return AMR_OK;
+  }
+  dt_fuse_ = FillFuse{};
   if ((rc = fill({{FILL_CC, AMR_FIELD_U}, {FILL_FC, AMR_FIELD_BI}}))) return rc;
   if ((rc = stage(1))) return rc;
   if ((rc = fill({{FILL_FC, AMR_FIELD_BI}, {FILL_FC, AMR_FIELD_FF}, {FILL_FC, AMR_FIELD_GG}}))) return rc;
@@ -741,7 +847,7 @@ int Engine::enqueue_step() {
   if (int rc = enqueue_stage_sequence()) return rc;
   bool any_amr = false;
   for (int a : active_) any_amr |= inst_[a].cfg.maxlevs > 1;
-  if (int rc = dt_crit(any_amr)) return rc;
+  if (int rc = dt_crit(any_amr, dt_fuse_.apply.nseg ? &dt_fuse_ : nullptr)) return rc;
   const size_t nt = tasks_.size();
   CK(cudaMemcpyAsync(h_lambda_.p, d_lambda_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");
   CK(cudaMemcpyAsync(h_grad_.p, d_grad_.p, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream_), "d2h");

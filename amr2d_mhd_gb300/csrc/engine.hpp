@@ -11,6 +11,7 @@
 
 #include "../../include/amr2d_mhd.h"
 #include "amr_common.h"
+#include "ghost.cuh"
 #include "ghost_compile.hpp"
 #include "host_par.hpp"
 #include "ic.hpp"
@@ -135,9 +136,17 @@ class Engine {
   int launch_step();               // launch_step_work, bracketed by events when profiling
   int launch_step_work();          // enqueue_step directly or as a replayed CUDA graph
   int fill(std::initializer_list<std::pair<FillKind, int>> what);
-  int stage(int step);
-  int ct2d(int step);
-  int dt_crit(bool want_grad);
+  // the stage, CT and dt kernels; with `fuse` (or the FillPass arguments) the
+  // kernels also gather the fill they consume and save the next one's
+  // snapshots (fused fills, enqueue_stage_sequence)
+  int stage(int step, const FillFuse *fuse = nullptr);
+  int ct2d(int step, const FillPass *in = nullptr, const FillPass *out = nullptr, int emf_buf = 0, int bnew_buf = 0);
+  int dt_crit(bool want_grad, const FillFuse *fuse = nullptr);
+  // fused fills: a fill of `what` with its snapshots in rotating buffer `buf`
+  FillPass fill_pass(std::initializer_list<std::pair<FillKind, int>> what, int buf, int tile_seg = -1);
+  FillFuse fill_fuse(const FillPass *apply, const FillPass *save) const;
+  int snap_only(const FillPass &p);    // a fill's snapshot pass as a launch of its own
+  bool fused_fills() const { return fuse_fills_ && fuse_ok_; }
   int finish_step();
   struct AdmeshMarks {
     const uint8_t *ref, *crs;
@@ -155,6 +164,8 @@ class Engine {
   int ng_ = 2, n_ = 20, nn_ = 400;
   bool f32_ = false;
   bool split_ = true;              // stage as prim / faces / resid kernels (else fused k_stage)
+  bool fuse_fills_ = true;         // AMR2D_FUSED_FILLS=0: every ghost fill as launches of its own
+  bool fuse_ok_ = false;           // every active program is grouped by leaf block
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
   bool initialised_ = false;
@@ -180,6 +191,8 @@ class Engine {
   int layout_programs(bool relayout);
   DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_, d_snaps_;
   DevBuf d_treeops_, d_stage_, d_slots_, d_ctr_;
+  DevBuf d_snap3_;                 // fused fills: three rotating snapshot buffers
+  FillFuse dt_fuse_{};             // fused fills: the last fill of the step, gathered by the dt kernel
   HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_ops_, h_snaps_, h_tasks_;
   std::vector<GhostCompiler *> gcs_;  // one per compile thread
   HostPool pool_;                      // host threads of the parallel loops (remesh, compile, layout)

@@ -330,6 +330,8 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
   }
   touched_.clear();
   run_sequence(t, bounds);
+  out.clear();
+  snap_blk_.clear();
   // a pre-fill value that the fill overwrites is read from a saved copy
   auto snap_of = [&](int blk, int pos) {
     const size_t idx = static_cast<size_t>(blk) * nn_ + pos;
@@ -337,6 +339,7 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
       snap_stamp_[idx] = gen_;
       snap_row_[idx] = static_cast<int>(out.snaps.size());
       out.snaps.push_back(GhostSnap{slot[blk], pos});
+      snap_blk_.push_back(blk);
     }
     return snap_row_[idx];
   };
@@ -352,45 +355,85 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     if (e.blk == blk && e.pos == pos + 1) return false;  // unchanged cell
     return !overwritten(e.blk, e.pos);
   };
-  out.ops.reserve(out.ops.size() + touched_.size());
-  for (const int idx : touched_) {
-    const Desc &d = cur_[idx];
-    const int blk = idx / nn_, pos = idx % nn_;
-    if (d.type == GOP_COPY && d.blk == blk && d.pos == pos) continue;  // unchanged
-    if (emit_stamp_[idx] == gen_) continue;                             // second cell of a pair
-    emit_stamp_[idx] = gen_;
-    GhostOp op{};
-    op.dst_slot = slot[blk];
-    op.dst_pos = static_cast<int16_t>(pos);
-    if (d.type == GOP_COPY) {
-      if (overwritten(d.blk, d.pos)) {
-        op.type = GOP_SNAP;
-        op.src_slot = snap_of(d.blk, d.pos);
+  // emitted block by block (the ops of a block are consecutive, so that the
+  // block's kernel can gather them), each block's cells in position order
+  const int nb = t.lastActive;
+  blk_count_.assign(static_cast<size_t>(nb), 0);
+  for (const int idx : touched_) blk_count_[idx / nn_]++;
+  out.ops.reserve(touched_.size());
+  out.op_start.assign(static_cast<size_t>(nb) + 1, 0);
+  bool leaves = true;
+  for (int blk = 0; blk < nb; blk++) {
+    out.op_start[blk] = static_cast<int>(out.ops.size());
+    if (!blk_count_[blk]) continue;
+    for (int pos = 0; pos < nn_; pos++) {
+      const int idx = blk * nn_ + pos;
+      if (stamp_[idx] != gen_) continue;
+      const Desc &d = cur_[idx];
+      if (d.type == GOP_COPY && d.blk == blk && d.pos == pos) continue;  // unchanged
+      if (emit_stamp_[idx] == gen_) continue;                             // second cell of a pair
+      emit_stamp_[idx] = gen_;
+      GhostOp op{};
+      op.dst_slot = slot[blk];
+      op.dst_pos = static_cast<int16_t>(pos);
+      if (d.type == GOP_COPY) {
+        if (overwritten(d.blk, d.pos)) {
+          op.type = GOP_SNAP;
+          op.src_slot = snap_of(d.blk, d.pos);
+        } else {
+          op.type = GOP_COPY;
+          op.src_slot = slot[d.blk];
+          op.src_pos = d.pos;
+          if (pairs_with(blk, pos, d)) {
+            op.type = GOP_COPY2;
+            emit_stamp_[idx + 1] = gen_;
+          }
+        }
       } else {
-        op.type = GOP_COPY;
-        op.src_slot = slot[d.blk];
-        op.src_pos = d.pos;
-        if (pairs_with(blk, pos, d)) {
-          op.type = GOP_COPY2;
-          emit_stamp_[idx + 1] = gen_;
+        const int c[4] = {d.pos, d.pos + n_, d.pos + 1, d.pos + 1 + n_};  // sum_irjr order
+        bool hazard = false;
+        for (int q = 0; q < 4; q++) hazard |= overwritten(d.blk, c[q]);
+        if (!hazard) {
+          op.type = GOP_FINE;
+          op.src_slot = slot[d.blk];
+          op.src_pos = d.pos;
+        } else {  // four consecutive rows, whether or not each was saved before
+          op.type = GOP_SFINE;
+          op.src_slot = static_cast<int>(out.snaps.size());
+          for (int q = 0; q < 4; q++) {
+            out.snaps.push_back(GhostSnap{slot[d.blk], c[q]});
+            snap_blk_.push_back(d.blk);
+          }
         }
       }
-    } else {
-      const int c[4] = {d.pos, d.pos + n_, d.pos + 1, d.pos + 1 + n_};  // sum_irjr order
-      bool hazard = false;
-      for (int q = 0; q < 4; q++) hazard |= overwritten(d.blk, c[q]);
-      if (!hazard) {
-        op.type = GOP_FINE;
-        op.src_slot = slot[d.blk];
-        op.src_pos = d.pos;
-      } else {  // four consecutive rows, whether or not each was saved before
-        op.type = GOP_SFINE;
-        op.src_slot = static_cast<int>(out.snaps.size());
-        for (int q = 0; q < 4; q++) out.snaps.push_back(GhostSnap{slot[d.blk], c[q]});
-      }
+      out.ops.push_back(op);
     }
-    out.ops.push_back(op);
+    if (out.op_start[blk] != static_cast<int>(out.ops.size()) && !t.leafs[blk]) leaves = false;
   }
+  out.op_start[nb] = static_cast<int>(out.ops.size());
+  // snapshots grouped by the block they save from, keeping their order
+  // within a block (the four rows of an SFINE stay consecutive)
+  const int ns = static_cast<int>(out.snaps.size());
+  out.snap_start.assign(static_cast<size_t>(nb) + 1, 0);
+  if (ns) {
+    for (int r = 0; r < ns; r++) out.snap_start[snap_blk_[r] + 1]++;
+    for (int b2 = 0; b2 < nb; b2++) {
+      if (out.snap_start[b2 + 1] && !t.leafs[b2]) leaves = false;
+      out.snap_start[b2 + 1] += out.snap_start[b2];
+    }
+    blk_count_.assign(out.snap_start.begin(), out.snap_start.end() - 1);  // next free row per block
+    snap_perm_.resize(static_cast<size_t>(ns));
+    std::vector<GhostSnap> grouped(static_cast<size_t>(ns));
+    for (int r = 0; r < ns; r++) {
+      const int g = blk_count_[snap_blk_[r]]++;
+      snap_perm_[r] = g;
+      grouped[g] = out.snaps[r];
+    }
+    out.snaps.swap(grouped);
+    for (GhostOp &op : out.ops)
+      if (op.type == GOP_SNAP || op.type == GOP_SFINE) op.src_slot = snap_perm_[op.src_slot];
+  }
+  out.by_block = leaves;
 }
 
 }  // namespace amr

@@ -23,18 +23,32 @@ namespace amr {
 // (boundaryec.cpp)
 enum FillKind { FILL_CC = 0, FILL_FC = 1, FILL_EC = 2 };
 
+// The program of one instance, grouped by block: the ops that write block
+// b's ghost cells are ops[op_start[b], op_start[b+1]) and the snapshots of
+// b's cells snaps[snap_start[b], snap_start[b+1]).  `by_block` is false when
+// a destination or a snapshot lies in a block that is not a leaf (the fill
+// can then only run as a launch of its own).
 struct GhostProgram {
   std::vector<GhostOp> ops;
   std::vector<GhostSnap> snaps;
-  void clear() { ops.clear(); snaps.clear(); }
+  std::vector<int> op_start, snap_start;
+  bool by_block = false;
+  void clear() {
+    ops.clear();
+    snaps.clear();
+    op_start.clear();
+    snap_start.clear();
+    by_block = false;
+  }
 };
 
 class GhostCompiler {
  public:
   // n = block edge with ghosts, ng = ghost layers
   GhostCompiler(int n, int ng) : n_(n), ng_(ng) {}
-  // Appends the gathers of one instance's ghost fill (any kind of field) to
-  // `out`.  `slot` maps block IDs to physical device slots.
+  // Writes the gathers of one instance's ghost fill (any kind of field) to
+  // `out` (cleared first), grouped by block.  `slot` maps block IDs to
+  // physical device slots.
   void compile(const Tree &t, const std::vector<Bound> &bounds, const int *slot, GhostProgram &out);
 
  private:
@@ -57,6 +71,9 @@ class GhostCompiler {
   std::vector<uint32_t> snap_stamp_;
   std::vector<int> snap_row_;
   std::vector<uint32_t> emit_stamp_;  // cell already written by an emitted op
+  std::vector<int> blk_count_;        // touched cells per block
+  std::vector<int> snap_blk_;         // block of each snapshot row, in emission order
+  std::vector<int> snap_perm_;        // emission row -> grouped row
 };
 
 }  // namespace amr

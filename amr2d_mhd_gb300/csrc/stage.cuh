@@ -9,6 +9,7 @@
 #pragma once
 
 #include "amr_common.h"
+#include "ghost.cuh"
 #include "physics.cuh"
 
 namespace amr {
@@ -35,6 +36,8 @@ struct StageArgs {
   unsigned *ctr;      // [2] block counter and finished-CTA counter of k_stage_dyn (zero between launches)
   int step;
   int ntasks;         // leaf blocks (k_stage_dyn)
+  FillFuse fuse;      // fused fills: the qin fill gathered first (mirrored in
+                      // shared memory), the flux fill's snapshots saved last
 };
 
 // First statement of every kernel of the step: when the kernel was launched
@@ -200,6 +203,12 @@ __device__ __forceinline__ bool stage_block(const StageArgs &a, int ti, uint64_t
     bulk_stage_wait(bar, phase);  // let the copy land before the CTA's shared memory is released
     return false;
   }
+  // fused fill: the block's ghost cells of qin (and of B), into global memory
+  // and over the staged copy, which held the values from before the fill
+  if (a.fuse.apply.nseg) {
+    fill_apply_task<N, S>(a.fuse, task, tid, nthr, sU);
+    __syncthreads();
+  }
 
   // 1. primitive variables of every cell (U2W / Us2W), with the traps (in
   // place unless the conserved state is kept)
@@ -310,6 +319,9 @@ __device__ __forceinline__ bool stage_block(const StageArgs &a, int ti, uint64_t
     if (a.step == 1) out[e] = q - dt * res;                         // Us = U - dt res
     else out[e] = T(0.5) * (out[e] + q - dt * res);                 // U = (U + Us - dt res)/2
   }
+  // fused fill: snapshots of the next fill (ff, gg and B, whose writes by
+  // this CTA precede the barrier after step 2)
+  if (a.fuse.save.nseg) fill_save_task<N>(a.fuse, task, tid, nthr);
   return true;
 }
 

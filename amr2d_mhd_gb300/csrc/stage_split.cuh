@@ -23,6 +23,8 @@ struct SplitArgs {
   unsigned *ctr;      // [2] work counter and finished-CTA counter of k_faces_dyn (zero between launches)
   int step;
   int ntasks;
+  FillFuse fuse;      // fused fills: the qin fill gathered by k_prim_task, the
+                      // flux fill's snapshots saved by k_resid
 };
 
 // U2W / Us2W (meshblock.cpp:119-179) for every cell of every leaf
@@ -51,6 +53,37 @@ __global__ void __launch_bounds__(512) k_prim(SplitArgs a) {
 #pragma unroll
   for (int k = 0; k < 8; k++) bad |= bits_nan(w[k]);
   if (bad) dev_fail(a.err, DERR_NAN, task.slot, i, j, 0.0);
+}
+
+// the same with the fill of qin (and B) fused in: one CTA per leaf gathers
+// its block's ghost cells, then converts the block
+template <int NG, typename S>
+__global__ void __launch_bounds__(256) k_prim_task(SplitArgs a) {
+  pdl_wait();
+  using G = Geo<NG>;
+  constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
+  const LeafTask task = a.tasks[blockIdx.x];
+  fill_apply_task<N, double>(a.fuse, task, threadIdx.x, blockDim.x, nullptr);
+  __syncthreads();
+  const size_t base = static_cast<size_t>(task.slot) * 8 * NN;
+  const S *Q = static_cast<const S *>(a.qin) + base;
+  S *W = static_cast<S *>(a.W) + base;
+  const double gamma = a.inst[task.inst].gamma;
+  for (int c = threadIdx.x; c < NN; c += blockDim.x) {
+    S u[8], w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = Q[k * NN + c];
+    cons2prim_cell<S>(u, w, gamma);
+#pragma unroll
+    for (int k = 0; k < 8; k++) W[k * NN + c] = w[k];
+    const int i = c % N, j = c / N;
+    if (w[4] <= S(0) && i > LO && i < HI + 1 && j > LO && j < HI + 1)
+      dev_fail(a.err, DERR_PRESSURE, task.slot, i, j, static_cast<double>(w[4]));
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 8; k++) bad |= bits_nan(w[k]);
+    if (bad) dev_fail(a.err, DERR_NAN, task.slot, i, j, 0.0);
+  }
 }
 
 // MUSCL2D.cpp:24-116 for one face of one leaf: x faces (i+1/2, j) for i, j in
@@ -180,6 +213,8 @@ __global__ void __launch_bounds__(512) k_resid(SplitArgs a) {
   using T = S;
   constexpr int N = G::N, NN = G::NN, LO = G::LO, HI = G::HI;
   const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  // fused fill: the flux fill's snapshots (this kernel writes only qout)
+  if (a.fuse.save.nseg) fill_save_all<N>(a.fuse, e, static_cast<size_t>(gridDim.x) * blockDim.x);
   if (e >= static_cast<size_t>(a.ntasks) * 8 * NN) return;
   const int t = static_cast<int>(e / (8 * NN)), r = static_cast<int>(e % (8 * NN));
   const int c = r % NN;

@@ -10,6 +10,10 @@
 #include "ghost_compile.hpp"
 #include "host_par.hpp"
 
+static int g_last_by_block = -1;
+// 1 if the last compiled program had every destination and snapshot in a leaf
+extern "C" int ghost_shim_last_by_block() { return g_last_by_block; }
+
 extern "C" int ghost_shim_apply(int last_active, const int *lp, const int *icoord, const unsigned char *leafs,
                                 int maxlevs, int nrx, int nry, int periodic, int ng, int kind, int nv,
                                 double *field, int *n_ops, int *n_snaps) {
@@ -31,6 +35,24 @@ extern "C" int ghost_shim_apply(int last_active, const int *lp, const int *icoor
   GhostCompiler gc(n, ng);
   GhostProgram p;
   gc.compile(t, bounds, slot.data(), p);
+  // grouping by block: block b's ops write only b, its snapshots read only b
+  if (p.op_start.size() != static_cast<size_t>(last_active) + 1 ||
+      p.snap_start.size() != static_cast<size_t>(last_active) + 1 || p.op_start[0] != 0 || p.snap_start[0] != 0 ||
+      p.op_start[last_active] != static_cast<int>(p.ops.size()) ||
+      p.snap_start[last_active] != static_cast<int>(p.snaps.size()))
+    return -3;
+  bool leaves_only = true;
+  for (int b = 0; b < last_active; b++) {
+    if (p.op_start[b + 1] < p.op_start[b] || p.snap_start[b + 1] < p.snap_start[b]) return -3;
+    for (int o = p.op_start[b]; o < p.op_start[b + 1]; o++)
+      if (p.ops[o].dst_slot != slot[b]) return -3;
+    for (int r = p.snap_start[b]; r < p.snap_start[b + 1]; r++)
+      if (p.snaps[r].slot != slot[b]) return -3;
+    if ((p.op_start[b + 1] > p.op_start[b] || p.snap_start[b + 1] > p.snap_start[b]) && !t.leafs[b])
+      leaves_only = false;
+  }
+  if (leaves_only != p.by_block) return -3;
+  g_last_by_block = p.by_block ? 1 : 0;
   std::vector<double> snap(p.snaps.size() * 8);
   for (size_t i = 0; i < p.snaps.size(); i++)
     for (int k = 0; k < nv; k++)

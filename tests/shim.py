@@ -30,6 +30,7 @@ def lib():
             [ctypes.c_void_p] * 3
         L.tree_shim_admesh.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int] + \
             [ctypes.c_void_p] * 4
+        L.ghost_shim_last_by_block.argtypes = []
         L.host_pool_shim.argtypes = [ctypes.c_int] * 3
         L.tree_shim_check.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 5 + \
             [ctypes.c_char_p, ctypes.c_int]
@@ -48,6 +49,12 @@ def ghost_apply(st, kind, nv, field, maxlevs, ng=2, nroots=(2, 2), periodic=Fals
                                 ctypes.byref(no), ctypes.byref(ns))
     assert rc == 0
     return a, no.value, ns.value
+
+
+def last_by_block():
+    """1 if the program of the last ghost_apply call had every written and
+    every saved cell in a leaf block (the fused fills' condition)."""
+    return lib().ghost_shim_last_by_block()
 
 
 def admesh(st, grad, maxlevs, ng=2, nroots=(2, 2), periodic=False, cap=100000, marks=None):

@@ -5,7 +5,7 @@ import pytest
 
 from oracle import pyoracle as P
 from parity_util import oracle_kw
-from shim import admesh, ghost_apply, host_pool, tree_check
+from shim import admesh, ghost_apply, host_pool, last_by_block, tree_check
 
 GHOST_CASES = [("BWx", "MC", 4, 2, 3), ("rotor", "MC", 5, 2, 30), ("BWx", "WENO5", 3, 4, 10),
                ("rotor", "WENO5", 3, 4, 25)]
@@ -25,6 +25,9 @@ def test_ghost_program_matches_sequential_fill(ic, lim, L, ng, steps):
         got, nops, _ = ghost_apply(st, kind, nv, f, L, ng)
         assert nops > 0
         assert np.array_equal(ref, got), (kind, nv, int((ref != got).sum()))
+        # grouped by block (checked inside the shim), all in leaves: the fills
+        # can run inside the step's per-block kernels
+        assert last_by_block() == 1
 
 
 @pytest.mark.parametrize("seed,periodic", [(11, False), (12, False), (13, True)])
@@ -51,6 +54,7 @@ def test_ghost_program_on_random_mark_trees(seed, periodic):
             f = rng.standard_normal((st["lastActive"], nv, 20, 20))
             got, _, _ = ghost_apply(st, kind, nv, f, L, 2, nroots, periodic)
             assert np.array_equal(o.fill(f, kind), got), (it, kind)
+            assert last_by_block() == 1
 
 
 def test_ghost_program_periodic_16_roots():
