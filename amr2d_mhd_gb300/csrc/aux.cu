@@ -128,6 +128,43 @@ cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int n, cudaStream_t
   return m.ng == 2 ? launch_k(m.pdl, k_ct_face<2>, n, 128, 0, s, a) : launch_k(m.pdl, k_ct_face<4>, n, 128, 0, s, a);
 }
 
+// one cooperative launch (all CTAs resident: grid = SMs x resident CTAs per
+// SM, capped at the task count), not a programmatic dependent
+cudaError_t launch_ct_coop(const Method &m, const CtArgs &a, const FillFuse &f_emf, const FillFuse &f_face,
+                           const FillFuse &f_cell, unsigned *bar, cudaStream_t s) {
+  if (a.ntasks <= 0) return cudaSuccess;
+  static int per_sm[2][2] = {{0, 0}, {0, 0}}, sms = 0;
+  const int gi = m.ng == 2 ? 0 : 1, si = m.f32 ? 1 : 0;
+  void (*k)(CtArgs, FillFuse, FillFuse, FillFuse, unsigned *) =
+      m.ng == 2 ? (m.f32 ? k_ct_coop<2, float> : k_ct_coop<2, double>)
+                : (m.f32 ? k_ct_coop<4, float> : k_ct_coop<4, double>);
+  if (!sms) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  int &ps = per_sm[gi][si];
+  if (!ps) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, k, 128, 0);
+    if (e != cudaSuccess) return e;
+    if (ps < 1) return cudaErrorInvalidConfiguration;
+  }
+  const int cap = sms * ps;
+  const int grid = a.ntasks < cap ? a.ntasks : cap;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, a, f_emf, f_face, f_cell, bar);
+}
+
 cudaError_t launch_diffuse(const Method &m, const CtArgs &a, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   return AMR_DISPATCH_NG_S_PDL(m, k_diffuse, n, 128, 0, s, a);

@@ -55,6 +55,7 @@ struct CtArgs {
   void *q;                // cell state corrected by the face average
   DevError *err;
   int step;
+  int ntasks;             // leaf tasks (k_ct_coop)
   FillFuse fuse;          // fused fills: the consumed fill first, the next one's snapshots last
 };
 
@@ -122,17 +123,15 @@ __device__ __forceinline__ void ct_emf_upwind(const CtArgs &a, const LeafTask &t
   }
 }
 
-// CT2D.cpp:16-26 corner EMF for i, j in [1, N)
+// CT2D.cpp:16-26 corner EMF for i, j in [1, N), block of task t (sp, sC:
+// shared scratch of the upwind form)
 template <int NG, typename S>
-__global__ void k_ct_emf(CtArgs a) {
-  pdl_wait();
+__device__ __forceinline__ void ct_emf_block(const CtArgs &a, const FillFuse &f, const LeafTask &t, S *sp, S *sC) {
   constexpr int N = Geo<NG>::N, NN = N * N;
-  const LeafTask t = a.tasks[blockIdx.x];
-  fuse_apply<N>(a.fuse, t);
+  fuse_apply<N>(f, t);
   if (a.inst[t.inst].ct_type == 2) {
-    __shared__ S sp[NN], sC[NN];
     ct_emf_upwind<NG, S>(a, t, sp, sC);
-    fuse_save<N>(a.fuse, t);
+    fuse_save<N>(f, t);
     return;
   }
   const S *ff = static_cast<const S *>(a.ff) + static_cast<size_t>(t.slot) * 8 * NN;
@@ -149,16 +148,14 @@ __global__ void k_ct_emf(CtArgs a) {
     const S f6a = ff[6 * NN + (j - 1) * N + i], f6b = ff[6 * NN + c];
     E[c] = static_cast<double>(S(0.25) * ((g5a + g5b) - (f6a + f6b)));
   }
-  fuse_save<N>(a.fuse, t);
+  fuse_save<N>(f, t);
 }
 
 // CT2D.cpp:78-92 face update with the RK2 combine
 template <int NG>
-__global__ void k_ct_face(CtArgs a) {
-  pdl_wait();
+__device__ __forceinline__ void ct_face_block(const CtArgs &a, const FillFuse &f, const LeafTask &t) {
   constexpr int N = Geo<NG>::N, NN = N * N;
-  const LeafTask t = a.tasks[blockIdx.x];
-  fuse_apply<N>(a.fuse, t);
+  fuse_apply<N>(f, t);
   const double dt = a.inst[t.inst].dt;
   const double *E = a.EMF + static_cast<size_t>(t.slot) * NN;
   const double *B0 = a.Bsrc + static_cast<size_t>(t.slot) * 2 * NN;
@@ -173,17 +170,15 @@ __global__ void k_ct_face(CtArgs a) {
     if (a.step == 1) B1[NN + c] = B0[NN + c] - dt * res;
     else B1[NN + c] = 0.5 * (B0[NN + c] + B1[NN + c] - dt * res);
   }
-  fuse_save<N>(a.fuse, t);
+  fuse_save<N>(f, t);
 }
 
 // CT2D.cpp:95-123 cell B := face average, with the energy correction, on
 // every cell of the block (ghosts included)
 template <int NG, typename S>
-__global__ void k_ct_cell(CtArgs a) {
-  pdl_wait();
+__device__ __forceinline__ void ct_cell_block(const CtArgs &a, const FillFuse &f, const LeafTask &t) {
   constexpr int N = Geo<NG>::N, NN = N * N;
-  const LeafTask t = a.tasks[blockIdx.x];
-  fuse_apply<N>(a.fuse, t);
+  fuse_apply<N>(f, t);
   const double *B = a.Bnew + static_cast<size_t>(t.slot) * 2 * NN;
   S *q = static_cast<S *>(a.q) + static_cast<size_t>(t.slot) * 8 * NN;
   for (int c = threadIdx.x; c < NN; c += blockDim.x) {
@@ -199,7 +194,80 @@ __global__ void k_ct_cell(CtArgs a) {
     q[5 * NN + c] = bx;
     q[6 * NN + c] = by;
   }
-  fuse_save<N>(a.fuse, t);
+  fuse_save<N>(f, t);
+}
+
+template <int NG, typename S>
+__global__ void k_ct_emf(CtArgs a) {
+  pdl_wait();
+  constexpr int NN = Geo<NG>::NN;
+  __shared__ S sp[NN], sC[NN];
+  ct_emf_block<NG, S>(a, a.fuse, a.tasks[blockIdx.x], sp, sC);
+}
+
+template <int NG>
+__global__ void k_ct_face(CtArgs a) {
+  pdl_wait();
+  ct_face_block<NG>(a, a.fuse, a.tasks[blockIdx.x]);
+}
+
+template <int NG, typename S>
+__global__ void k_ct_cell(CtArgs a) {
+  pdl_wait();
+  ct_cell_block<NG, S>(a, a.fuse, a.tasks[blockIdx.x]);
+}
+
+// Barrier of all CTAs of a cooperative grid (all resident at once): the last
+// CTA to arrive zeroes the count and advances the generation.  The wait is
+// bounded; a CTA that gives up records DERR_TIMEOUT and the barrier returns
+// false in every thread of that CTA.
+constexpr long kGridSpinLimit = 1L << 24;   // x 64 ns sleeps: about a second
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, DevError *err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    int good = 1;
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      bar[0] = 0;
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      for (long it = 0; *gen == g; it++) {
+        if (it > kGridSpinLimit) { good = 0; break; }
+        __nanosleep(64);
+      }
+      if (!good) dev_fail(err, DERR_TIMEOUT, -1, static_cast<int>(blockIdx.x), 0, 0.0);
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// CT2D.cpp:11-124 of one RK stage as one cooperative launch: the EMF, the
+// face update and the cell correction, each over every leaf (a CTA takes
+// tasks blockIdx.x, + gridDim.x, ...), separated by grid barriers.  The two
+// fills CT2D makes between them (boundaryec on the EMF, boundaryfc on the new
+// face field) are fused: gathered by the phase that consumes them, their
+// snapshots saved by the phase before.
+template <int NG, typename S>
+__global__ void __launch_bounds__(128) k_ct_coop(CtArgs a, FillFuse f_emf, FillFuse f_face, FillFuse f_cell,
+                                                 unsigned *bar) {
+  pdl_wait();
+  constexpr int NN = Geo<NG>::NN;
+  __shared__ S sp[NN], sC[NN];
+  for (int ti = blockIdx.x; ti < a.ntasks; ti += gridDim.x) {
+    ct_emf_block<NG, S>(a, f_emf, a.tasks[ti], sp, sC);
+    __syncthreads();  // the upwind form's shared scratch is reused by the next task
+  }
+  if (!grid_barrier(bar, a.err)) return;
+  for (int ti = blockIdx.x; ti < a.ntasks; ti += gridDim.x) ct_face_block<NG>(a, f_face, a.tasks[ti]);
+  if (!grid_barrier(bar, a.err)) return;
+  for (int ti = blockIdx.x; ti < a.ntasks; ti += gridDim.x) ct_cell_block<NG, S>(a, f_cell, a.tasks[ti]);
 }
 
 // diffusivity.cpp:6-17 on the blocks flagged TASK_DIFFUSE (main.cpp:190-193:

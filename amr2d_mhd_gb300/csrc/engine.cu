@@ -80,7 +80,7 @@ Engine::~Engine() {
   for (void *p : {U_, Us_, ff_, gg_, W_}) if (p) cudaFree(p);
   for (double *p : {Bi_, Bis_, EMF_}) if (p) cudaFree(p);
   for (DevBuf *b : {&d_tasks_, &d_params_, &d_lambda_, &d_grad_, &d_err_, &d_snap_, &d_treeops_, &d_stage_, &d_slots_,
-                    &d_ctr_})
+                    &d_ctr_, &d_snap3_, &d_bar_})
     b->release();
   d_ops_.release();
   d_snaps_.release();
@@ -158,6 +158,7 @@ int Engine::create(const amr_config *cfgs, int n) {
   if (const char *g = std::getenv("AMR2D_GRAPHS")) graph_on_ = std::strcmp(g, "0") != 0;
   if (const char *p = std::getenv("AMR2D_PDL")) m_.pdl = std::strcmp(p, "0") != 0 ? 1 : 0;
   if (const char *f = std::getenv("AMR2D_FUSED_FILLS")) fuse_fills_ = std::strcmp(f, "0") != 0;
+  if (const char *f = std::getenv("AMR2D_CT_COOP")) ct_coop_ = std::strcmp(f, "0") != 0;
   if (const char *f = std::getenv("AMR2D_FACE_KERNEL"))
     m_.persistent = !std::strcmp(f, "dynamic") ? 2 : (!std::strcmp(f, "persistent") ? 1 : 0);
   ng_ = m_.ng;
@@ -199,6 +200,8 @@ int Engine::create(const amr_config *cfgs, int n) {
   CK(cudaMemsetAsync(d_err_.p, 0, sizeof(DevError), stream_), "memset");
   CK(d_ctr_.ensure(2 * sizeof(unsigned)), "alloc");   // k_faces_dyn's counters, zero between launches
   CK(cudaMemsetAsync(d_ctr_.p, 0, 2 * sizeof(unsigned), stream_), "memset");
+  CK(d_bar_.ensure(2 * sizeof(unsigned)), "alloc");   // k_ct_coop's grid barrier (count, generation)
+  CK(cudaMemsetAsync(d_bar_.p, 0, 2 * sizeof(unsigned), stream_), "memset");
   CK(h_err_.ensure(sizeof(DevError)), "alloc");
   CK(h_params_.ensure(sizeof(InstParams) * n), "alloc");
   CK(d_params_.ensure(sizeof(InstParams) * n), "alloc");
@@ -767,9 +770,16 @@ int Engine::ct2d(int step, const FillPass *in, const FillPass *out, int emf_buf,
   a.err = d_err_.as<DevError>();
   a.step = step;
   const int n = static_cast<int>(tasks_.size());
+  a.ntasks = n;
   if (in) {
     const FillPass emf = fill_pass({{FILL_EC, AMR_FIELD_EMF}}, emf_buf);
     const FillPass bnew = fill_pass({{FILL_FC, step == 1 ? AMR_FIELD_BIS : AMR_FIELD_BI}}, bnew_buf);
+    if (ct_coop_) {  // one cooperative launch, grid barriers between the phases
+      CK(launch_ct_coop(m_, a, fill_fuse(in, &emf), fill_fuse(&emf, &bnew), fill_fuse(&bnew, out),
+                        d_bar_.as<unsigned>(), stream_), "ct kernel");
+      prof_.launches += 1;
+      return AMR_OK;
+    }
     a.fuse = fill_fuse(in, &emf);
     CK(launch_ct_emf(m_, a, n, stream_), "ct emf");
     a.fuse = fill_fuse(&emf, &bnew);

@@ -166,6 +166,7 @@ class Engine {
   bool split_ = true;              // stage as prim / faces / resid kernels (else fused k_stage)
   bool fuse_fills_ = true;         // AMR2D_FUSED_FILLS=0: every ghost fill as launches of its own
   bool fuse_ok_ = false;           // every active program is grouped by leaf block
+  bool ct_coop_ = true;            // fused fills: CT2D as one cooperative launch (AMR2D_CT_COOP=0: three)
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
   bool initialised_ = false;
@@ -192,6 +193,7 @@ class Engine {
   DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_, d_snaps_;
   DevBuf d_treeops_, d_stage_, d_slots_, d_ctr_;
   DevBuf d_snap3_;                 // fused fills: three rotating snapshot buffers
+  DevBuf d_bar_;                   // grid barrier of the cooperative CT launch
   FillFuse dt_fuse_{};             // fused fills: the last fill of the step, gathered by the dt kernel
   HostBuf h_params_, h_lambda_, h_grad_, h_err_, h_ops_, h_snaps_, h_tasks_;
   std::vector<GhostCompiler *> gcs_;  // one per compile thread

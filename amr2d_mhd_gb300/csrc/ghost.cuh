@@ -63,34 +63,58 @@ __device__ __forceinline__ F fine_value(int kind, int k, F a00, F a01, F a10, F 
   return a00;
 }
 
-// variable k of one gather; `tile` (may be null) is the destination block's
-// copy of the field in shared memory ([nv][N*N]), written as well
+// the value(s) of variable k of one gather, computed in the field's type F
+// (a pair gives two); and their store to the destination and, when `tile` is
+// not null, to the destination block's copy of the field in shared memory
+// ([nv][N*N])
 template <int N, typename F>
-__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, int k, const double *snap,
-                                                F *tile = nullptr) {
+__device__ __forceinline__ void ghost_gather(const GhostSeg &s, const GhostOp &op, int k, const double *snap, F &v0,
+                                             F &v1) {
   constexpr int NN = N * N;
-  F *fld = static_cast<F *>(s.field);
-  F *dst = fld + (static_cast<size_t>(op.dst_slot) * s.nv + k) * NN + op.dst_pos;
+  const F *fld = static_cast<const F *>(s.field);
   if (op.type == GOP_COPY2) {  // even positions in an even-sized plane: aligned pair
     using P2 = typename std::conditional<sizeof(F) == 4, float2, double2>::type;
     const P2 v =
         *reinterpret_cast<const P2 *>(fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos);
+    v0 = v.x;
+    v1 = v.y;
+    return;
+  }
+  if (op.type == GOP_COPY || op.type == GOP_FINE) {
+    const F *c = fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos;
+    v0 = op.type == GOP_COPY ? c[0] : fine_value<F>(s.kind, k, c[0], c[N], c[1], c[1 + N]);
+  } else {
+    const double *r = snap + static_cast<size_t>(op.src_slot) * 8 + k;
+    v0 = op.type == GOP_SNAP ? static_cast<F>(r[0])
+                             : fine_value<F>(s.kind, k, static_cast<F>(r[0]), static_cast<F>(r[8]),
+                                             static_cast<F>(r[16]), static_cast<F>(r[24]));
+  }
+}
+
+template <int N, typename F>
+__device__ __forceinline__ void ghost_put(const GhostSeg &s, const GhostOp &op, int k, F v0, F v1, F *tile) {
+  constexpr int NN = N * N;
+  F *dst = static_cast<F *>(s.field) + (static_cast<size_t>(op.dst_slot) * s.nv + k) * NN + op.dst_pos;
+  if (op.type == GOP_COPY2) {
+    using P2 = typename std::conditional<sizeof(F) == 4, float2, double2>::type;
+    P2 v;
+    v.x = v0;
+    v.y = v1;
     *reinterpret_cast<P2 *>(dst) = v;
     if (tile) *reinterpret_cast<P2 *>(tile + k * NN + op.dst_pos) = v;
     return;
   }
-  F v;
-  if (op.type == GOP_COPY || op.type == GOP_FINE) {
-    const F *c = fld + (static_cast<size_t>(op.src_slot) * s.nv + k) * NN + op.src_pos;
-    v = op.type == GOP_COPY ? c[0] : fine_value<F>(s.kind, k, c[0], c[N], c[1], c[1 + N]);
-  } else {
-    const double *r = snap + static_cast<size_t>(op.src_slot) * 8 + k;
-    v = op.type == GOP_SNAP ? static_cast<F>(r[0])
-                            : fine_value<F>(s.kind, k, static_cast<F>(r[0]), static_cast<F>(r[8]),
-                                            static_cast<F>(r[16]), static_cast<F>(r[24]));
-  }
-  *dst = v;
-  if (tile) tile[k * NN + op.dst_pos] = v;
+  *dst = v0;
+  if (tile) tile[k * NN + op.dst_pos] = v0;
+}
+
+// variable k of one gather (`tile` as for ghost_put)
+template <int N, typename F>
+__device__ __forceinline__ void ghost_apply_one(const GhostSeg &s, const GhostOp &op, int k, const double *snap,
+                                                F *tile = nullptr) {
+  F v0, v1 = F(0.);
+  ghost_gather<N, F>(s, op, k, snap, v0, v1);
+  ghost_put<N, F>(s, op, k, v0, v1, tile);
 }
 
 // ------------------------------------------------------------ fused fills
@@ -136,6 +160,66 @@ __device__ __forceinline__ void fill_apply_task(const FillFuse &f, const LeafTas
   const int n = t.op_count;
   const int total = n * f.apply.rows;
   for (int e = tid; e < total; e += nthr) {
+    const int row = e / n;
+    const GhostOp op = f.ops[t.op_begin + (e - row * n)];
+    int q, k;
+    const GhostSeg s = pass_seg(f.apply, row, q, k);
+    const double *snap = f.apply.snapbuf + static_cast<size_t>(q) * f.nsnaps * 8;
+    TileT *tl = q == f.apply.tile_seg ? tile : nullptr;
+    if (s.f32) ghost_apply_one<N, float>(s, op, k, snap, reinterpret_cast<float *>(tl));
+    else ghost_apply_one<N, double>(s, op, k, snap, reinterpret_cast<double *>(tl));
+  }
+}
+
+// The first gather of a thread, loaded ahead (while the fused stage
+// kernel's bulk copy is in flight) and stored by fill_apply_task_after; the
+// values are held as double (exact for float fields).
+struct FillPre {
+  GhostOp op;
+  double v0, v1;
+  int row;
+  bool on;
+};
+
+template <int N>
+__device__ __forceinline__ FillPre fill_prefetch(const FillFuse &f, const LeafTask &t, int tid) {
+  FillPre p{};
+  const int n = t.op_count;
+  p.on = f.apply.nseg != 0 && tid < n * f.apply.rows;
+  if (!p.on) return p;
+  p.row = tid / n;
+  p.op = f.ops[t.op_begin + (tid - p.row * n)];
+  int q, k;
+  const GhostSeg s = pass_seg(f.apply, p.row, q, k);
+  const double *snap = f.apply.snapbuf + static_cast<size_t>(q) * f.nsnaps * 8;
+  if (s.f32) {
+    float a = 0.f, b = 0.f;
+    ghost_gather<N, float>(s, p.op, k, snap, a, b);
+    p.v0 = a;
+    p.v1 = b;
+  } else {
+    ghost_gather<N, double>(s, p.op, k, snap, p.v0, p.v1);
+  }
+  return p;
+}
+
+// fill_apply_task with the thread's first gather already loaded in `p`
+template <int N, typename TileT>
+__device__ __forceinline__ void fill_apply_task_after(const FillFuse &f, const LeafTask &t, int tid, int nthr,
+                                                      TileT *tile, const FillPre &p) {
+  if (p.on) {
+    int q, k;
+    const GhostSeg s = pass_seg(f.apply, p.row, q, k);
+    TileT *tl = q == f.apply.tile_seg ? tile : nullptr;
+    if (s.f32)
+      ghost_put<N, float>(s, p.op, k, static_cast<float>(p.v0), static_cast<float>(p.v1),
+                          reinterpret_cast<float *>(tl));
+    else
+      ghost_put<N, double>(s, p.op, k, p.v0, p.v1, reinterpret_cast<double *>(tl));
+  }
+  const int n = t.op_count;
+  const int total = n * f.apply.rows;
+  for (int e = tid + nthr; e < total; e += nthr) {
     const int row = e / n;
     const GhostOp op = f.ops[t.op_begin + (e - row * n)];
     int q, k;

@@ -19,6 +19,7 @@ void GhostCompiler::set(int blk, int pos, const Desc &d) {
   if (stamp_[idx] != gen_) {
     stamp_[idx] = gen_;
     touched_.push_back(static_cast<int>(idx));
+    touched_blk_.push_back(blk);
   }
   cur_[idx] = d;
 }
@@ -329,6 +330,7 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     gen_ = 1;
   }
   touched_.clear();
+  touched_blk_.clear();
   run_sequence(t, bounds);
   out.clear();
   snap_blk_.clear();
@@ -355,62 +357,71 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     if (e.blk == blk && e.pos == pos + 1) return false;  // unchanged cell
     return !overwritten(e.blk, e.pos);
   };
-  // emitted block by block (the ops of a block are consecutive, so that the
-  // block's kernel can gather them), each block's cells in position order
+  // emitted in the order of the first writes (the replay's order, which
+  // keeps consecutive gathers' sources close), then grouped by block with a
+  // stable counting sort: the ops of a block are consecutive, so that the
+  // block's kernel can gather them
   const int nb = t.lastActive;
-  blk_count_.assign(static_cast<size_t>(nb), 0);
-  for (const int idx : touched_) blk_count_[idx / nn_]++;
-  out.ops.reserve(touched_.size());
-  out.op_start.assign(static_cast<size_t>(nb) + 1, 0);
-  bool leaves = true;
-  for (int blk = 0; blk < nb; blk++) {
-    out.op_start[blk] = static_cast<int>(out.ops.size());
-    if (!blk_count_[blk]) continue;
-    for (int pos = 0; pos < nn_; pos++) {
-      const int idx = blk * nn_ + pos;
-      if (stamp_[idx] != gen_) continue;
-      const Desc &d = cur_[idx];
-      if (d.type == GOP_COPY && d.blk == blk && d.pos == pos) continue;  // unchanged
-      if (emit_stamp_[idx] == gen_) continue;                             // second cell of a pair
-      emit_stamp_[idx] = gen_;
-      GhostOp op{};
-      op.dst_slot = slot[blk];
-      op.dst_pos = static_cast<int16_t>(pos);
-      if (d.type == GOP_COPY) {
-        if (overwritten(d.blk, d.pos)) {
-          op.type = GOP_SNAP;
-          op.src_slot = snap_of(d.blk, d.pos);
-        } else {
-          op.type = GOP_COPY;
-          op.src_slot = slot[d.blk];
-          op.src_pos = d.pos;
-          if (pairs_with(blk, pos, d)) {
-            op.type = GOP_COPY2;
-            emit_stamp_[idx + 1] = gen_;
-          }
-        }
+  const size_t nt = touched_.size();
+  op_blk_.clear();
+  emitted_.clear();
+  emitted_.reserve(nt);
+  op_blk_.reserve(nt);
+  for (size_t q = 0; q < nt; q++) {
+    const int idx = touched_[q];
+    const int blk = touched_blk_[q];
+    const int pos = idx - blk * nn_;
+    const Desc &d = cur_[idx];
+    if (d.type == GOP_COPY && d.blk == blk && d.pos == pos) continue;  // unchanged
+    if (emit_stamp_[idx] == gen_) continue;                             // second cell of a pair
+    emit_stamp_[idx] = gen_;
+    GhostOp op{};
+    op.dst_slot = slot[blk];
+    op.dst_pos = static_cast<int16_t>(pos);
+    if (d.type == GOP_COPY) {
+      if (overwritten(d.blk, d.pos)) {
+        op.type = GOP_SNAP;
+        op.src_slot = snap_of(d.blk, d.pos);
       } else {
-        const int c[4] = {d.pos, d.pos + n_, d.pos + 1, d.pos + 1 + n_};  // sum_irjr order
-        bool hazard = false;
-        for (int q = 0; q < 4; q++) hazard |= overwritten(d.blk, c[q]);
-        if (!hazard) {
-          op.type = GOP_FINE;
-          op.src_slot = slot[d.blk];
-          op.src_pos = d.pos;
-        } else {  // four consecutive rows, whether or not each was saved before
-          op.type = GOP_SFINE;
-          op.src_slot = static_cast<int>(out.snaps.size());
-          for (int q = 0; q < 4; q++) {
-            out.snaps.push_back(GhostSnap{slot[d.blk], c[q]});
-            snap_blk_.push_back(d.blk);
-          }
+        op.type = GOP_COPY;
+        op.src_slot = slot[d.blk];
+        op.src_pos = d.pos;
+        if (pairs_with(blk, pos, d)) {
+          op.type = GOP_COPY2;
+          emit_stamp_[idx + 1] = gen_;
         }
       }
-      out.ops.push_back(op);
+    } else {
+      const int c[4] = {d.pos, d.pos + n_, d.pos + 1, d.pos + 1 + n_};  // sum_irjr order
+      bool hazard = false;
+      for (int k = 0; k < 4; k++) hazard |= overwritten(d.blk, c[k]);
+      if (!hazard) {
+        op.type = GOP_FINE;
+        op.src_slot = slot[d.blk];
+        op.src_pos = d.pos;
+      } else {  // four consecutive rows, whether or not each was saved before
+        op.type = GOP_SFINE;
+        op.src_slot = static_cast<int>(out.snaps.size());
+        for (int k = 0; k < 4; k++) {
+          out.snaps.push_back(GhostSnap{slot[d.blk], c[k]});
+          snap_blk_.push_back(d.blk);
+        }
+      }
     }
-    if (out.op_start[blk] != static_cast<int>(out.ops.size()) && !t.leafs[blk]) leaves = false;
+    emitted_.push_back(op);
+    op_blk_.push_back(blk);
   }
-  out.op_start[nb] = static_cast<int>(out.ops.size());
+  const size_t no = emitted_.size();
+  out.op_start.assign(static_cast<size_t>(nb) + 1, 0);
+  for (size_t q = 0; q < no; q++) out.op_start[op_blk_[q] + 1]++;
+  bool leaves = true;
+  for (int b2 = 0; b2 < nb; b2++) {
+    if (out.op_start[b2 + 1] && !t.leafs[b2]) leaves = false;
+    out.op_start[b2 + 1] += out.op_start[b2];
+  }
+  blk_count_.assign(out.op_start.begin(), out.op_start.end() - 1);  // next free op per block
+  out.ops.resize(no);
+  for (size_t q = 0; q < no; q++) out.ops[blk_count_[op_blk_[q]]++] = emitted_[q];
   // snapshots grouped by the block they save from, keeping their order
   // within a block (the four rows of an SFINE stay consecutive)
   const int ns = static_cast<int>(out.snaps.size());

@@ -68,10 +68,13 @@ class GhostCompiler {
   std::vector<uint32_t> stamp_;
   std::vector<Desc> cur_;
   std::vector<int> touched_;
+  std::vector<int> touched_blk_;      // block of each touched cell
   std::vector<uint32_t> snap_stamp_;
   std::vector<int> snap_row_;
   std::vector<uint32_t> emit_stamp_;  // cell already written by an emitted op
-  std::vector<int> blk_count_;        // touched cells per block
+  std::vector<int> blk_count_;        // next free row per block while grouping
+  std::vector<GhostOp> emitted_;      // ops in emission order
+  std::vector<int> op_blk_;           // destination block of each emitted op
   std::vector<int> snap_blk_;         // block of each snapshot row, in emission order
   std::vector<int> snap_perm_;        // emission row -> grouped row
 };

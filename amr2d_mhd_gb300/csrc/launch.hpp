@@ -78,6 +78,11 @@ cudaError_t launch_ghost(const Method &m, const GhostLaunch &g, cudaStream_t s);
 cudaError_t launch_ct_emf(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 cudaError_t launch_ct_cell(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
+// the three CT kernels of a stage with fused fills, as one cooperative launch
+// whose phases are separated by grid barriers (bar: two zeroed words)
+struct FillFuse;
+cudaError_t launch_ct_coop(const Method &m, const CtArgs &a, const FillFuse &f_emf, const FillFuse &f_face,
+                           const FillFuse &f_cell, unsigned *bar, cudaStream_t s);
 // diffusivity.cpp on the tasks flagged TASK_DIFFUSE (a.q = U after stage 2)
 cudaError_t launch_diffuse(const Method &m, const CtArgs &a, int ntasks, cudaStream_t s);
 // per-leaf max wave speed and refinement criterion from the primitive state

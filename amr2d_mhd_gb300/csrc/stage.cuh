@@ -197,6 +197,8 @@ __device__ __forceinline__ bool stage_block(const StageArgs &a, int ti, uint64_t
   // 0. the block's conserved state (8 planes, contiguous) into shared memory by TMA
   static_assert((8 * NN * sizeof(S)) % 16 == 0, "bulk copies move multiples of 16 bytes");
   if (tid == 0) bulk_stage_issue(sU, Q, static_cast<uint32_t>(8 * NN * sizeof(S)), bar);
+  // fused fill: each thread's first gather is loaded while the copy is in flight
+  const FillPre pre = fill_prefetch<N>(a.fuse, task, tid);
   const bool late = !bulk_stage_wait(bar, phase);
   if (__syncthreads_or(late)) {
     if (tid == 0) dev_fail(a.err, DERR_TIMEOUT, task.slot, 0, 0, 0.0);
@@ -206,7 +208,7 @@ __device__ __forceinline__ bool stage_block(const StageArgs &a, int ti, uint64_t
   // fused fill: the block's ghost cells of qin (and of B), into global memory
   // and over the staged copy, which held the values from before the fill
   if (a.fuse.apply.nseg) {
-    fill_apply_task<N, S>(a.fuse, task, tid, nthr, sU);
+    fill_apply_task_after<N, S>(a.fuse, task, tid, nthr, sU, pre);
     __syncthreads();
   }
 

@@ -23,8 +23,9 @@ CASES = {
 }
 
 
-def make(gpu, configs, kernel, fused):
-    env = {"AMR2D_STAGE_KERNEL": kernel, "AMR2D_FUSED_FILLS": "1" if fused else "0"}
+def make(gpu, configs, kernel, fused, coop=True):
+    env = {"AMR2D_STAGE_KERNEL": kernel, "AMR2D_FUSED_FILLS": "1" if fused else "0",
+           "AMR2D_CT_COOP": "1" if coop else "0"}
     old = {k: os.environ.get(k) for k in env}
     os.environ.update(env)
     try:
@@ -57,16 +58,21 @@ def same_state(a, b, n):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("coop", [True, False], ids=["ct_coop", "ct_3"])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_fused_fills_bit_identical(gpu, case):
+def test_fused_fills_bit_identical(gpu, case, coop):
+    """coop: the three CT kernels of a stage as one cooperative launch with
+    grid barriers (6 launches per step with the fused stage kernel)."""
     cfg, kernel, steps = CASES[case]
-    a = make(gpu, cfg, kernel, True)
+    a = make(gpu, cfg, kernel, True, coop)
     b = make(gpu, cfg, kernel, False)
     la = launches_per_step(a, steps)
     lb = launches_per_step(b, steps)
     same_state(a, b, 1)
-    print("%s: %.1f launches per step fused, %.1f unfused" % (case, la, lb))
+    print("%s %s: %.1f launches per step fused, %.1f unfused" % (case, "coop" if coop else "3 CT", la, lb))
     assert la < lb
+    if coop and kernel == "fused":
+        assert la <= 8
 
 
 @pytest.mark.gpu
@@ -80,9 +86,14 @@ def test_fused_fills_blast_batch(gpu, precision):
         c.maxlevs = min(c.maxlevs, 4)
         c.t_end = 0.004 * (i + 1)
         cfgs.append(c)
+    # each stage kernel against itself: the FP32 split and fused stage
+    # kernels round differently (FMA contraction in the fused one)
     a = make(gpu, cfgs, "fused", True)
     b = make(gpu, cfgs, "fused", False)
+    c = make(gpu, cfgs, "split", True)
+    d = make(gpu, cfgs, "split", False)
     for _ in range(4):
-        a.run(12)
-        b.run(12)
+        for sim in (a, b, c, d):
+            sim.run(12)
         same_state(a, b, len(cfgs))
+        same_state(c, d, len(cfgs))
