@@ -19,7 +19,6 @@ void GhostCompiler::set(int blk, int pos, const Desc &d) {
   if (stamp_[idx] != gen_) {
     stamp_[idx] = gen_;
     touched_.push_back(static_cast<int>(idx));
-    touched_blk_.push_back(blk);
   }
   cur_[idx] = d;
 }
@@ -329,11 +328,9 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     std::fill(emit_stamp_.begin(), emit_stamp_.end(), 0u);
     gen_ = 1;
   }
-  touched_.clear();
-  touched_blk_.clear();
-  run_sequence(t, bounds);
   out.clear();
-  snap_blk_.clear();
+  touched_.clear();
+  run_sequence(t, bounds);
   // a pre-fill value that the fill overwrites is read from a saved copy
   auto snap_of = [&](int blk, int pos) {
     const size_t idx = static_cast<size_t>(blk) * nn_ + pos;
@@ -341,7 +338,6 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
       snap_stamp_[idx] = gen_;
       snap_row_[idx] = static_cast<int>(out.snaps.size());
       out.snaps.push_back(GhostSnap{slot[blk], pos});
-      snap_blk_.push_back(blk);
     }
     return snap_row_[idx];
   };
@@ -357,21 +353,10 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     if (e.blk == blk && e.pos == pos + 1) return false;  // unchanged cell
     return !overwritten(e.blk, e.pos);
   };
-  // emitted in the order of the first writes (the replay's order, which
-  // keeps consecutive gathers' sources close), then grouped by block with a
-  // stable counting sort: the ops of a block are consecutive, so that the
-  // block's kernel can gather them
-  const int nb = t.lastActive;
-  const size_t nt = touched_.size();
-  op_blk_.clear();
-  emitted_.clear();
-  emitted_.reserve(nt);
-  op_blk_.reserve(nt);
-  for (size_t q = 0; q < nt; q++) {
-    const int idx = touched_[q];
-    const int blk = touched_blk_[q];
-    const int pos = idx - blk * nn_;
+  out.ops.reserve(touched_.size());
+  for (const int idx : touched_) {
     const Desc &d = cur_[idx];
+    const int blk = idx / nn_, pos = idx % nn_;
     if (d.type == GOP_COPY && d.blk == blk && d.pos == pos) continue;  // unchanged
     if (emit_stamp_[idx] == gen_) continue;                             // second cell of a pair
     emit_stamp_[idx] = gen_;
@@ -394,7 +379,7 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
     } else {
       const int c[4] = {d.pos, d.pos + n_, d.pos + 1, d.pos + 1 + n_};  // sum_irjr order
       bool hazard = false;
-      for (int k = 0; k < 4; k++) hazard |= overwritten(d.blk, c[k]);
+      for (int q = 0; q < 4; q++) hazard |= overwritten(d.blk, c[q]);
       if (!hazard) {
         op.type = GOP_FINE;
         op.src_slot = slot[d.blk];
@@ -402,48 +387,48 @@ void GhostCompiler::compile(const Tree &t, const std::vector<Bound> &bounds, con
       } else {  // four consecutive rows, whether or not each was saved before
         op.type = GOP_SFINE;
         op.src_slot = static_cast<int>(out.snaps.size());
-        for (int k = 0; k < 4; k++) {
-          out.snaps.push_back(GhostSnap{slot[d.blk], c[k]});
-          snap_blk_.push_back(d.blk);
-        }
+        for (int q = 0; q < 4; q++) out.snaps.push_back(GhostSnap{slot[d.blk], c[q]});
       }
     }
-    emitted_.push_back(op);
-    op_blk_.push_back(blk);
+    out.ops.push_back(op);
   }
-  const size_t no = emitted_.size();
-  out.op_start.assign(static_cast<size_t>(nb) + 1, 0);
-  for (size_t q = 0; q < no; q++) out.op_start[op_blk_[q] + 1]++;
+  group_by_block(t, slot, out);
+}
+
+// Stable counting sorts of the ops by destination block and of the
+// snapshots by the block they save from (an SFINE's four rows stay
+// consecutive), with the snapshot rows of the ops renumbered.
+void GhostCompiler::group_by_block(const Tree &t, const int *slot, GhostProgram &out) {
+  const int nb = t.lastActive;
+  int top = 0;
+  for (int b = 0; b < nb; b++) top = slot[b] > top ? slot[b] : top;
+  if (static_cast<int>(blk_of_slot_.size()) <= top) blk_of_slot_.resize(static_cast<size_t>(top) + 1);
+  for (int b = 0; b < nb; b++)
+    if (slot[b] >= 0) blk_of_slot_[slot[b]] = b;
   bool leaves = true;
-  for (int b2 = 0; b2 < nb; b2++) {
-    if (out.op_start[b2 + 1] && !t.leafs[b2]) leaves = false;
-    out.op_start[b2 + 1] += out.op_start[b2];
-  }
-  blk_count_.assign(out.op_start.begin(), out.op_start.end() - 1);  // next free op per block
-  out.ops.resize(no);
-  for (size_t q = 0; q < no; q++) out.ops[blk_count_[op_blk_[q]]++] = emitted_[q];
-  // snapshots grouped by the block they save from, keeping their order
-  // within a block (the four rows of an SFINE stay consecutive)
-  const int ns = static_cast<int>(out.snaps.size());
-  out.snap_start.assign(static_cast<size_t>(nb) + 1, 0);
-  if (ns) {
-    for (int r = 0; r < ns; r++) out.snap_start[snap_blk_[r] + 1]++;
-    for (int b2 = 0; b2 < nb; b2++) {
-      if (out.snap_start[b2 + 1] && !t.leafs[b2]) leaves = false;
-      out.snap_start[b2 + 1] += out.snap_start[b2];
+  auto sort = [&](auto &items, auto &tmp, std::vector<int> &start, auto slot_of, std::vector<int> *perm) {
+    const size_t n = items.size();
+    start.assign(static_cast<size_t>(nb) + 1, 0);
+    for (size_t q = 0; q < n; q++) start[blk_of_slot_[slot_of(items[q])] + 1]++;
+    for (int b = 0; b < nb; b++) {
+      if (start[b + 1] && !t.leafs[b]) leaves = false;
+      start[b + 1] += start[b];
     }
-    blk_count_.assign(out.snap_start.begin(), out.snap_start.end() - 1);  // next free row per block
-    snap_perm_.resize(static_cast<size_t>(ns));
-    std::vector<GhostSnap> grouped(static_cast<size_t>(ns));
-    for (int r = 0; r < ns; r++) {
-      const int g = blk_count_[snap_blk_[r]]++;
-      snap_perm_[r] = g;
-      grouped[g] = out.snaps[r];
+    count_.assign(start.begin(), start.end() - 1);
+    tmp.resize(n);
+    if (perm) perm->resize(n);
+    for (size_t q = 0; q < n; q++) {
+      const int g = count_[blk_of_slot_[slot_of(items[q])]]++;
+      tmp[g] = items[q];
+      if (perm) (*perm)[q] = g;
     }
-    out.snaps.swap(grouped);
+    items.swap(tmp);
+  };
+  sort(out.snaps, snaps_tmp_, out.snap_start, [](const GhostSnap &s) { return s.slot; }, &snap_perm_);
+  if (!out.snaps.empty())
     for (GhostOp &op : out.ops)
       if (op.type == GOP_SNAP || op.type == GOP_SFINE) op.src_slot = snap_perm_[op.src_slot];
-  }
+  sort(out.ops, ops_tmp_, out.op_start, [](const GhostOp &o) { return o.dst_slot; }, nullptr);
   out.by_block = leaves;
 }
 

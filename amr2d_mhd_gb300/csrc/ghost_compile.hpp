@@ -68,14 +68,16 @@ class GhostCompiler {
   std::vector<uint32_t> stamp_;
   std::vector<Desc> cur_;
   std::vector<int> touched_;
-  std::vector<int> touched_blk_;      // block of each touched cell
   std::vector<uint32_t> snap_stamp_;
   std::vector<int> snap_row_;
   std::vector<uint32_t> emit_stamp_;  // cell already written by an emitted op
-  std::vector<int> blk_count_;        // next free row per block while grouping
-  std::vector<GhostOp> emitted_;      // ops in emission order
-  std::vector<int> op_blk_;           // destination block of each emitted op
-  std::vector<int> snap_blk_;         // block of each snapshot row, in emission order
+  // grouping by block after the emission (kept apart from the replay and
+  // emission loops, whose speed depends on their code staying small)
+  void group_by_block(const Tree &t, const int *slot, GhostProgram &out);
+  std::vector<int> blk_of_slot_;      // inverse of `slot` for this instance's blocks
+  std::vector<int> count_;
+  std::vector<GhostOp> ops_tmp_;
+  std::vector<GhostSnap> snaps_tmp_;
   std::vector<int> snap_perm_;        // emission row -> grouped row
 };
 
