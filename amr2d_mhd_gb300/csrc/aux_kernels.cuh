@@ -254,9 +254,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, DevError *err) {
 // fills CT2D makes between them (boundaryec on the EMF, boundaryfc on the new
 // face field) are fused: gathered by the phase that consumes them, their
 // snapshots saved by the phase before.
-template <int NG, typename S>
-__global__ void __launch_bounds__(128) k_ct_coop(CtArgs a, FillFuse f_emf, FillFuse f_face, FillFuse f_cell,
-                                                 unsigned *bar) {
+template <int NG, typename S, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_ct_coop(CtArgs a, FillFuse f_emf, FillFuse f_face, FillFuse f_cell,
+                                                     unsigned *bar) {
   pdl_wait();
   constexpr int NN = Geo<NG>::NN;
   __shared__ S sp[NN], sC[NN];

@@ -79,7 +79,7 @@ Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (void *p : {U_, Us_, ff_, gg_, W_}) if (p) cudaFree(p);
   for (double *p : {Bi_, Bis_, EMF_}) if (p) cudaFree(p);
-  for (DevBuf *b : {&d_tasks_, &d_params_, &d_lambda_, &d_grad_, &d_err_, &d_snap_, &d_treeops_, &d_stage_, &d_slots_,
+  for (DevBuf *b : {&d_tasks_, &d_params_, &d_lambda_, &d_grad_, &d_err_, &d_snap_, &d_treeops_, &d_stage_,
                     &d_ctr_, &d_snap3_, &d_bar_})
     b->release();
   d_ops_.release();
@@ -88,6 +88,7 @@ Engine::~Engine() {
                     &t_UsPre_, &t_BnewF_, &t_UPre_})
     b->release();
   for (DevBuf &b : a_C_) b.release();
+  for (Instance &in : inst_) in.d_slotmap.release();
   for (DevBuf &b : ckpt_) b.release();
   for (HostBuf *b : {&h_params_, &h_lambda_, &h_grad_, &h_err_, &h_ops_, &h_snaps_, &h_tasks_})
     b->release();
@@ -159,6 +160,7 @@ int Engine::create(const amr_config *cfgs, int n) {
   if (const char *p = std::getenv("AMR2D_PDL")) m_.pdl = std::strcmp(p, "0") != 0 ? 1 : 0;
   if (const char *f = std::getenv("AMR2D_FUSED_FILLS")) fuse_fills_ = std::strcmp(f, "0") != 0;
   if (const char *f = std::getenv("AMR2D_CT_COOP")) ct_coop_ = std::strcmp(f, "0") != 0;
+  if (const char *f = std::getenv("AMR2D_ZERO_COPY")) zero_copy_ = std::strcmp(f, "0") != 0;
   if (const char *f = std::getenv("AMR2D_FACE_KERNEL"))
     m_.persistent = !std::strcmp(f, "dynamic") ? 2 : (!std::strcmp(f, "persistent") ? 1 : 0);
   ng_ = m_.ng;

@@ -61,6 +61,10 @@ struct Instance {
   uint64_t prog_version = ~0ull;
   bool prog_dirty = true;            // range not yet uploaded
   int64_t ops_off = 0, ops_cap = 0, snaps_off = 0, snaps_cap = 0;
+  // device copy of slot[0, slotmap_n) for uploads and downloads (a block's
+  // slot never changes once assigned)
+  DevBuf d_slotmap;
+  int slotmap_n = 0;
   explicit Instance(const TreeShape &s) : tree(s) {}
 };
 
@@ -167,6 +171,10 @@ class Engine {
   bool fuse_fills_ = true;         // AMR2D_FUSED_FILLS=0: every ghost fill as launches of its own
   bool fuse_ok_ = false;           // every active program is grouped by leaf block
   bool ct_coop_ = true;            // fused fills: CT2D as one cooperative launch (AMR2D_CT_COOP=0: three)
+  // uploads / downloads: the scatter / gather kernel reads / writes the
+  // caller's page-locked array itself instead of a copy through a staging
+  // buffer (AMR2D_ZERO_COPY=0: always the copy)
+  bool zero_copy_ = true;
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
   bool initialised_ = false;
@@ -191,7 +199,7 @@ class Engine {
   int compile_programs();          // recompile changed instances (host threads)
   int layout_programs(bool relayout);
   DevBuf d_tasks_, d_params_, d_lambda_, d_grad_, d_err_, d_snap_, d_ops_, d_snaps_;
-  DevBuf d_treeops_, d_stage_, d_slots_, d_ctr_;
+  DevBuf d_treeops_, d_stage_, d_ctr_;
   DevBuf d_snap3_;                 // fused fills: three rotating snapshot buffers
   DevBuf d_bar_;                   // grid barrier of the cooperative CT launch
   FillFuse dt_fuse_{};             // fused fills: the last fill of the step, gathered by the dt kernel

@@ -17,46 +17,71 @@ namespace amr {
   } while (0)
 
 // copy blocks [0, lastActive) of one field between a dense float64 host
-// array [block][var][j][i] and the slot pool.  The bulk copy goes straight
-// between the caller's (pageable) array and a device staging buffer: the
-// driver's pageable path (direct DMA on a coherent CPU-GPU link) beats a host
-// memcpy into pinned memory followed by a pinned copy; a scatter / gather
-// kernel then moves the blocks between the staging buffer and their slots.
-// A pageable host-to-device copy has read its source when it returns, so an
-// upload from pageable memory returns without waiting for the device (later
-// work on the stream is ordered after the scatter); from page-locked or
-// managed memory the copy is truly asynchronous, and the upload waits for it
-// so that the caller may reuse the array at once.  A download waits for its
-// copy.
+// array [block][var][j][i] and the slot pool.  From or into page-locked
+// memory the scatter / gather kernel reads or writes the caller's array
+// directly: one pass over the link and no staging copy (2.6 % more
+// end-to-end cell-updates/s on the rotor; for pageable memory the kernel's
+// accesses through the host page tables were 5 % slower than the copy, so
+// pageable arrays keep it).  Otherwise the bulk copy goes between the caller's array and
+// a device staging buffer (the driver's pageable path, direct DMA on a
+// coherent link, beats a host memcpy into pinned memory followed by a pinned
+// copy) and the kernel moves the blocks between the staging buffer and their
+// slots.  A pageable host-to-device copy has read its source when it
+// returns, so that upload returns without waiting for the device (later work
+// on the stream is ordered after the scatter); every other upload, and every
+// download, waits, so that the caller may reuse or read the array at once.
 int Engine::xfer(Instance &in, int field, double *host, bool to_device) {
   const int nblk = in.tree.lastActive;
   const int per = field_nv(field) * nn_;
   const size_t bytes = static_cast<size_t>(nblk) * per * sizeof(double);
   if (nblk == 0) return AMR_OK;
-  // a growing staging buffer is freed and reallocated: let an earlier
-  // upload's scatter finish reading it first
-  if (sizeof(int) * nblk > d_slots_.bytes || bytes > d_stage_.bytes) CK(cudaStreamSynchronize(stream_), "sync");
-  CK(d_slots_.ensure(sizeof(int) * nblk), "alloc");
-  CK(d_stage_.ensure(bytes), "alloc");
-  CK(cudaMemcpyAsync(d_slots_.p, in.slot.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice, stream_), "h2d");
+  if (nblk > in.slotmap_n) {  // slots are never reassigned: only new blocks need uploading
+    if (sizeof(int) * nblk > in.d_slotmap.bytes) CK(cudaStreamSynchronize(stream_), "sync");
+    CK(in.d_slotmap.ensure(sizeof(int) * nblk), "alloc");
+    // a pageable source: read by the time the call returns
+    CK(cudaMemcpyAsync(in.d_slotmap.p, in.slot.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice, stream_), "h2d");
+    prof_.h2d_bytes += static_cast<int64_t>(sizeof(int) * nblk);
+    in.slotmap_n = nblk;
+  }
+  const int *slots = in.d_slotmap.as<int>();
   void *fp = field_ptr(field);
-  if (to_device) {
-    CK(cudaMemcpyAsync(d_stage_.p, host, bytes, cudaMemcpyHostToDevice, stream_), "h2d");
-    CK(launch_scatter(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
-       "scatter");
-    prof_.h2d_bytes += static_cast<int64_t>(bytes + sizeof(int) * nblk);
-    prof_.launches += 1;
-    CK(cudaGetLastError(), "scatter");
+  // the device's view of the caller's array, if it has one
+  double *direct = nullptr;
+  bool pinned = false;
+  {
     cudaPointerAttributes pa{};
     if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
       cudaGetLastError();  // an unknown (pageable) pointer on older runtimes
     } else if (pa.type == cudaMemoryTypeHost || pa.type == cudaMemoryTypeManaged) {
-      CK(cudaStreamSynchronize(stream_), "sync");
+      pinned = true;
+      if (zero_copy_ && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+        direct = static_cast<double *>(pa.devicePointer);
     }
+  }
+  if (direct) {
+    if (to_device) {
+      CK(launch_scatter(slots, nblk, fp, field_f32(field), per, direct, stream_), "scatter");
+      prof_.h2d_bytes += static_cast<int64_t>(bytes);
+    } else {
+      CK(launch_gather(slots, nblk, fp, field_f32(field), per, direct, stream_), "gather");
+      prof_.d2h_bytes += static_cast<int64_t>(bytes);
+    }
+    prof_.launches += 1;
+    CK(cudaStreamSynchronize(stream_), "sync");
+    return AMR_OK;
+  }
+  // a growing staging buffer is freed and reallocated: let an earlier
+  // upload's scatter finish reading it first
+  if (bytes > d_stage_.bytes) CK(cudaStreamSynchronize(stream_), "sync");
+  CK(d_stage_.ensure(bytes), "alloc");
+  if (to_device) {
+    CK(cudaMemcpyAsync(d_stage_.p, host, bytes, cudaMemcpyHostToDevice, stream_), "h2d");
+    CK(launch_scatter(slots, nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_), "scatter");
+    prof_.h2d_bytes += static_cast<int64_t>(bytes);
+    prof_.launches += 1;
+    if (pinned) CK(cudaStreamSynchronize(stream_), "sync");
   } else {
-    CK(launch_gather(d_slots_.as<int>(), nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_),
-       "gather");
-    prof_.h2d_bytes += static_cast<int64_t>(sizeof(int) * nblk);
+    CK(launch_gather(slots, nblk, fp, field_f32(field), per, d_stage_.as<double>(), stream_), "gather");
     prof_.d2h_bytes += static_cast<int64_t>(bytes);
     prof_.launches += 1;
     CK(cudaMemcpyAsync(host, d_stage_.p, bytes, cudaMemcpyDeviceToHost, stream_), "d2h");
