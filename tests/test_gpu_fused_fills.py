@@ -20,12 +20,14 @@ CASES = {
                             diffusion=True), "fused", 30),
     "ot_periodic": (dict(ic="OT", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=4, nroots=(3, 3), periodic=True,
                          geom_ref=False, lenx=2 * np.pi, leny=2 * np.pi), "split", 25),
+    "bwx_weno5_fp32_fused": (dict(ic="BWx", limiter="WENO5", flux="HLLD", cfl=0.4, maxlevs=4, nghosts=4,
+                                  precision="fp32"), "fused", 25),
 }
 
 
-def make(gpu, configs, kernel, fused, coop=True):
+def make(gpu, configs, kernel, fused, coop=True, graphs=True):
     env = {"AMR2D_STAGE_KERNEL": kernel, "AMR2D_FUSED_FILLS": "1" if fused else "0",
-           "AMR2D_CT_COOP": "1" if coop else "0"}
+           "AMR2D_CT_COOP": "1" if coop else "0", "AMR2D_GRAPHS": "1" if graphs else "0"}
     old = {k: os.environ.get(k) for k in env}
     os.environ.update(env)
     try:
@@ -97,3 +99,18 @@ def test_fused_fills_blast_batch(gpu, precision):
             sim.run(12)
         same_state(a, b, len(cfgs))
         same_state(c, d, len(cfgs))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["fused", "split"])
+def test_fused_fills_without_graphs(gpu, kernel):
+    """The fused step launched kernel by kernel (no captured graph) equals the
+    captured one, and the separate fills."""
+    cfg = dict(ic="rotor", limiter="MC", flux="HLLD", cfl=0.4, maxlevs=5)
+    a = make(gpu, cfg, kernel, True, graphs=False)
+    b = make(gpu, cfg, kernel, True)
+    c = make(gpu, cfg, kernel, False)
+    for sim in (a, b, c):
+        sim.run(30)
+    same_state(a, b, 1)
+    same_state(a, c, 1)
