@@ -78,20 +78,55 @@ __device__ __forceinline__ void cons2prim_cell<double>(const double *u, double *
   w[4] = p - (g - 1) * (0.5 * (u[5] * u[5] + u[6] * u[6] + u[7] * u[7]));
 }
 
+// a^2 + b^2 + c^2 of FP32 values as an unevaluated sum hi + lo, exact to
+// about 2^-48 relative: each square split exactly by an FMA (Dekker's
+// product) and the partial sums by Knuth's TwoSum, with the error terms
+// summed in FP32.  The _rn intrinsics keep the compiler from fusing or
+// reordering the steps.
+__device__ __forceinline__ void sum_sq3(float a, float b, float c, float &hi, float &lo) {
+  const float pa = __fmul_rn(a, a), pb = __fmul_rn(b, b), pc = __fmul_rn(c, c);
+  const float ea = __fmaf_rn(a, a, -pa), eb = __fmaf_rn(b, b, -pb), ec = __fmaf_rn(c, c, -pc);
+  const float s1 = __fadd_rn(pa, pb), v1 = __fsub_rn(s1, pa);
+  const float t1 = __fadd_rn(__fsub_rn(pa, __fsub_rn(s1, v1)), __fsub_rn(pb, v1));
+  const float s2 = __fadd_rn(s1, pc), v2 = __fsub_rn(s2, s1);
+  const float t2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, v2)), __fsub_rn(pc, v2));
+  hi = s2;
+  lo = __fadd_rn(__fadd_rn(__fadd_rn(ea, eb), ec), __fadd_rn(t1, t2));
+}
+
 // FP32 path: the pressure recovered from the total energy in FP64 (the
-// cancellation E - |m|^2/2rho - |B|^2/2 is where FP32 loses digits), with
-// 1/rho from the FP32 reciprocal refined by one FP64 Newton step instead of
-// FP64 divisions (FP64 runs at 1/64 of the FP32 rate); the velocities in FP32
-// from the same FP32 reciprocal.
+// cancellation E - |m|^2/2rho - |B|^2/2 is where FP32 loses digits).  The
+// sums of squares |m|^2 and |B|^2 come from the FP32 pipe as hi + lo pairs
+// (sum_sq3) and are added in FP64; 1/rho is the FP32 reciprocal refined by
+// one FP64 Newton step; then E - (|m|^2/rho + |B|^2)/2 and the factor
+// gamma - 1 in FP64.  On this GPU FP64 runs at 1/64 of the FP32 rate: this
+// takes about half the FP64 operations of squaring and summing in FP64.
+// The velocities are the FP32 momenta times the FP32 reciprocal.  (A
+// component above ~1.8e19 overflows its FP32 square; such a state is out of
+// the FP32 path's range in any case.)  AMR_PRESSURE_DF=0 restores the FP64
+// squares and sums.
+#ifndef AMR_PRESSURE_DF
+#define AMR_PRESSURE_DF 1
+#endif
 template <>
 __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, double g) {
   const float ir = 1.0f / u[0];
   double ird = static_cast<double>(ir);
+#if AMR_PRESSURE_DF
+  ird = __fma_rn(ird, __fma_rn(-static_cast<double>(u[0]), ird, 1.0), ird);
+  float mh, ml, bh, bl;
+  sum_sq3(u[1], u[2], u[3], mh, ml);
+  sum_sq3(u[5], u[6], u[7], bh, bl);
+  const double m2 = static_cast<double>(mh) + static_cast<double>(ml);
+  const double b2 = static_cast<double>(bh) + static_cast<double>(bl);
+  double p = (g - 1) * (static_cast<double>(u[4]) - 0.5 * (m2 * ird + b2));
+#else
   ird = ird * (2.0 - static_cast<double>(u[0]) * ird);
   const double mx = u[1], my = u[2], mz = u[3];
   const double bx = u[5], by = u[6], bz = u[7];
   double p = (g - 1) * (static_cast<double>(u[4]) - 0.5 * (mx * mx + my * my + mz * mz) * ird) -
              (g - 1) * (0.5 * (bx * bx + by * by + bz * bz));
+#endif
   // positivity fix of the FP32 path: the FP32 conserved state can put the
   // recovered pressure below zero where the FP64 path stays positive
   if (!(p > kPressureFloor)) p = kPressureFloor;
