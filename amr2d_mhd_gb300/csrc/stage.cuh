@@ -96,23 +96,38 @@ __device__ __forceinline__ void sum_sq3(float a, float b, float c, float &hi, fl
 
 // FP32 path: the pressure recovered from the total energy in FP64 (the
 // cancellation E - |m|^2/2rho - |B|^2/2 is where FP32 loses digits).  The
-// sums of squares |m|^2 and |B|^2 come from the FP32 pipe as hi + lo pairs
-// (sum_sq3) and are added in FP64; 1/rho is the FP32 reciprocal refined by
-// one FP64 Newton step; then E - (|m|^2/rho + |B|^2)/2 and the factor
-// gamma - 1 in FP64.  On this GPU FP64 runs at 1/64 of the FP32 rate: this
-// takes about half the FP64 operations of squaring and summing in FP64.
+// sums of squares |m|^2 and |B|^2 and the quotient |m|^2/rho come from the
+// FP32 pipe as hi + lo pairs (sum_sq3, and the product with 1/rho = ir + rl),
+// accurate to ~2^-45, and are widened to FP64 only for E - (|m|^2/rho +
+// |B|^2)/2 and the factor gamma - 1.  On this GPU FP64 runs at 1/64 of the
+// FP32 rate: this takes a third of the FP64 operations of squaring, summing
+// and dividing in FP64.  AMR_PRESSURE_DF=1: |m|^2/rho with 1/rho refined by
+// one FP64 Newton step instead.
 // The velocities are the FP32 momenta times the FP32 reciprocal.  (A
 // component above ~1.8e19 overflows its FP32 square; such a state is out of
 // the FP32 path's range in any case.)  AMR_PRESSURE_DF=0 restores the FP64
 // squares and sums.
 #ifndef AMR_PRESSURE_DF
-#define AMR_PRESSURE_DF 1
+#define AMR_PRESSURE_DF 2
 #endif
 template <>
 __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, double g) {
   const float ir = 1.0f / u[0];
+#if AMR_PRESSURE_DF == 2
+  // |m|^2 / rho as hi + lo on the FP32 pipe too: 1/rho = ir + rl (rl from the
+  // FMA residual 1 - rho*ir, ~2^-45 relative), the product of the two pairs
+  // with Dekker's exact error term
+  const float rl = __fmul_rn(__fmaf_rn(-u[0], ir, 1.0f), ir);
+  float mh, ml, bh, bl;
+  sum_sq3(u[1], u[2], u[3], mh, ml);
+  sum_sq3(u[5], u[6], u[7], bh, bl);
+  const float kh = __fmul_rn(mh, ir);
+  const float kl = __fadd_rn(__fmaf_rn(mh, ir, -kh), __fadd_rn(__fmul_rn(mh, rl), __fmul_rn(ml, ir)));
+  double p = (g - 1) * (static_cast<double>(u[4]) -
+                        0.5 * ((static_cast<double>(kh) + static_cast<double>(kl)) +
+                               (static_cast<double>(bh) + static_cast<double>(bl))));
+#elif AMR_PRESSURE_DF
   double ird = static_cast<double>(ir);
-#if AMR_PRESSURE_DF
   ird = __fma_rn(ird, __fma_rn(-static_cast<double>(u[0]), ird, 1.0), ird);
   float mh, ml, bh, bl;
   sum_sq3(u[1], u[2], u[3], mh, ml);
@@ -121,6 +136,7 @@ __device__ __forceinline__ void cons2prim_cell<float>(const float *u, float *w, 
   const double b2 = static_cast<double>(bh) + static_cast<double>(bl);
   double p = (g - 1) * (static_cast<double>(u[4]) - 0.5 * (m2 * ird + b2));
 #else
+  double ird = static_cast<double>(ir);
   ird = ird * (2.0 - static_cast<double>(u[0]) * ird);
   const double mx = u[1], my = u[2], mz = u[3];
   const double bx = u[5], by = u[6], bz = u[7];
