@@ -133,10 +133,14 @@ cudaError_t launch_ct_face(const Method &m, const CtArgs &a, int n, cudaStream_t
 cudaError_t launch_ct_coop(const Method &m, const CtArgs &a, const FillFuse &f_emf, const FillFuse &f_face,
                            const FillFuse &f_cell, unsigned *bar, cudaStream_t s) {
   if (a.ntasks <= 0) return cudaSuccess;
-  // 128 threads per CTA: 256 measured 3 % slower on the FP32 batches
+  // 128 threads per CTA: 256 measured 3 % slower on the FP32 batches, 64
+  // 1-3 % slower on the FP32 64-rotor batch and the FP64 rotor
   static int per_sm[2][2] = {{0, 0}, {0, 0}}, sms = 0;
   const int gi = m.ng == 2 ? 0 : 1, si = m.f32 ? 1 : 0;
-  constexpr int threads = 128;
+#ifndef AMR_CT_COOP_THREADS
+#define AMR_CT_COOP_THREADS 128
+#endif
+  constexpr int threads = AMR_CT_COOP_THREADS;
   void (*k)(CtArgs, FillFuse, FillFuse, FillFuse, unsigned *) =
       m.ng == 2 ? (m.f32 ? k_ct_coop<2, float, threads> : k_ct_coop<2, double, threads>)
                 : (m.f32 ? k_ct_coop<4, float, threads> : k_ct_coop<4, double, threads>);
