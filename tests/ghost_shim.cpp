@@ -93,6 +93,80 @@ extern "C" int ghost_shim_apply(int last_active, const int *lp, const int *icoor
   return 0;
 }
 
+// The fill as the fused kernels run it: every block's snapshots saved first
+// (by the kernel before), then each block's gathers applied in place, one
+// block after another in a shuffled order (the CTAs of the consuming
+// kernel), each write visible at once.  The result equals the sequential
+// walk only if no gather reads a cell that another block's gathers write.
+extern "C" int ghost_shim_apply_fused(int last_active, const int *lp, const int *icoord, const unsigned char *leafs,
+                                      int maxlevs, int nrx, int nry, int periodic, int ng, int kind, int nv,
+                                      double *field, unsigned seed) {
+  using namespace amr;
+  TreeShape s{16, 16, ng, maxlevs, nrx, nry, periodic != 0};
+  Tree t(s);
+  if (last_active > t.maxblocks()) return -1;
+  t.lastActive = last_active;
+  for (int b = 0; b < last_active; b++) {
+    for (int q = 0; q < 8; q++) t.lp[b][q] = lp[8 * b + q];
+    t.icoord[b] = {icoord[2 * b], icoord[2 * b + 1]};
+    t.leafs[b] = leafs[b];
+  }
+  std::vector<Bound> bounds;
+  t.locate_bounds(bounds);
+  const int n = 16 + 2 * ng, nn = n * n;
+  std::vector<int> slot(last_active);
+  for (int b = 0; b < last_active; b++) slot[b] = b;
+  GhostCompiler gc(n, ng);
+  GhostProgram p;
+  gc.compile(t, bounds, slot.data(), p);
+  if (!p.by_block) return -4;
+  std::vector<int> order(last_active);
+  for (int b = 0; b < last_active; b++) order[b] = b;
+  auto shuffle = [&]() {  // Fisher-Yates with a small LCG (deterministic per seed)
+    for (int b = last_active - 1; b > 0; b--) {
+      seed = seed * 1664525u + 1013904223u;
+      std::swap(order[b], order[(seed >> 8) % static_cast<unsigned>(b + 1)]);
+    }
+  };
+  std::vector<double> snap(p.snaps.size() * 8);
+  shuffle();
+  for (int b : order)
+    for (int r = p.snap_start[b]; r < p.snap_start[b + 1]; r++)
+      for (int k = 0; k < nv; k++)
+        snap[static_cast<size_t>(r) * 8 + k] =
+            field[(static_cast<size_t>(p.snaps[r].slot) * nv + k) * nn + p.snaps[r].pos];
+  auto fine = [&](int k, double a00, double a01, double a10, double a11) {
+    double v = 0.;
+    if (kind == FILL_CC) { v += a00; v += a01; v += a10; v += a11; return 0.25 * v; }
+    if (kind == FILL_FC) { v += a00; v += k == 0 ? a01 : a10; return 0.5 * v; }
+    return a00;
+  };
+  shuffle();
+  for (int b : order)
+    for (int o = p.op_start[b]; o < p.op_start[b + 1]; o++) {
+      const GhostOp &op = p.ops[o];
+      for (int k = 0; k < nv; k++) {
+        const double *src = field + (static_cast<size_t>(op.src_slot) * nv + k) * nn + op.src_pos;
+        const double *r = snap.data() + static_cast<size_t>(op.src_slot) * 8 + k;
+        double *dst = field + (static_cast<size_t>(op.dst_slot) * nv + k) * nn + op.dst_pos;
+        if (op.type == GOP_COPY2) {
+          const double v0 = src[0], v1 = src[1];
+          dst[0] = v0;
+          dst[1] = v1;
+        } else if (op.type == GOP_COPY) {
+          dst[0] = src[0];
+        } else if (op.type == GOP_SNAP) {
+          dst[0] = r[0];
+        } else if (op.type == GOP_FINE) {
+          dst[0] = fine(k, src[0], src[n], src[1], src[1 + n]);
+        } else {
+          dst[0] = fine(k, r[0], r[8], r[16], r[24]);
+        }
+      }
+    }
+  return 0;
+}
+
 // the product's Tree::admesh on a given tree and per-block criterion (or,
 // with grad NULL, Tree::admesh_marked on the marks mref / mcrs); writes the
 // new tree back and returns the number of refine and coarsen operations

@@ -31,6 +31,8 @@ def lib():
         L.tree_shim_admesh.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int] + \
             [ctypes.c_void_p] * 4
         L.ghost_shim_last_by_block.argtypes = []
+        L.ghost_shim_apply_fused.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 7 + \
+            [ctypes.c_void_p, ctypes.c_uint]
         L.host_pool_shim.argtypes = [ctypes.c_int] * 3
         L.tree_shim_check.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 5 + \
             [ctypes.c_char_p, ctypes.c_int]
@@ -49,6 +51,19 @@ def ghost_apply(st, kind, nv, field, maxlevs, ng=2, nroots=(2, 2), periodic=Fals
                                 ctypes.byref(no), ctypes.byref(ns))
     assert rc == 0
     return a, no.value, ns.value
+
+
+def ghost_apply_fused(st, kind, nv, field, maxlevs, seed, ng=2, nroots=(2, 2), periodic=False):
+    """The compiled fill applied block by block in a shuffled order, in place
+    (as the fused kernels apply it), after every block's snapshots."""
+    a = np.array(field, dtype=np.float64, copy=True)
+    lp = np.ascontiguousarray(st["lp"], np.int32)
+    ic = np.ascontiguousarray(st["icoord"], np.int32)
+    lf = np.ascontiguousarray(st["leafs"].astype(np.uint8))
+    rc = lib().ghost_shim_apply_fused(st["lastActive"], lp.ctypes.data, ic.ctypes.data, lf.ctypes.data, maxlevs,
+                                      nroots[0], nroots[1], int(periodic), ng, kind, nv, a.ctypes.data, seed)
+    assert rc == 0, rc
+    return a
 
 
 def last_by_block():

@@ -5,7 +5,7 @@ import pytest
 
 from oracle import pyoracle as P
 from parity_util import oracle_kw
-from shim import admesh, ghost_apply, host_pool, last_by_block, tree_check
+from shim import admesh, ghost_apply, ghost_apply_fused, host_pool, last_by_block, tree_check
 
 GHOST_CASES = [("BWx", "MC", 4, 2, 3), ("rotor", "MC", 5, 2, 30), ("BWx", "WENO5", 3, 4, 10),
                ("rotor", "WENO5", 3, 4, 25)]
@@ -28,6 +28,24 @@ def test_ghost_program_matches_sequential_fill(ic, lim, L, ng, steps):
         # grouped by block (checked inside the shim), all in leaves: the fills
         # can run inside the step's per-block kernels
         assert last_by_block() == 1
+
+
+@pytest.mark.parametrize("ic,lim,L,ng,steps", GHOST_CASES)
+def test_fused_fill_order_free(ic, lim, L, ng, steps):
+    """The fill as the fused kernels apply it (all snapshots first, then each
+    block's gathers in place, blocks in any order) equals the sequential walk:
+    no gather reads a cell that another block's gathers write."""
+    o = P.Oracle(ic=ic, limiter=lim, flux="RUSA", cfl=0.4, maxlevs=L, nghosts=ng).init()
+    for _ in range(steps):
+        o.step()
+    st = o.state()
+    n = 16 + 2 * ng
+    rng = np.random.default_rng(steps + 7)
+    for kind, nv in [(0, 8), (1, 2), (2, 1)]:
+        f = rng.standard_normal((st["lastActive"], nv, n, n))
+        ref = o.fill(f, kind)
+        for seed in (1, 2, 3):
+            assert np.array_equal(ghost_apply_fused(st, kind, nv, f, L, seed, ng), ref), (kind, seed)
 
 
 @pytest.mark.parametrize("seed,periodic", [(11, False), (12, False), (13, True)])
@@ -53,8 +71,10 @@ def test_ghost_program_on_random_mark_trees(seed, periodic):
         for kind, nv in [(0, 8), (1, 2), (2, 1)]:
             f = rng.standard_normal((st["lastActive"], nv, 20, 20))
             got, _, _ = ghost_apply(st, kind, nv, f, L, 2, nroots, periodic)
-            assert np.array_equal(o.fill(f, kind), got), (it, kind)
+            ref = o.fill(f, kind)
+            assert np.array_equal(ref, got), (it, kind)
             assert last_by_block() == 1
+            assert np.array_equal(ghost_apply_fused(st, kind, nv, f, L, seed + it, 2, nroots, periodic), ref)
 
 
 def test_ghost_program_periodic_16_roots():
