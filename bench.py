@@ -426,6 +426,7 @@ def run_batch(stream, steps, advance):
                          step_gpu_ms_per_step=p["step_gpu_ms"] / steps,
                          stage_kernel_ms_per_step=p["stage_ms"] / steps,
                          gpu_launches=int(p["launches"]),
+                         launches_per_step=round(int(p["launches"]) / max(int(p["steps"]), 1), 2),
                          schedule=next((l[2:] for l in tune.splitlines() if l.startswith("*")), "default"))
         sim.close()
     l1 = []
@@ -901,6 +902,7 @@ def main():
         "cpu_baseline": cpu,
         "clocks": {"sm_mhz": clk.get("sm_mhz"), "sm_max_mhz": clk.get("sm_max_mhz"), "reasons": clk.get("reasons", [])},
         "gpu_launches": int(prof["launches"]),
+        "launches_per_step": round(int(prof["launches"]) / max(int(prof["steps"]), 1), 2),
     }
     print(json.dumps(line))
     return 0
