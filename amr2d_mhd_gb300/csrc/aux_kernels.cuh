@@ -253,7 +253,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, DevError *err) {
 // tasks blockIdx.x, + gridDim.x, ...), separated by grid barriers.  The two
 // fills CT2D makes between them (boundaryec on the EMF, boundaryfc on the new
 // face field) are fused: gathered by the phase that consumes them, their
-// snapshots saved by the phase before.
+// snapshots saved by the phase before.  The EMF phase also gathers the fill
+// of the fluxes and face field that precedes CT2D (main.cpp:161-163), and
+// the cell phase saves the snapshots of the cell fill that follows it.
 template <int NG, typename S, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_ct_coop(CtArgs a, FillFuse f_emf, FillFuse f_face, FillFuse f_cell,
                                                      unsigned *bar) {
